@@ -1,0 +1,685 @@
+// CPU FP64 oracle for the monitored-circuit trajectory path.
+//
+// TEST INFRASTRUCTURE. Only the tests, __graft_entry__.smoke() and bench.py's
+// CPU-baseline / reference arm load this library, and only as the checker or
+// as the timed CPU baseline; the product never calls it.
+//
+// This is a restatement, written for this project, of the reference's
+// algorithm (paths are inside the reference project):
+//   * seeding: splitmix64 and trajectory_seed   cpp/include/mipt/types.hpp:262-273
+//     two mt19937 streams per trajectory         cpp/include/mipt/circuit.hpp:129-140
+//   * Haar brickwork layer draw                  cpp/include/mipt/circuits/haar.hpp:226-305
+//     (gates of a layer first, then Bernoulli(p) measurement flags per site;
+//     odd layers close the ring with bond (n-1, 0) when closed)
+//   * Haar U(4): Gram-Schmidt of four complex   cpp/include/mipt/circuits/haar.hpp:39-85
+//     Gaussian columns, row-major, bit 0 = q0. The reference then runs a
+//     cosine-sine decomposition and rebuilds the 4x4 from it
+//     (cpp/include/mipt/cusv/gates.hpp:139-173); the rebuilt matrix equals the
+//     drawn unitary to ~1e-15, so the oracle applies the drawn unitary itself
+//     and keeps only the decomposition's retry rule (haar.hpp:171-181,211-224).
+//   * joint layer measurement: chunks of <=16 sites in ascending order, one
+//     U(0,1) per chunk, histogram bin i has bit j = outcome of chunk site j,
+//     linear CDF scan, starved-bin fallback, collapse scaled by
+//     1/sqrt(branch weight)                      cpp/include/mipt/cusv/engine.hpp:293-368
+//   * sequential single-site measurement         cpp/include/mipt/free_energy_measure.hpp:18-96
+//   * reduced density matrix of any kept-mode list, qubit or fermionic trace
+//                                                cpp/include/mipt/tmi/linalg.hpp:1098-1142,
+//                                                cpp/include/mipt/cuda/schmidt_gram.cuh:196-249
+//   * entropies in bits with the 1e-15 eigenvalue cut and 1e-12 zero snap
+//                                                cpp/include/mipt/tmi/linalg.hpp:125-141,201-208
+//   * TMI over four contiguous cyclic quarters   cpp/include/mipt/tmi/compute.hpp:186-227
+//   * three-site RDMs on the periodic ring       cpp/include/mipt/rdm.hpp:92-106,149-305
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <stdexcept>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using cd = std::complex<double>;
+
+namespace
+{
+std::uint64_t mix64(std::uint64_t v)
+{
+    v += 0x9e3779b97f4a7c15ull;
+    v = (v ^ (v >> 30)) * 0xbf58476d1ce4e5b9ull;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebull;
+    return v ^ (v >> 31);
+}
+
+void seed_pair(std::uint64_t s, std::mt19937 &gates, std::mt19937 &meas)
+{
+    std::seed_seq a{static_cast<std::uint32_t>(s), static_cast<std::uint32_t>(s >> 32)};
+    gates.seed(a);
+    const std::uint64_t m = mix64(s ^ 0xa0761d0dull);
+    std::seed_seq b{static_cast<std::uint32_t>(m), static_cast<std::uint32_t>(m >> 32)};
+    meas.seed(b);
+}
+
+// One Haar U(4) (row-major), redrawn while its cosine-sine split would be
+// singular, exactly as often as the reference redraws.
+std::array<cd, 16> draw_u4(std::mt19937 &rng)
+{
+    for (;;)
+    {
+        std::normal_distribution<double> gauss(0.0, 1.0);
+        std::array<cd, 16> q{};
+        for (int c = 0; c < 4; ++c)
+        {
+            cd v[4];
+            for (int r = 0; r < 4; ++r)
+            {
+                // The reference writes cd(normal(rng), normal(rng)); the order
+                // in which those two arguments are evaluated is unspecified in
+                // C++, and the g++ build that serves as the parity record
+                // evaluates the imaginary part first. Draw in that order
+                // explicitly.
+                const double im = gauss(rng);
+                const double re = gauss(rng);
+                v[r] = cd(re, im);
+            }
+            for (int k = 0; k < c; ++k)
+            {
+                cd dot = 0.0;
+                for (int r = 0; r < 4; ++r) dot += std::conj(q[r * 4 + k]) * v[r];
+                for (int r = 0; r < 4; ++r) v[r] -= q[r * 4 + k] * dot;
+            }
+            double nn = 0.0;
+            for (int r = 0; r < 4; ++r) nn += std::norm(v[r]);
+            const double len = std::sqrt(nn);
+            if (len < 1e-14)
+            {
+                --c;
+                continue;
+            }
+            for (int r = 0; r < 4; ++r) q[r * 4 + c] = v[r] / len;
+        }
+        // Singular-value check of the top-left 2x2 block X: eigenvalues of
+        // X^H X are the squared cosines; a cosine or sine below 1e-12 makes
+        // the reference discard the draw.
+        const cd x00 = q[0], x01 = q[1], x10 = q[4], x11 = q[5];
+        const double h00 = std::norm(x00) + std::norm(x10);
+        const double h11 = std::norm(x01) + std::norm(x11);
+        const cd h01 = std::conj(x00) * x01 + std::conj(x10) * x11;
+        const double disc = std::sqrt(std::max(0.0, (h00 - h11) * (h00 - h11) + 4.0 * std::norm(h01)));
+        const double l0 = std::clamp(0.5 * (h00 + h11 + disc), 0.0, 1.0);
+        const double l1 = std::clamp(0.5 * (h00 + h11 - disc), 0.0, 1.0);
+        const double eps = 1e-12;
+        if (std::sqrt(l0) < eps || std::sqrt(l1) < eps || std::sqrt(std::max(0.0, 1.0 - l0)) < eps ||
+            std::sqrt(std::max(0.0, 1.0 - l1)) < eps)
+            continue;
+        return q;
+    }
+}
+
+struct Layer
+{
+    std::vector<int> q;          // 2 per gate
+    std::vector<cd> m;           // 16 per gate
+    std::vector<int> sites;      // measured sites, ascending
+};
+
+void draw_layer(Layer &L, int n, int start, double p, bool closed, std::mt19937 &rng)
+{
+    const int stop = (closed && start == 1 && n > 2) ? n : n - 1;
+    L.q.clear();
+    L.m.clear();
+    L.sites.clear();
+    for (int i = start; i < stop; i += 2)
+    {
+        const auto u = draw_u4(rng);
+        L.q.push_back(i);
+        L.q.push_back((i + 1) % n);
+        L.m.insert(L.m.end(), u.begin(), u.end());
+    }
+    if (p >= 1.0)
+    {
+        for (int s = 0; s < n; ++s) L.sites.push_back(s);
+    }
+    else if (p > 0.0)
+    {
+        std::bernoulli_distribution flag(p);
+        for (int s = 0; s < n; ++s)
+            if (flag(rng)) L.sites.push_back(s);
+    }
+}
+
+void draw_trajectory(std::vector<Layer> &layers, std::uint64_t seed, int n, int periods, double p,
+                     bool closed, std::mt19937 &meas)
+{
+    if (n % 2 != 0) throw std::invalid_argument("Haar brickwork needs even n");
+    std::mt19937 gates;
+    seed_pair(seed, gates, meas);
+    layers.resize(2 * periods);
+    for (int t = 0; t < 2 * periods; ++t) draw_layer(layers[t], n, t & 1, p, closed, gates);
+}
+
+// psi <- U psi on (q0, q1); U row-major with index bit 0 = q0, bit 1 = q1.
+void apply_bond(cd *psi, int n, int q0, int q1, const cd *U)
+{
+    const std::uint64_t a = 1ull << q0, b = 1ull << q1;
+    const std::uint64_t lo = std::min(a, b), hi = std::max(a, b);
+    const std::uint64_t groups = 1ull << (n - 2);
+    for (std::uint64_t g = 0; g < groups; ++g)
+    {
+        std::uint64_t base = g;
+        base = ((base & ~(lo - 1)) << 1) | (base & (lo - 1));
+        base = ((base & ~(hi - 1)) << 1) | (base & (hi - 1));
+        const std::uint64_t idx[4] = {base, base | a, base | b, base | a | b};
+        cd in[4];
+        for (int c = 0; c < 4; ++c) in[c] = psi[idx[c]];
+        for (int r = 0; r < 4; ++r)
+        {
+            cd acc = 0.0;
+            for (int c = 0; c < 4; ++c) acc += U[r * 4 + c] * in[c];
+            psi[idx[r]] = acc;
+        }
+    }
+}
+
+// Joint measurement of `sites` (ascending) in chunks; returns the layer's
+// surprisal -log P. `forced` (optional) replays recorded outcomes instead of
+// sampling; `probs` (optional) receives each chunk's branch/total.
+double measure_layer(cd *psi, int n, const std::vector<int> &sites, int chunk_bits,
+                     const double *uniforms, int &u_used, const int *forced, int *outcomes)
+{
+    double surprisal = 0.0;
+    const std::uint64_t dim = 1ull << n;
+    std::vector<double> bins;
+    for (std::size_t begin = 0; begin < sites.size(); begin += chunk_bits)
+    {
+        const std::size_t end = std::min(sites.size(), begin + static_cast<std::size_t>(chunk_bits));
+        const int m = static_cast<int>(end - begin);
+        bins.assign(1ull << m, 0.0);
+        for (std::uint64_t x = 0; x < dim; ++x)
+        {
+            std::uint64_t bin = 0;
+            for (int j = 0; j < m; ++j) bin |= ((x >> sites[begin + j]) & 1ull) << j;
+            bins[bin] += std::norm(psi[x]);
+        }
+        double total = 0.0;
+        for (double v : bins) total += v;
+        if (!(total > 0.0) || !std::isfinite(total)) throw std::runtime_error("zero-norm state");
+        const double u = uniforms[u_used++];
+        std::uint64_t chosen = bins.size() - 1;
+        if (forced)
+        {
+            chosen = 0;
+            for (int j = 0; j < m; ++j) chosen |= static_cast<std::uint64_t>(forced[begin + j] & 1) << j;
+        }
+        else
+        {
+            const double draw = u * total;
+            double run = 0.0;
+            for (std::uint64_t i = 0; i < bins.size(); ++i)
+            {
+                run += bins[i];
+                if (draw < run)
+                {
+                    chosen = i;
+                    break;
+                }
+            }
+        }
+        double branch = bins[chosen];
+        if (!(branch > 0.0))
+        {
+            if (forced) throw std::runtime_error("forced outcome has zero weight");
+            chosen = static_cast<std::uint64_t>(std::max_element(bins.begin(), bins.end()) - bins.begin());
+            branch = bins[chosen];
+            if (!(branch > 0.0)) throw std::runtime_error("no outcome with positive weight");
+        }
+        for (int j = 0; j < m; ++j) outcomes[begin + j] = static_cast<int>((chosen >> j) & 1ull);
+        surprisal += -std::log(branch / total);
+        const double scale = 1.0 / std::sqrt(branch);
+        for (std::uint64_t x = 0; x < dim; ++x)
+        {
+            std::uint64_t bin = 0;
+            for (int j = 0; j < m; ++j) bin |= ((x >> sites[begin + j]) & 1ull) << j;
+            psi[x] = (bin == chosen) ? psi[x] * scale : cd(0.0, 0.0);
+        }
+    }
+    return surprisal;
+}
+
+// rho[row*D + col] = sum_env M[row, env] conj(M[col, env]); row bit k <-> kept[k],
+// env index over the complement in ascending mode order; fermionic trace flips
+// the sign of M[row, env] once per occupied environment mode below each
+// occupied kept mode.
+void rdm(const cd *psi, int n, const int *kept, int k, bool fermion, cd *rho)
+{
+    std::vector<int> env;
+    std::vector<char> is_kept(n, 0);
+    for (int i = 0; i < k; ++i)
+    {
+        if (kept[i] < 0 || kept[i] >= n || is_kept[kept[i]]) throw std::invalid_argument("bad kept modes");
+        is_kept[kept[i]] = 1;
+    }
+    for (int q = 0; q < n; ++q)
+        if (!is_kept[q]) env.push_back(q);
+    const std::uint64_t D = 1ull << k, E = 1ull << env.size();
+    std::vector<std::uint64_t> roff(D), cross(D, 0);
+    std::vector<std::uint64_t> below(k, 0);
+    for (int i = 0; i < k; ++i)
+        for (std::size_t e = 0; e < env.size(); ++e)
+            if (env[e] < kept[i]) below[i] |= 1ull << e;
+    for (std::uint64_t r = 0; r < D; ++r)
+    {
+        std::uint64_t o = 0, c = 0;
+        for (int i = 0; i < k; ++i)
+            if ((r >> i) & 1ull)
+            {
+                o |= 1ull << kept[i];
+                c ^= below[i];
+            }
+        roff[r] = o;
+        cross[r] = c;
+    }
+    std::fill(rho, rho + D * D, cd(0.0, 0.0));
+    std::vector<cd> col(D);
+    for (std::uint64_t e = 0; e < E; ++e)
+    {
+        std::uint64_t eo = 0;
+        for (std::size_t j = 0; j < env.size(); ++j)
+            if ((e >> j) & 1ull) eo |= 1ull << env[j];
+        for (std::uint64_t r = 0; r < D; ++r)
+        {
+            cd v = psi[eo | roff[r]];
+            if (fermion && (__builtin_popcountll(e & cross[r]) & 1)) v = -v;
+            col[r] = v;
+        }
+        for (std::uint64_t r = 0; r < D; ++r)
+            for (std::uint64_t c = 0; c < D; ++c) rho[r * D + c] += col[r] * std::conj(col[c]);
+    }
+}
+
+// Eigenvalues of a Hermitian matrix (row-major, destroyed) by cyclic complex
+// Jacobi rotations, to full double accuracy.
+void eig_hermitian(std::vector<cd> &a, int n, std::vector<double> &w)
+{
+    for (int i = 0; i < n; ++i)
+    {
+        a[i * n + i] = cd(a[i * n + i].real(), 0.0);
+        for (int j = i + 1; j < n; ++j)
+        {
+            const cd h = 0.5 * (a[i * n + j] + std::conj(a[j * n + i]));
+            a[i * n + j] = h;
+            a[j * n + i] = std::conj(h);
+        }
+    }
+    for (int sweep = 0; sweep < 100; ++sweep)
+    {
+        double off = 0.0, diag = 0.0;
+        for (int i = 0; i < n; ++i)
+        {
+            diag += a[i * n + i].real() * a[i * n + i].real();
+            for (int j = i + 1; j < n; ++j) off += std::norm(a[i * n + j]);
+        }
+        if (off <= 1e-32 * std::max(diag, 1e-300)) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q)
+            {
+                const cd apq = a[p * n + q];
+                const double mag = std::abs(apq);
+                if (mag < 1e-300) continue;
+                const double app = a[p * n + p].real(), aqq = a[q * n + q].real();
+                const double theta = (aqq - app) / (2.0 * mag);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::abs(theta) + std::sqrt(1.0 + theta * theta));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+                const cd ph = apq / mag; // e^{i phi}
+                // Rotation acting on columns p, q:  [c, s*ph; -s*conj(ph), c]
+                for (int k = 0; k < n; ++k)
+                {
+                    const cd akp = a[k * n + p], akq = a[k * n + q];
+                    a[k * n + p] = c * akp - s * std::conj(ph) * akq;
+                    a[k * n + q] = s * ph * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k)
+                {
+                    const cd apk = a[p * n + k], aqk = a[q * n + k];
+                    a[p * n + k] = c * apk - s * ph * aqk;
+                    a[q * n + k] = s * std::conj(ph) * apk + c * aqk;
+                }
+                a[p * n + q] = 0.0;
+                a[q * n + p] = 0.0;
+            }
+    }
+    w.resize(n);
+    for (int i = 0; i < n; ++i) w[i] = a[i * n + i].real();
+}
+
+double snap(double s) { return std::abs(s) < 1e-12 ? 0.0 : s; }
+
+double entropy_from_rdm(const cd *rho, int d, int order)
+{
+    if (d == 1) return 0.0;
+    if (order == 2)
+    {
+        double pur = 0.0;
+        for (int i = 0; i < d; ++i)
+        {
+            pur += rho[i * d + i].real() * rho[i * d + i].real();
+            for (int j = i + 1; j < d; ++j)
+            {
+                const cd h = 0.5 * (rho[i * d + j] + std::conj(rho[j * d + i]));
+                pur += 2.0 * std::norm(h);
+            }
+        }
+        if (!(pur > 0.0) || pur >= 1.0) return 0.0;
+        return snap(-std::log2(pur));
+    }
+    std::vector<cd> a(rho, rho + static_cast<std::size_t>(d) * d);
+    std::vector<double> w;
+    eig_hermitian(a, d, w);
+    double s = 0.0;
+    for (double l : w)
+        if (l > 1e-15) s -= l * std::log2(l);
+    return snap(s);
+}
+
+double subsystem_entropy(const cd *psi, int n, const std::vector<int> &kept, int order)
+{
+    const int d = 1 << kept.size();
+    std::vector<cd> rho(static_cast<std::size_t>(d) * d);
+    rdm(psi, n, kept.data(), static_cast<int>(kept.size()), false, rho.data());
+    return entropy_from_rdm(rho.data(), d, order);
+}
+
+std::vector<int> cyc(int begin, int count, int n)
+{
+    std::vector<int> v;
+    for (int i = 0; i < count; ++i) v.push_back(((begin + i) % n + n) % n);
+    return v;
+}
+
+double tmi(const cd *psi, int n, int offset, int order)
+{
+    const int b = n / 4;
+    const auto A = cyc(offset, b, n), B = cyc(offset + b, b, n), C = cyc(offset + 2 * b, b, n),
+               D = cyc(offset + 3 * b, b, n);
+    auto cat = [](std::vector<int> x, const std::vector<int> &y) {
+        x.insert(x.end(), y.begin(), y.end());
+        return x;
+    };
+    return subsystem_entropy(psi, n, A, order) + subsystem_entropy(psi, n, B, order) +
+           subsystem_entropy(psi, n, C, order) + subsystem_entropy(psi, n, D, order) -
+           subsystem_entropy(psi, n, cat(A, B), order) - subsystem_entropy(psi, n, cat(A, C), order) -
+           subsystem_entropy(psi, n, cat(B, C), order);
+}
+
+std::vector<int> half_chain(int n)
+{
+    std::vector<int> v;
+    for (int i = 0; i < n / 2; ++i) v.push_back(i);
+    return v;
+}
+} // namespace
+
+extern "C" {
+
+std::uint64_t orc_splitmix64(std::uint64_t v) { return mix64(v); }
+std::uint64_t orc_trajectory_seed(std::uint64_t master, std::uint64_t index)
+{
+    return mix64(master + 0x2545f4914f6cdd1dull * (index + 1ull));
+}
+
+// Same output layout as the reference harness's ref_haar_draw.
+int orc_haar_draw(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
+                  int *gates_per_layer, int *gate_q, double *gate_m, int *sites_per_layer, int *sites,
+                  double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<Layer> layers;
+        draw_trajectory(layers, seed, n, periods, p, closed != 0, meas);
+        const int mg = n / 2;
+        int u = 0;
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        for (std::size_t t = 0; t < layers.size(); ++t)
+        {
+            const int g = static_cast<int>(layers[t].q.size() / 2);
+            gates_per_layer[t] = g;
+            for (int i = 0; i < g; ++i)
+            {
+                gate_q[(t * mg + i) * 2] = layers[t].q[2 * i];
+                gate_q[(t * mg + i) * 2 + 1] = layers[t].q[2 * i + 1];
+                for (int e = 0; e < 16; ++e)
+                {
+                    gate_m[(t * mg + i) * 32 + 2 * e] = layers[t].m[16 * i + e].real();
+                    gate_m[(t * mg + i) * 32 + 2 * e + 1] = layers[t].m[16 * i + e].imag();
+                }
+            }
+            sites_per_layer[t] = static_cast<int>(layers[t].sites.size());
+            for (std::size_t s = 0; s < layers[t].sites.size(); ++s) sites[t * n + s] = layers[t].sites[s];
+            for (std::size_t s = 0; s < layers[t].sites.size(); s += chunk_bits) uniforms[u++] = unif(meas);
+        }
+        *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+void orc_apply_bond(double *psi_ri, int n, int q0, int q1, const double *m_ri)
+{
+    apply_bond(reinterpret_cast<cd *>(psi_ri), n, q0, q1, reinterpret_cast<const cd *>(m_ri));
+}
+
+int orc_measure_layer(double *psi_ri, int n, const int *sites, int m, int chunk_bits, const double *uniforms,
+                      const int *forced, int *outcomes, double *surprisal)
+{
+    try
+    {
+        std::vector<int> s(sites, sites + m);
+        int used = 0;
+        *surprisal = measure_layer(reinterpret_cast<cd *>(psi_ri), n, s, chunk_bits, uniforms, used, forced, outcomes);
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+int orc_measure_collapse(double *psi_ri, int n, int q, double u, int *outcome, double *cond_p)
+{
+    cd *psi = reinterpret_cast<cd *>(psi_ri);
+    const std::uint64_t dim = 1ull << n, mask = 1ull << q;
+    long double tot = 0.0L, one = 0.0L;
+    for (std::uint64_t x = 0; x < dim; ++x)
+    {
+        const long double w = std::norm(psi[x]);
+        tot += w;
+        if (x & mask) one += w;
+    }
+    const double t = static_cast<double>(tot), o = static_cast<double>(one);
+    if (!(t > 0.0) || !std::isfinite(t) || !(u >= 0.0 && u < 1.0)) return 1;
+    const double p1 = std::clamp(o / t, 0.0, 1.0);
+    const int bit = u < p1 ? 1 : 0;
+    const double branch = bit ? o : t - o;
+    if (!(branch > 0.0)) return 1;
+    const double scale = 1.0 / std::sqrt(branch);
+    for (std::uint64_t x = 0; x < dim; ++x)
+        psi[x] = (((x & mask) != 0) == (bit == 1)) ? psi[x] * scale : cd(0.0, 0.0);
+    *outcome = bit;
+    *cond_p = bit ? p1 : 1.0 - p1;
+    return 0;
+}
+
+int orc_rdm(const double *psi_ri, int n, const int *kept, int k, int fermion, double *rho_ri)
+{
+    try
+    {
+        rdm(reinterpret_cast<const cd *>(psi_ri), n, kept, k, fermion != 0, reinterpret_cast<cd *>(rho_ri));
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+double orc_entropy_hermitian(const double *rho_ri, int d, int order)
+{
+    return entropy_from_rdm(reinterpret_cast<const cd *>(rho_ri), d, order);
+}
+
+int orc_eigvalsh(const double *rho_ri, int d, double *w_out)
+{
+    std::vector<cd> a(reinterpret_cast<const cd *>(rho_ri), reinterpret_cast<const cd *>(rho_ri) + d * d);
+    std::vector<double> w;
+    eig_hermitian(a, d, w);
+    std::sort(w.begin(), w.end());
+    std::copy(w.begin(), w.end(), w_out);
+    return 0;
+}
+
+double orc_tmi(const double *psi_ri, int n, int offset, int order)
+{
+    return tmi(reinterpret_cast<const cd *>(psi_ri), n, offset, order);
+}
+
+int orc_rho3(const double *psi_ri, int n, const int *subs, int count, int fermion, double *out)
+{
+    try
+    {
+        for (int s = 0; s < count; ++s)
+        {
+            const int *q = subs + 3 * s;
+            cd *rho = reinterpret_cast<cd *>(out + 128 * s);
+            rdm(reinterpret_cast<const cd *>(psi_ri), n, q, 3, fermion != 0, rho);
+            if (!fermion) continue;
+            // The three-site trace orders modes as (q0, q1, q2, environment
+            // ascending), so besides the kept/environment crossings it also
+            // carries the sign of sorting the occupied kept modes among
+            // themselves (cpp/src/cuda/rho_reduce.cu:49-68, rdm.hpp:41-75).
+            int sgn[8];
+            for (int r = 0; r < 8; ++r)
+            {
+                int par = 0;
+                for (int i = 0; i < 3; ++i)
+                    for (int j = i + 1; j < 3; ++j)
+                        if (((r >> i) & 1) && ((r >> j) & 1) && q[i] > q[j]) par ^= 1;
+                sgn[r] = par ? -1 : 1;
+            }
+            for (int r = 0; r < 8; ++r)
+                for (int c = 0; c < 8; ++c) rho[r * 8 + c] *= static_cast<double>(sgn[r] * sgn[c]);
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// One whole Haar trajectory in FP64.
+//   obs_flags bit 0: half-chain S_vN, bit 1: half-chain S_2,
+//             bit 2: TMI (von Neumann, offset 0), bit 3: TMI (Renyi-2, offset 0)
+//   layer_obs[layer][4] gets those values (NaN where not requested) after
+//   every layer whose index+1 is a multiple of observe_every (0 = last only).
+//   outcomes[layer][n]: outcome of each measured site (in ascending-site
+//   order), -1 padding; forced (same layout, optional) replays outcomes.
+//   surprisal[layer]: -log P of the layer's joint outcome.
+int orc_run_haar_trajectory(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
+                            int obs_flags, int observe_every, const int *forced, int *outcomes,
+                            double *surprisal, double *layer_obs, double *final_psi_ri)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<Layer> layers;
+        draw_trajectory(layers, seed, n, periods, p, closed != 0, meas);
+        const std::uint64_t dim = 1ull << n;
+        std::vector<cd> psi(dim, cd(0.0, 0.0));
+        psi[0] = 1.0;
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        const int T = static_cast<int>(layers.size());
+        for (int t = 0; t < T; ++t)
+        {
+            const Layer &L = layers[t];
+            for (std::size_t g = 0; g < L.q.size() / 2; ++g)
+                apply_bond(psi.data(), n, L.q[2 * g], L.q[2 * g + 1], &L.m[16 * g]);
+            std::vector<double> us;
+            for (std::size_t s = 0; s < L.sites.size(); s += chunk_bits) us.push_back(unif(meas));
+            std::vector<int> oc(L.sites.size(), 0);
+            int used = 0;
+            const double sp = measure_layer(psi.data(), n, L.sites, chunk_bits, us.data(), used,
+                                            forced ? forced + static_cast<std::size_t>(t) * n : nullptr, oc.data());
+            if (surprisal) surprisal[t] = sp;
+            if (outcomes)
+            {
+                for (int s = 0; s < n; ++s) outcomes[static_cast<std::size_t>(t) * n + s] = -1;
+                for (std::size_t s = 0; s < oc.size(); ++s) outcomes[static_cast<std::size_t>(t) * n + s] = oc[s];
+            }
+            if (layer_obs)
+            {
+                double *o = layer_obs + 4 * static_cast<std::size_t>(t);
+                for (int j = 0; j < 4; ++j) o[j] = std::nan("");
+                const bool due = observe_every > 0 ? ((t + 1) % observe_every == 0) : (t == T - 1);
+                if (due)
+                {
+                    if (obs_flags & 1) o[0] = subsystem_entropy(psi.data(), n, half_chain(n), 1);
+                    if (obs_flags & 2) o[1] = subsystem_entropy(psi.data(), n, half_chain(n), 2);
+                    if ((obs_flags & 4) && n % 4 == 0) o[2] = tmi(psi.data(), n, 0, 1);
+                    if ((obs_flags & 8) && n % 4 == 0) o[3] = tmi(psi.data(), n, 0, 2);
+                }
+            }
+        }
+        if (final_psi_ri) std::memcpy(final_psi_ri, psi.data(), dim * sizeof(cd));
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Many trajectories (trajectory_seed(master, first + i)), spread over host
+// threads; returns the per-trajectory final half-chain S_2 in s2_out and
+// the per-layer surprisal sum in surprisal_out. Used as the timed CPU
+// baseline.
+int orc_run_batch(std::uint64_t master, int first, int count, int n, int periods, double p, int closed,
+                  int chunk_bits, int obs_flags, double *s2_out, double *surprisal_out, int threads)
+{
+    int failed = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : failed)
+#endif
+    for (int i = 0; i < count; ++i)
+    {
+        const std::uint64_t seed = orc_trajectory_seed(master, static_cast<std::uint64_t>(first + i));
+        std::vector<double> sp(2 * periods), obs(4 * 2 * periods);
+        const int rc = orc_run_haar_trajectory(seed, n, periods, p, closed, chunk_bits, obs_flags, 0, nullptr,
+                                               nullptr, sp.data(), obs.data(), nullptr);
+        if (rc) failed |= 1;
+        double tot = 0.0;
+        for (double v : sp) tot += v;
+        if (surprisal_out) surprisal_out[i] = tot;
+        if (s2_out) s2_out[i] = obs[4 * (2 * periods - 1) + 1];
+    }
+    return failed;
+}
+
+int orc_max_threads()
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+} // extern "C"

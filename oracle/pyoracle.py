@@ -1,0 +1,175 @@
+"""ctypes binding for the CPU FP64 oracle (oracle/oracle.cpp).
+
+Test infrastructure: imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline and reference legs, always as the checker or as the
+timed CPU baseline.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build():
+    subprocess.check_call([os.path.join(HERE, "build_oracle.sh")])
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ci, cd, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+    L.orc_splitmix64.restype = u64
+    L.orc_splitmix64.argtypes = [u64]
+    L.orc_trajectory_seed.restype = u64
+    L.orc_trajectory_seed.argtypes = [u64, u64]
+    L.orc_haar_draw.argtypes = [u64, ci, ci, cd, ci, ci] + [vp] * 7
+    L.orc_apply_bond.argtypes = [vp, ci, ci, ci, vp]
+    L.orc_measure_layer.argtypes = [vp, ci, vp, ci, ci, vp, vp, vp, vp]
+    L.orc_measure_collapse.argtypes = [vp, ci, ci, cd, vp, vp]
+    L.orc_rdm.argtypes = [vp, ci, vp, ci, ci, vp]
+    L.orc_entropy_hermitian.restype = cd
+    L.orc_entropy_hermitian.argtypes = [vp, ci, ci]
+    L.orc_eigvalsh.argtypes = [vp, ci, vp]
+    L.orc_tmi.restype = cd
+    L.orc_tmi.argtypes = [vp, ci, ci, ci]
+    L.orc_rho3.argtypes = [vp, ci, vp, ci, ci, vp]
+    L.orc_run_haar_trajectory.argtypes = [u64, ci, ci, cd, ci, ci, ci, ci, vp, vp, vp, vp, vp]
+    L.orc_run_batch.argtypes = [u64, ci, ci, ci, ci, cd, ci, ci, ci, vp, vp, ci]
+    L.orc_max_threads.restype = ci
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def trajectory_seed(master, index):
+    return lib().orc_trajectory_seed(master, index)
+
+
+def haar_draw(seed, n, periods, p, closed=True, chunk_bits=16):
+    """Returns dict(gates_per_layer, gate_q, gate_m[complex L x n/2 x 4 x 4],
+    sites_per_layer, sites, uniforms)."""
+    L, mg = 2 * periods, n // 2
+    gpl = np.zeros(L, np.int32)
+    gq = np.zeros((L, mg, 2), np.int32)
+    gm = np.zeros((L, mg, 32))
+    spl = np.zeros(L, np.int32)
+    sites = np.full((L, n), -1, np.int32)
+    uni = np.zeros(L * n + 1)
+    nu = np.zeros(1, np.int32)
+    rc = lib().orc_haar_draw(seed, n, periods, p, int(closed), chunk_bits,
+                             *[_p(a) for a in (gpl, gq, gm, spl, sites, uni, nu)])
+    if rc:
+        raise RuntimeError("orc_haar_draw failed")
+    return dict(gates_per_layer=gpl, gate_q=gq, gate_m=gm, sites_per_layer=spl, sites=sites,
+                uniforms=uni[: nu[0]].copy())
+
+
+def measure_collapse(psi, q, u):
+    psi = np.ascontiguousarray(psi, np.complex128).copy()
+    n = int(np.log2(psi.size))
+    oc = np.zeros(1, np.int32)
+    cp = np.zeros(1)
+    if lib().orc_measure_collapse(_p(psi), n, q, u, _p(oc), _p(cp)):
+        raise RuntimeError("orc_measure_collapse failed")
+    return psi, int(oc[0]), float(cp[0])
+
+
+def rdm(psi, kept, fermion=False):
+    psi = np.ascontiguousarray(psi, np.complex128)
+    n = int(np.log2(psi.size))
+    kk = np.ascontiguousarray(kept, np.int32)
+    d = 1 << len(kept)
+    rho = np.zeros((d, d), np.complex128)
+    if lib().orc_rdm(_p(psi), n, _p(kk), len(kept), int(fermion), _p(rho)):
+        raise RuntimeError("orc_rdm failed")
+    return rho
+
+
+def entropy(rho, order=1):
+    rho = np.ascontiguousarray(rho, np.complex128)
+    return lib().orc_entropy_hermitian(_p(rho), rho.shape[0], order)
+
+
+def eigvalsh(rho):
+    rho = np.ascontiguousarray(rho, np.complex128)
+    w = np.zeros(rho.shape[0])
+    lib().orc_eigvalsh(_p(rho), rho.shape[0], _p(w))
+    return w
+
+
+def tmi(psi, offset=0, order=1):
+    psi = np.ascontiguousarray(psi, np.complex128)
+    return lib().orc_tmi(_p(psi), int(np.log2(psi.size)), offset, order)
+
+
+def rho3(psi, subs, fermion=False):
+    psi = np.ascontiguousarray(psi, np.complex128)
+    subs = np.ascontiguousarray(subs, np.int32)
+    out = np.zeros(128 * len(subs))
+    if lib().orc_rho3(_p(psi), int(np.log2(psi.size)), _p(subs), len(subs), int(fermion), _p(out)):
+        raise RuntimeError("orc_rho3 failed")
+    return out
+
+
+def apply_bond(psi, q0, q1, U):
+    psi = np.ascontiguousarray(psi, np.complex128).copy()
+    U = np.ascontiguousarray(U, np.complex128)
+    lib().orc_apply_bond(_p(psi), int(np.log2(psi.size)), q0, q1, _p(U))
+    return psi
+
+
+def measure_layer(psi, sites, uniforms, chunk_bits=16, forced=None):
+    psi = np.ascontiguousarray(psi, np.complex128).copy()
+    s = np.ascontiguousarray(sites, np.int32)
+    u = np.ascontiguousarray(uniforms, np.float64)
+    f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+    oc = np.zeros(max(1, len(sites)), np.int32)
+    sp = np.zeros(1)
+    if lib().orc_measure_layer(_p(psi), int(np.log2(psi.size)), _p(s), len(sites), chunk_bits, _p(u), _p(f),
+                               _p(oc), _p(sp)):
+        raise RuntimeError("orc_measure_layer failed")
+    return psi, oc[: len(sites)].copy(), float(sp[0])
+
+
+OBS_SVN, OBS_S2, OBS_TMI1, OBS_TMI2 = 1, 2, 4, 8
+
+
+def run_trajectory(seed, n, periods, p, closed=True, chunk_bits=16, obs_flags=0, observe_every=0,
+                   forced=None, want_state=False):
+    T = 2 * periods
+    outcomes = np.full((T, n), -1, np.int32)
+    surprisal = np.zeros(T)
+    obs = np.full((T, 4), np.nan)
+    f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+    psi = np.zeros(1 << n, np.complex128) if want_state else None
+    rc = lib().orc_run_haar_trajectory(seed, n, periods, p, int(closed), chunk_bits, obs_flags, observe_every,
+                                       _p(f), _p(outcomes), _p(surprisal), _p(obs), _p(psi))
+    if rc:
+        raise RuntimeError("orc_run_haar_trajectory failed")
+    return dict(outcomes=outcomes, surprisal=surprisal, obs=obs, psi=psi)
+
+
+def run_batch(master, first, count, n, periods, p, closed=True, chunk_bits=16, obs_flags=OBS_S2, threads=0):
+    s2 = np.zeros(count)
+    sp = np.zeros(count)
+    if lib().orc_run_batch(master, first, count, n, periods, p, int(closed), chunk_bits, obs_flags, _p(s2), _p(sp),
+                           threads):
+        raise RuntimeError("orc_run_batch failed")
+    return s2, sp
+
+
+def max_threads():
+    return lib().orc_max_threads()

@@ -1,0 +1,213 @@
+// Parity harness: the reference's own host code, compiled from its headers in
+// place (see oracle/ref/build_ref.sh), behind a small C ABI that the fixture
+// generator (tests/golden/make_golden.py) calls through ctypes.
+//
+// TEST INFRASTRUCTURE ONLY. Nothing in the product links or loads this; it
+// exists to pin the CPU oracle (oracle/oracle.cpp) and the product's host
+// sampler to the reference's actual outputs.
+//
+// Reference functions exercised here (paths inside the reference project):
+//   seeding::splitmix64 / trajectory_seed      cpp/include/mipt/types.hpp:262-273
+//   Circuit1D::seed (seed_seq of the two halves, measurement stream from
+//   splitmix64(seed ^ 0xa0761d0d))              cpp/include/mipt/circuit.hpp:129-140
+//   build_haar_layers / fill_haar_layer         cpp/include/mipt/circuits/haar.hpp:226-305
+//   haar_unitary_4                              cpp/include/mipt/circuits/haar.hpp:39-85
+//   build_haar_layer_ops / haar_bond_matrix     cpp/include/mipt/cusv/gates.hpp:139-193
+//   Engine::measure_layer's uniform draws       cpp/include/mipt/cusv/engine.hpp:300-327
+//   measure_collapse_host                       cpp/include/mipt/free_energy_measure.hpp:18-96
+//   reduced_density_manual_from_state           cpp/include/mipt/tmi/linalg.hpp:1098-1142
+//   entropy_hermitian_inplace (Jacobi path)     cpp/include/mipt/tmi/linalg.hpp:524-583
+//   reduced_density_complex_from_host_statevector cpp/include/mipt/rdm.hpp:149-305
+#include "mipt/circuits/haar.hpp"
+#include "mipt/cusv/gates.hpp"
+#include "mipt/free_energy_measure.hpp"
+#include "mipt/rdm.hpp"
+#include "mipt/tmi/linalg.hpp"
+#include "mipt/types.hpp"
+
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+using C64 = std::complex<double>;
+
+namespace
+{
+// Same construction as Circuit1D::seed: the layer stream is seeded with the
+// 32-bit halves of the trajectory seed, the measurement stream with the halves
+// of splitmix64(seed ^ 0xa0761d0d).
+void seed_streams(std::uint64_t value, std::mt19937 &layer_rng, std::mt19937 &measure_rng)
+{
+    std::seed_seq sequence{static_cast<std::uint32_t>(value & 0xffffffffu),
+                           static_cast<std::uint32_t>(value >> 32)};
+    layer_rng.seed(sequence);
+    const std::uint64_t m = mipt::seeding::splitmix64(value ^ 0xa0761d0dull);
+    std::seed_seq measure_sequence{static_cast<std::uint32_t>(m & 0xffffffffu),
+                                   static_cast<std::uint32_t>(m >> 32)};
+    measure_rng.seed(measure_sequence);
+}
+
+std::vector<C64> unpack(const double *ri, std::size_t count)
+{
+    std::vector<C64> out(count);
+    for (std::size_t i = 0; i < count; ++i) out[i] = C64(ri[2 * i], ri[2 * i + 1]);
+    return out;
+}
+} // namespace
+
+extern "C" {
+
+std::uint64_t ref_splitmix64(std::uint64_t v) { return mipt::seeding::splitmix64(v); }
+
+std::uint64_t ref_trajectory_seed(std::uint64_t master, std::uint64_t index)
+{
+    return mipt::seeding::trajectory_seed(master, index);
+}
+
+// One Haar trajectory drawn exactly as HaarCircuit1D::simulate draws it, with
+// the measurement uniforms the cuStateVec engine would consume.
+//   gates_per_layer[2*periods]
+//   gate_q[layer][max_gates][2]          (q0, q1)
+//   gate_m[layer][max_gates][32]         row-major 4x4 complex (re, im)
+//   sites_per_layer[2*periods], sites[layer][n]
+//   uniforms[...] one per measured chunk of <= chunk_bits sites, in order
+int ref_haar_draw(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
+                  int *gates_per_layer, int *gate_q, double *gate_m, int *sites_per_layer,
+                  int *sites, double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        std::mt19937 layer_rng, measure_rng;
+        seed_streams(seed, layer_rng, measure_rng);
+        std::vector<mipt::HaarLayer> layers;
+        mipt::build_haar_layers(layers, n, periods, p, layer_rng, closed != 0);
+        const int max_gates = n / 2;
+        int u = 0;
+        for (std::size_t l = 0; l < layers.size(); ++l)
+        {
+            const auto ops = mipt::cusv::build_haar_layer_ops(layers[l], n);
+            gates_per_layer[l] = static_cast<int>(ops.ops.size());
+            for (std::size_t g = 0; g < ops.ops.size(); ++g)
+            {
+                const auto &op = ops.ops[g];
+                gate_q[(l * max_gates + g) * 2 + 0] = op.targets[0];
+                gate_q[(l * max_gates + g) * 2 + 1] = op.targets[1];
+                for (int e = 0; e < 16; ++e)
+                {
+                    gate_m[(l * max_gates + g) * 32 + 2 * e + 0] = op.matrix.values[e].real();
+                    gate_m[(l * max_gates + g) * 32 + 2 * e + 1] = op.matrix.values[e].imag();
+                }
+            }
+            sites_per_layer[l] = static_cast<int>(ops.measure_sites.size());
+            for (std::size_t s = 0; s < ops.measure_sites.size(); ++s)
+                sites[l * n + s] = ops.measure_sites[s];
+            // Engine::measure_layer: one U(0,1) per chunk, none for an empty layer.
+            std::uniform_real_distribution<double> uniform(0.0, 1.0);
+            for (std::size_t b = 0; b < ops.measure_sites.size(); b += static_cast<std::size_t>(chunk_bits))
+                uniforms[u++] = uniform(measure_rng);
+        }
+        *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Raw haar_unitary_4 draws from an mt19937 seeded with seed_seq{lo, hi}.
+int ref_haar_unitary(std::uint64_t seed, int count, double *out)
+{
+    std::mt19937 rng, unused;
+    seed_streams(seed, rng, unused);
+    for (int i = 0; i < count; ++i)
+    {
+        const auto u = mipt::haar_unitary_4(rng);
+        for (int e = 0; e < 16; ++e)
+        {
+            out[i * 32 + 2 * e] = u[e].real();
+            out[i * 32 + 2 * e + 1] = u[e].imag();
+        }
+    }
+    return 0;
+}
+
+int ref_measure_collapse(double *psi_ri, int n, int q, double u, int *outcome, double *cond_p,
+                         double *surprisal)
+{
+    try
+    {
+        auto psi = unpack(psi_ri, std::size_t{1} << n);
+        const auto r = mipt::free_energy::measure_collapse_host(psi.data(), n, q, u);
+        for (std::size_t i = 0; i < psi.size(); ++i)
+        {
+            psi_ri[2 * i] = psi[i].real();
+            psi_ri[2 * i + 1] = psi[i].imag();
+        }
+        *outcome = r.outcome;
+        *cond_p = r.conditional_probability;
+        *surprisal = r.surprisal;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+int ref_rdm_from_state(const double *psi_ri, int n, const int *kept, int k, int fermion,
+                       double *rho_ri)
+{
+    try
+    {
+        const auto psi = unpack(psi_ri, std::size_t{1} << n);
+        mipt::tmi::StateEntropyWorkspace ws;
+        std::vector<C64> out;
+        const std::vector<int> modes(kept, kept + k);
+        mipt::tmi::reduced_density_manual_from_state(psi.data(), n, modes, fermion != 0, ws, out);
+        for (std::size_t i = 0; i < out.size(); ++i)
+        {
+            rho_ri[2 * i] = out[i].real();
+            rho_ri[2 * i + 1] = out[i].imag();
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Entropy in bits of a row-major (re, im) density matrix; order 1 = von
+// Neumann (Jacobi path: no LAPACK is loadable here), order 2 = Renyi-2.
+double ref_entropy_hermitian(const double *rho_ri, int dim, int order)
+{
+    std::vector<C64> a = unpack(rho_ri, static_cast<std::size_t>(dim) * dim);
+    mipt::tmi::EntropyWorkspace ws;
+    return mipt::tmi::entropy_hermitian_inplace(
+        a, static_cast<std::size_t>(dim), ws,
+        order == 2 ? mipt::tmi::EntropyOrder::Renyi2 : mipt::tmi::EntropyOrder::VonNeumann);
+}
+
+double ref_renyi2_from_purity(double purity) { return mipt::tmi::renyi2_from_purity(purity); }
+
+int ref_rho3_from_state(const double *psi_ri, int n, const int *subs, int count, int fermion,
+                        double *out)
+{
+    try
+    {
+        const auto psi = unpack(psi_ri, std::size_t{1} << n);
+        std::vector<mipt::Subsystem> s(static_cast<std::size_t>(count));
+        for (int i = 0; i < count; ++i) s[i] = {subs[3 * i], subs[3 * i + 1], subs[3 * i + 2]};
+        mipt::reduced_density_complex_from_host_statevector(psi.data(), n, s, out, fermion != 0);
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+} // extern "C"

@@ -1,0 +1,199 @@
+"""Generate tests/golden/ref_fixtures.npz from the reference's own host code.
+
+Runs in the development container only: it loads oracle/_ref/libmipt_ref.so,
+which oracle/ref/build_ref.sh compiles from the reference checkout's headers
+(the reference's samplers, bond-matrix builders, measurement primitive,
+reduced-density and entropy code). The fixtures it writes are what the CPU
+oracle and the product are pinned to on machines without the reference.
+
+    python tests/golden/make_golden.py
+"""
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+LIB = os.path.join(ROOT, "oracle", "_ref", "libmipt_ref.so")
+
+# (seed, n, periods, p, closed, chunk_bits): covers open and closed chains,
+# p = 0 and p = 1 (the sampler's two short-cuts), chunk splitting, and the
+# BASELINE-scale chain lengths.
+DRAWS = [
+    (0, 12, 12, 0.2, 0, 16),
+    (1, 12, 3, 0.2, 1, 16),
+    (123, 24, 2, 0.35, 1, 16),
+    (5, 22, 2, 1.0, 1, 16),
+    (9, 8, 5, 0.0, 1, 4),
+    (77, 20, 2, 0.9, 1, 3),
+    (2024, 16, 3, 0.15, 1, 16),
+    (31337, 4, 4, 0.5, 1, 16),
+]
+
+
+def xorshift_state(n, seed):
+    """Dense random state in the style of the reference's GPU RDM tests:
+    xorshift64 uniforms, Box-Muller normals, normalised."""
+    state = seed & 0xFFFFFFFFFFFFFFFF
+    mask = 0xFFFFFFFFFFFFFFFF
+
+    def uniform():
+        nonlocal state
+        state ^= (state << 13) & mask
+        state ^= state >> 7
+        state ^= (state << 17) & mask
+        return (state >> 11) * (1.0 / 9007199254740992.0)
+
+    def normal():
+        u1 = max(1.0e-12, uniform())
+        u2 = uniform()
+        return np.sqrt(-2.0 * np.log(u1)) * np.cos(6.283185307179586 * u2)
+
+    dim = 1 << n
+    psi = np.empty(dim, np.complex128)
+    for i in range(dim):
+        re = normal()
+        im = normal()
+        psi[i] = re + 1j * im
+    return psi / np.linalg.norm(psi)
+
+
+def main():
+    if not os.path.exists(LIB):
+        subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh")])
+    lib = ctypes.CDLL(LIB)
+    vp = ctypes.c_void_p
+    lib.ref_haar_draw.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_int, ctypes.c_int] + [vp] * 7
+    lib.ref_trajectory_seed.restype = ctypes.c_uint64
+    lib.ref_trajectory_seed.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
+    lib.ref_splitmix64.restype = ctypes.c_uint64
+    lib.ref_splitmix64.argtypes = [ctypes.c_uint64]
+    lib.ref_measure_collapse.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double, vp, vp, vp]
+    lib.ref_rdm_from_state.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp]
+    lib.ref_entropy_hermitian.restype = ctypes.c_double
+    lib.ref_entropy_hermitian.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.ref_renyi2_from_purity.restype = ctypes.c_double
+    lib.ref_renyi2_from_purity.argtypes = [ctypes.c_double]
+    lib.ref_rho3_from_state.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp]
+
+    out = {}
+    # --- seeding -----------------------------------------------------------
+    seeds_in = np.array([0, 1, 2, 12345, 2**63 + 7, 2**64 - 1], np.uint64)
+    out["splitmix_in"] = seeds_in
+    out["splitmix_out"] = np.array([lib.ref_splitmix64(int(s)) for s in seeds_in], np.uint64)
+    out["trajseed_out"] = np.array([[lib.ref_trajectory_seed(m, i) for i in range(5)]
+                                    for m in (0, 1, 0xDEADBEEF)], np.uint64)
+
+    # --- Haar trajectory draws ---------------------------------------------
+    out["draw_params"] = np.array([d for d in DRAWS], np.float64)
+    for k, (seed, n, periods, p, closed, chunk) in enumerate(DRAWS):
+        L, mg = 2 * periods, n // 2
+        gpl = np.zeros(L, np.int32)
+        gq = np.zeros((L, mg, 2), np.int32)
+        gm = np.zeros((L, mg, 32))
+        spl = np.zeros(L, np.int32)
+        sites = np.full((L, n), -1, np.int32)
+        uni = np.zeros(L * n + 1)
+        nu = np.zeros(1, np.int32)
+        rc = lib.ref_haar_draw(seed, n, periods, p, closed, chunk,
+                               *[a.ctypes.data for a in (gpl, gq, gm, spl, sites, uni, nu)])
+        assert rc == 0
+        out[f"draw{k}_gates_per_layer"] = gpl
+        out[f"draw{k}_gate_q"] = gq
+        out[f"draw{k}_gate_m"] = gm
+        out[f"draw{k}_sites_per_layer"] = spl
+        out[f"draw{k}_sites"] = sites
+        out[f"draw{k}_uniforms"] = uni[: nu[0]].copy()
+
+    # --- sequential measurement (reference known answer + random states) ---
+    cases = []
+    psi = np.array([1, 2, 3, 4], np.complex128)
+    cases.append((psi, 2, 0, 0.5))
+    cases.append((None, 2, 1, 0.9))  # continues from the collapsed state above
+    for k, (n, q, u) in enumerate([(6, 2, 0.3), (8, 7, 0.99), (5, 0, 0.01), (7, 4, 0.5)]):
+        cases.append((xorshift_state(n, 0x1234 + k), n, q, u))
+    states_in, states_out, meas = [], [], []
+    prev = None
+    for psi, n, q, u in cases:
+        if psi is None:
+            psi = prev
+        buf = np.ascontiguousarray(psi.astype(np.complex128)).view(np.float64).copy()
+        states_in.append(buf.copy())
+        oc = np.zeros(1, np.int32)
+        cp = np.zeros(1)
+        sp = np.zeros(1)
+        rc = lib.ref_measure_collapse(buf.ctypes.data, n, q, u, oc.ctypes.data, cp.ctypes.data, sp.ctypes.data)
+        assert rc == 0
+        states_out.append(buf.copy())
+        prev = buf.view(np.complex128).copy()
+        meas.append((n, q, u, oc[0], cp[0], sp[0]))
+    for i, (a, b) in enumerate(zip(states_in, states_out)):
+        out[f"mc{i}_in"] = a
+        out[f"mc{i}_out"] = b
+    out["mc_params"] = np.array(meas, np.float64)
+
+    # --- RDMs and entropies on dense random states --------------------------
+    rdm_cases = [
+        (6, [0, 1, 2], 0), (6, [4, 1], 1), (7, [6, 0, 3], 1), (8, [0, 1, 2, 3], 0),
+        (8, [2, 5, 7, 0], 1), (9, [8, 0, 1], 0), (10, [0, 1, 2, 3, 4], 0), (10, [9, 3, 5, 1, 7], 1),
+        (12, [0, 1, 2, 3, 4, 5], 0), (12, [6, 7, 8, 0, 1, 2], 0),
+    ]
+    ent = []
+    for k, (n, kept, ferm) in enumerate(rdm_cases):
+        psi = xorshift_state(n, 0xABCDEF0123456789 + n + len(kept))
+        ri = np.ascontiguousarray(psi).view(np.float64)
+        d = 1 << len(kept)
+        kk = np.array(kept, np.int32)
+        rho = np.zeros(2 * d * d)
+        assert lib.ref_rdm_from_state(ri.ctypes.data, n, kk.ctypes.data, len(kept), ferm, rho.ctypes.data) == 0
+        s1 = lib.ref_entropy_hermitian(rho.ctypes.data, d, 1)
+        s2 = lib.ref_entropy_hermitian(rho.ctypes.data, d, 2)
+        out[f"rdm{k}_psi"] = ri.copy()
+        out[f"rdm{k}_kept"] = kk
+        out[f"rdm{k}_rho"] = rho
+        ent.append((n, ferm, s1, s2))
+    out["rdm_params"] = np.array(ent, np.float64)
+
+    # --- closed-form entropies (maximally mixed, pure, rank 2) --------------
+    closed_forms = []
+    for d in (2, 4, 8, 64):
+        rho = np.eye(d, dtype=np.complex128) / d
+        ri = np.ascontiguousarray(rho).view(np.float64)
+        closed_forms.append((d, 0, lib.ref_entropy_hermitian(ri.ctypes.data, d, 1),
+                             lib.ref_entropy_hermitian(ri.ctypes.data, d, 2)))
+    rho = np.zeros((4, 4), np.complex128)
+    rho[0, 0] = 1.0
+    ri = np.ascontiguousarray(rho).view(np.float64)
+    closed_forms.append((4, 1, lib.ref_entropy_hermitian(ri.ctypes.data, 4, 1),
+                         lib.ref_entropy_hermitian(ri.ctypes.data, 4, 2)))
+    rho = np.diag([0.3, 0.7, 0.0, 0.0]).astype(np.complex128)
+    ri = np.ascontiguousarray(rho).view(np.float64)
+    closed_forms.append((4, 2, lib.ref_entropy_hermitian(ri.ctypes.data, 4, 1),
+                         lib.ref_entropy_hermitian(ri.ctypes.data, 4, 2)))
+    out["closed_forms"] = np.array(closed_forms, np.float64)
+    out["renyi2_purity_in"] = np.array([1.0, 1.0 + 1e-15, 0.5, 0.25, 0.0, -1.0, 0.999999999999])
+    out["renyi2_purity_out"] = np.array([lib.ref_renyi2_from_purity(float(x)) for x in out["renyi2_purity_in"]])
+
+    # --- three-site RDMs on the periodic ring --------------------------------
+    for k, (n, ferm) in enumerate([(6, 0), (6, 1), (8, 1), (5, 0)]):
+        psi = xorshift_state(n, 0x5151 + 7 * k)
+        ri = np.ascontiguousarray(psi).view(np.float64)
+        subs = np.array([[s, (s + 1) % n, (s + 2) % n] for s in range(n)], np.int32)
+        rho3 = np.zeros(128 * n)
+        assert lib.ref_rho3_from_state(ri.ctypes.data, n, subs.ctypes.data, n, ferm, rho3.ctypes.data) == 0
+        out[f"rho3_{k}_psi"] = ri.copy()
+        out[f"rho3_{k}_subs"] = subs
+        out[f"rho3_{k}_ferm"] = np.array([ferm])
+        out[f"rho3_{k}_out"] = rho3
+
+    path = os.path.join(HERE, "ref_fixtures.npz")
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.1f} KiB, {len(out)} arrays)")
+
+
+if __name__ == "__main__":
+    sys.exit(main())
