@@ -1,0 +1,202 @@
+/*
+ * mipt_gb300 -- C ABI of the GB300-native monitored-circuit trajectory path.
+ *
+ * Conventions shared by every entry point:
+ *   - return 0 on success, nonzero on failure (a cudaError_t value, or
+ *     MIPT_GB300_E_* below); mipt_gb300_last_error() describes the failure
+ *     of the calling thread's last call;
+ *   - device state vectors are borrowed, never freed, and hold 2^n
+ *     interleaved complex amplitudes (float2 for *_f32, double2 for *_f64),
+ *     qubit q = bit q of the amplitude index;
+ *   - host output buffers are caller-owned; density matrices are row-major
+ *     (re, im) pairs;
+ *   - calls without a stream argument are synchronous to the host.
+ *
+ * The mipt_cuda_* functions keep the names, arguments and meaning of the
+ * reference's C ABI (paths inside the reference project are cited per
+ * function); a caller linked against the reference's CUDA objects can link
+ * this library instead.
+ */
+#ifndef MIPT_GB300_H
+#define MIPT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MIPT_GB300_E_INVALID 9001  /* bad argument */
+#define MIPT_GB300_E_NUMERIC 9002  /* zero-norm state / no outcome with weight */
+#define MIPT_GB300_E_NODEVICE 9003 /* no CUDA device */
+#define MIPT_GB300_E_INTERNAL 9004
+
+const char *mipt_gb300_last_error(void);
+const char *mipt_gb300_version(void);
+
+/* ------------------------------------------------------------------ RDMs */
+
+/* Reduced density matrix of the retained modes (row index bit k <-> mode
+ * host_kept_modes[k]); fermion_trace != 0 applies the Jordan-Wigner sign of
+ * moving the kept modes ahead of the environment.
+ * Replaces cpp/include/mipt/cuda/tmi_cuda_rdm.hpp:20-34. */
+int mipt_cuda_rdm_subsystem_f64(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                                int kept_count, int fermion_trace, double *host_rho_ri_row_major);
+int mipt_cuda_rdm_subsystem_f32(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                                int kept_count, int fermion_trace, double *host_rho_ri_row_major);
+
+/* Von Neumann entropy (bits) of the same subsystem.
+ * Replaces cpp/include/mipt/cuda/tmi_cuda_svd.hpp:58-72. */
+int mipt_cuda_entropy_svd_f64(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                              int kept_count, int fermion_trace, double *entropy_out);
+int mipt_cuda_entropy_svd_f32(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                              int kept_count, int fermion_trace, double *entropy_out);
+
+/* Renyi-2 entropy S_2 = -log2 Tr(rho^2) (bits), from the Gram matrix only.
+ * Replaces cpp/include/mipt/cuda/tmi_cuda_svd.hpp:84-98. */
+int mipt_cuda_renyi2_f64(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                         int kept_count, int fermion_trace, double *entropy_out);
+int mipt_cuda_renyi2_f32(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
+                         int kept_count, int fermion_trace, double *entropy_out);
+
+/* Three-site reduced density matrices, 128 doubles per subsystem;
+ * host_subsystems is a flat int[3*subsystem_count].
+ * Replaces cpp/include/mipt/cuda/rho_reduce.hpp:22-126. */
+int mipt_cuda_rho3_subsystems_complex_f64(const void *device_state_vector, int n_qubits, const int *host_subsystems,
+                                          int subsystem_count, double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_f32(const void *device_state_vector, int n_qubits, const int *host_subsystems,
+                                          int subsystem_count, double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_fermion_f64(const void *device_state_vector, int n_qubits,
+                                                  const int *host_subsystems, int subsystem_count,
+                                                  double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_fermion_f32(const void *device_state_vector, int n_qubits,
+                                                  const int *host_subsystems, int subsystem_count,
+                                                  double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_both_f64(const void *device_state_vector, int n_qubits,
+                                               const int *host_subsystems, int subsystem_count,
+                                               double *host_rho_ri_row_major, double *host_fermion_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_both_f32(const void *device_state_vector, int n_qubits,
+                                               const int *host_subsystems, int subsystem_count,
+                                               double *host_rho_ri_row_major, double *host_fermion_rho_ri_row_major);
+
+/* ----------------------------------------------------------- measurement */
+
+/* Sequential single-site Born measurement with collapse; the collapse is
+ * normalised by the raw branch weight. uniform_01 in [0,1).
+ * Replaces cpp/include/mipt/cuda/free_energy_measure.hpp:13-29. */
+int mipt_cuda_measure_collapse_f32(void *device_state_vector, int n_qubits, int measured_qubit, double uniform_01,
+                                   int *outcome, double *realized_probability);
+int mipt_cuda_measure_collapse_f64(void *device_state_vector, int n_qubits, int measured_qubit, double uniform_01,
+                                   int *outcome, double *realized_probability);
+const char *mipt_cuda_measure_collapse_last_error(void);
+
+/* ---------------------------------------------------------------- engine */
+
+/* One state vector driven layer by layer: the C form of the reference's
+ * cuStateVec Engine (cpp/include/mipt/cusv/engine.hpp:100-582). */
+typedef struct mipt_gb300_engine mipt_gb300_engine;
+
+int mipt_gb300_engine_create(int fp64, mipt_gb300_engine **out);
+void mipt_gb300_engine_destroy(mipt_gb300_engine *engine);
+/* Allocate (if needed) and set |0...0>.                   engine.hpp:143-155 */
+int mipt_gb300_engine_reset(mipt_gb300_engine *engine, int n_qubits);
+/* Operate on a caller-owned device buffer (never freed).  engine.hpp:131-140 */
+int mipt_gb300_engine_adopt(mipt_gb300_engine *engine, void *device_state_vector, int n_qubits);
+void *mipt_gb300_engine_data(mipt_gb300_engine *engine);
+int mipt_gb300_engine_set_from_host(mipt_gb300_engine *engine, const double *host_state_ri, int n_qubits);
+int mipt_gb300_engine_to_host(mipt_gb300_engine *engine, double *host_state_ri);
+/* Apply a layer of pairwise-disjoint two-qubit gates: bond j acts on qubits
+ * (pairs[2j], pairs[2j+1]) with the row-major 4x4 complex matrix
+ * matrices_ri[32j .. 32j+32) whose index bit 0 is pairs[2j].
+ *                                                           engine.hpp:236-288 */
+int mipt_gb300_engine_apply_bonds(mipt_gb300_engine *engine, const int *pairs, int bond_count,
+                                  const double *matrices_ri);
+/* Joint Born measurement of the ascending site list in chunks of chunk_bits
+ * sites, one uniform per chunk; forced_outcomes (nullable, one per site)
+ * replays a recorded outcome. Writes outcomes[i] for sites[i] and the
+ * layer surprisal -log P.                                   engine.hpp:293-368 */
+int mipt_gb300_engine_measure_layer(mipt_gb300_engine *engine, const int *sites, int site_count, int chunk_bits,
+                                    const double *uniforms, const int *forced_outcomes, int *outcomes,
+                                    double *surprisal);
+
+/* ------------------------------------------------------ batched trajectories */
+
+/* Per-layer or final observables of a batch (flags). */
+#define MIPT_GB300_OBS_SVN_HALF 1  /* half-chain von Neumann entropy (bits) */
+#define MIPT_GB300_OBS_S2_HALF 2   /* half-chain Renyi-2 entropy (bits) */
+#define MIPT_GB300_OBS_TMI_VN 4    /* TMI of contiguous quarters, von Neumann */
+#define MIPT_GB300_OBS_TMI_S2 8    /* TMI of contiguous quarters, Renyi-2 */
+
+typedef struct mipt_gb300_batch_config
+{
+    int n_qubits;      /* even, 4..30 */
+    int periods;       /* layers = 2 * periods */
+    int closed;        /* 1: odd layers close the ring with bond (n-1, 0) */
+    int fp64;          /* 0: FP32 state vectors (FP64 probabilities), 1: FP64 */
+    int chunk_bits;    /* joint-measurement chunk, 1..20 (reference default 16) */
+    int observables;   /* MIPT_GB300_OBS_* */
+    int observe_every; /* evaluate observables after every k-th layer; 0 = final state only */
+    int rho3;          /* 1: final three-site RDMs of the n ring triples */
+    int fermion_trace; /* trace convention for RDMs / rho3 */
+    int host_threads;  /* host sampler threads, 0 = all */
+    int tile_qubits;   /* local qubits per pass tile, 0 = default */
+} mipt_gb300_batch_config;
+
+typedef struct mipt_gb300_batch mipt_gb300_batch;
+
+int mipt_gb300_batch_create(const mipt_gb300_batch_config *config, int capacity, mipt_gb300_batch **out);
+void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
+
+/* Draw `count` Haar trajectories (trajectory i from seeds[i] with
+ * measurement rate p[i]) on host threads exactly as the reference's
+ * HaarCircuit1D draws them (cpp/include/mipt/circuit.hpp:129-140,415-439),
+ * and upload gates, measurement sites and uniforms. forced_outcomes
+ * (nullable, [count][2*periods] bit masks) replays recorded outcomes. */
+int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *batch, const uint64_t *seeds, const double *p, int count,
+                                  const uint64_t *forced_outcomes);
+/* Run every layer of the prepared batch on the device, asynchronously on
+ * `stream` (a cudaStream_t; NULL = default stream). */
+int mipt_gb300_batch_execute(mipt_gb300_batch *batch, void *stream);
+/* Wait for the batch and copy results to host (each pointer nullable):
+ *   measured[count][layers], outcomes[count][layers]  site bit masks
+ *   surprisal[count][layers]                          -log P per layer
+ *   obs[count][points][4]  (S_vN half, S_2 half, TMI vN, TMI S2; NaN where
+ *                          not requested), points = layers/observe_every or 1
+ *   rho3[count][n][128]                               final three-site RDMs */
+int mipt_gb300_batch_fetch(mipt_gb300_batch *batch, uint64_t *measured, uint64_t *outcomes, double *surprisal,
+                           double *obs, double *rho3);
+/* prepare + execute + fetch in one synchronous call. */
+int mipt_gb300_batch_run_haar(mipt_gb300_batch *batch, const uint64_t *seeds, const double *p, int count,
+                              const uint64_t *forced_outcomes, uint64_t *measured, uint64_t *outcomes,
+                              double *surprisal, double *obs, double *rho3);
+/* Device pointer of trajectory i's state vector after execute. */
+void *mipt_gb300_batch_state(mipt_gb300_batch *batch, int index);
+/* Number of kernel launches the last execute enqueued. */
+long long mipt_gb300_batch_launches(mipt_gb300_batch *batch);
+/* Bracket each launch category of execute with CUDA events on its stream;
+ * mipt_gb300_batch_kernel_stats then reports, for the last fetched execute,
+ * device milliseconds and bracket counts per category:
+ *   [0] layer passes (gates + fused histograms)  [1] stand-alone histograms
+ *   [2] outcome sampling                          [3] observables
+ *   [4] initialisation and final collapse */
+int mipt_gb300_batch_set_profiling(mipt_gb300_batch *batch, int enable);
+int mipt_gb300_batch_kernel_stats(mipt_gb300_batch *batch, double *ms, long long *launches);
+
+/* Host-side seeding helpers (the reference's splitmix64 streams,
+ * cpp/include/mipt/types.hpp:262-273). */
+uint64_t mipt_gb300_splitmix64(uint64_t value);
+uint64_t mipt_gb300_trajectory_seed(uint64_t master, uint64_t index);
+
+/* Draw one Haar trajectory on the host (no GPU needed): gates_per_layer[L],
+ * bond_q[L][n/2][2], bond_u[L][n/2][32] (row-major 4x4, re/im), measured[L]
+ * site masks, uniforms[] one per measurement chunk (n_uniforms returned). */
+int mipt_gb300_draw_haar(uint64_t seed, int n_qubits, int periods, double p, int closed, int chunk_bits,
+                         int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured, double *uniforms,
+                         int *n_uniforms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MIPT_GB300_H */

@@ -1,0 +1,313 @@
+"""GB300-native monitored-circuit trajectory path (Python host side).
+
+Everything here calls the C ABI of ``mipt_gb300/_build/libmipt_gb300.so``
+(declared in ``include/mipt_gb300.h``) through ctypes. There is no CPU or
+eager fallback: if the library is missing, importing the bindings raises.
+
+The functions mirror the reference's operator interface for this path
+(cpp/include/mipt/cuda/*.hpp and the cuStateVec Engine of
+cpp/include/mipt/cusv/engine.hpp in the reference project): same names,
+argument meaning and error behaviour (nonzero status -> exception carrying
+the library's message).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmipt_gb300.so")
+
+OBS_SVN_HALF, OBS_S2_HALF, OBS_TMI_VN, OBS_TMI_S2 = 1, 2, 4, 8
+
+_lib = None
+
+
+class MiptError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"mipt_gb300 status {status}: {message}")
+        self.status = status
+
+
+class BatchConfig(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_int) for name in (
+        "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
+        "fermion_trace", "host_threads", "tile_qubits")]
+
+
+def lib():
+    """Load the compiled library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m mipt_gb300.build`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, ci, cd, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+    L.mipt_gb300_last_error.restype = ctypes.c_char_p
+    L.mipt_gb300_version.restype = ctypes.c_char_p
+    L.mipt_cuda_measure_collapse_last_error.restype = ctypes.c_char_p
+    for name in ("mipt_cuda_rdm_subsystem", "mipt_cuda_entropy_svd", "mipt_cuda_renyi2"):
+        for suffix in ("_f32", "_f64"):
+            getattr(L, name + suffix).argtypes = [vp, ci, vp, ci, ci, vp]
+    for mid in ("", "fermion_"):
+        for suffix in ("f32", "f64"):
+            getattr(L, f"mipt_cuda_rho3_subsystems_complex_{mid}{suffix}").argtypes = [vp, ci, vp, ci, vp]
+    for suffix in ("f32", "f64"):
+        getattr(L, f"mipt_cuda_rho3_subsystems_complex_both_{suffix}").argtypes = [vp, ci, vp, ci, vp, vp]
+        getattr(L, f"mipt_cuda_measure_collapse_{suffix}").argtypes = [vp, ci, ci, cd, vp, vp]
+    L.mipt_gb300_engine_create.argtypes = [ci, ctypes.POINTER(vp)]
+    L.mipt_gb300_engine_destroy.argtypes = [vp]
+    L.mipt_gb300_engine_destroy.restype = None
+    L.mipt_gb300_engine_reset.argtypes = [vp, ci]
+    L.mipt_gb300_engine_adopt.argtypes = [vp, vp, ci]
+    L.mipt_gb300_engine_data.argtypes = [vp]
+    L.mipt_gb300_engine_data.restype = vp
+    L.mipt_gb300_engine_set_from_host.argtypes = [vp, vp, ci]
+    L.mipt_gb300_engine_to_host.argtypes = [vp, vp]
+    L.mipt_gb300_engine_apply_bonds.argtypes = [vp, vp, ci, vp]
+    L.mipt_gb300_engine_measure_layer.argtypes = [vp, vp, ci, ci, vp, vp, vp, vp]
+    L.mipt_gb300_batch_create.argtypes = [ctypes.POINTER(BatchConfig), ci, ctypes.POINTER(vp)]
+    L.mipt_gb300_batch_destroy.argtypes = [vp]
+    L.mipt_gb300_batch_destroy.restype = None
+    L.mipt_gb300_batch_prepare_haar.argtypes = [vp, vp, vp, ci, vp]
+    L.mipt_gb300_batch_execute.argtypes = [vp, vp]
+    L.mipt_gb300_batch_fetch.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_batch_state.argtypes = [vp, ci]
+    L.mipt_gb300_batch_state.restype = vp
+    L.mipt_gb300_batch_launches.argtypes = [vp]
+    L.mipt_gb300_batch_launches.restype = ctypes.c_longlong
+    L.mipt_gb300_batch_set_profiling.argtypes = [vp, ci]
+    L.mipt_gb300_batch_kernel_stats.argtypes = [vp, vp, vp]
+    L.mipt_gb300_splitmix64.argtypes = [u64]
+    L.mipt_gb300_splitmix64.restype = u64
+    L.mipt_gb300_trajectory_seed.argtypes = [u64, u64]
+    L.mipt_gb300_trajectory_seed.restype = u64
+    L.mipt_gb300_draw_haar.argtypes = [u64, ci, ci, cd, ci, ci, vp, vp, vp, vp, vp, vp]
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        raise MiptError(status, lib().mipt_gb300_last_error().decode(errors="replace"))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _dtype_suffix(fp64):
+    return "f64" if fp64 else "f32"
+
+
+# ----------------------------------------------------------------- seeding
+def splitmix64(v):
+    return lib().mipt_gb300_splitmix64(v)
+
+
+def trajectory_seed(master, index):
+    return lib().mipt_gb300_trajectory_seed(master, index)
+
+
+def draw_haar(seed, n, periods, p, closed=True, chunk_bits=16):
+    """Host draw of one Haar trajectory (no GPU): the reference's random record."""
+    L = 2 * periods
+    gpl = np.zeros(L, np.int32)
+    bq = np.zeros((L, n // 2, 2), np.int32)
+    bu = np.zeros((L, n // 2, 32))
+    meas = np.zeros(L, np.uint64)
+    uni = np.zeros(L * n + 1)
+    nu = np.zeros(1, np.int32)
+    _check(lib().mipt_gb300_draw_haar(seed, n, periods, p, int(closed), chunk_bits, _p(gpl), _p(bq), _p(bu),
+                                      _p(meas), _p(uni), _p(nu)))
+    return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu[0]].copy())
+
+
+# -------------------------------------------------- reference-compatible ops
+def rdm_subsystem(state_ptr, n, kept, fermion_trace=False, fp64=True):
+    """mipt_cuda_rdm_subsystem_*: RDM of `kept` from a device state pointer."""
+    kept = np.ascontiguousarray(kept, np.int32)
+    d = 1 << len(kept)
+    out = np.zeros((d, d), np.complex128)
+    fn = getattr(lib(), "mipt_cuda_rdm_subsystem_" + _dtype_suffix(fp64))
+    _check(fn(state_ptr, n, _p(kept), len(kept), int(fermion_trace), _p(out)))
+    return out
+
+
+def entropy_svd(state_ptr, n, kept, fermion_trace=False, fp64=True):
+    kept = np.ascontiguousarray(kept, np.int32)
+    out = np.zeros(1)
+    fn = getattr(lib(), "mipt_cuda_entropy_svd_" + _dtype_suffix(fp64))
+    _check(fn(state_ptr, n, _p(kept), len(kept), int(fermion_trace), _p(out)))
+    return float(out[0])
+
+
+def renyi2(state_ptr, n, kept, fermion_trace=False, fp64=True):
+    kept = np.ascontiguousarray(kept, np.int32)
+    out = np.zeros(1)
+    fn = getattr(lib(), "mipt_cuda_renyi2_" + _dtype_suffix(fp64))
+    _check(fn(state_ptr, n, _p(kept), len(kept), int(fermion_trace), _p(out)))
+    return float(out[0])
+
+
+def rho3_subsystems(state_ptr, n, subsystems, fermion_trace=False, fp64=True):
+    subs = np.ascontiguousarray(subsystems, np.int32).reshape(-1, 3)
+    out = np.zeros(128 * len(subs))
+    mid = "fermion_" if fermion_trace else ""
+    fn = getattr(lib(), f"mipt_cuda_rho3_subsystems_complex_{mid}{_dtype_suffix(fp64)}")
+    _check(fn(state_ptr, n, _p(subs), len(subs), _p(out)))
+    return out
+
+
+def measure_collapse(state_ptr, n, qubit, uniform_01, fp64=True):
+    outcome = np.zeros(1, np.int32)
+    prob = np.zeros(1)
+    fn = getattr(lib(), "mipt_cuda_measure_collapse_" + _dtype_suffix(fp64))
+    status = fn(state_ptr, n, qubit, uniform_01, _p(outcome), _p(prob))
+    if status != 0:
+        raise MiptError(status, lib().mipt_cuda_measure_collapse_last_error().decode(errors="replace"))
+    return int(outcome[0]), float(prob[0])
+
+
+# ------------------------------------------------------------------ engine
+class Engine:
+    """One state vector, layer by layer (the reference's cuStateVec Engine)."""
+
+    def __init__(self, fp64=True):
+        h = ctypes.c_void_p()
+        _check(lib().mipt_gb300_engine_create(int(fp64), ctypes.byref(h)))
+        self._h = h
+        self.fp64 = fp64
+        self.n = 0
+
+    def close(self):
+        if self._h:
+            lib().mipt_gb300_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self, n):
+        _check(lib().mipt_gb300_engine_reset(self._h, n))
+        self.n = n
+
+    def adopt(self, ptr, n):
+        _check(lib().mipt_gb300_engine_adopt(self._h, ptr, n))
+        self.n = n
+
+    @property
+    def data(self):
+        return lib().mipt_gb300_engine_data(self._h)
+
+    def set_state(self, psi):
+        psi = np.ascontiguousarray(psi, np.complex128)
+        n = int(np.log2(psi.size))
+        _check(lib().mipt_gb300_engine_set_from_host(self._h, _p(psi), n))
+        self.n = n
+
+    def state(self):
+        out = np.zeros(1 << self.n, np.complex128)
+        _check(lib().mipt_gb300_engine_to_host(self._h, _p(out)))
+        return out
+
+    def apply_bonds(self, pairs, matrices):
+        pairs = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        m = np.ascontiguousarray(np.asarray(matrices, np.complex128).reshape(len(pairs), 16))
+        _check(lib().mipt_gb300_engine_apply_bonds(self._h, _p(pairs), len(pairs), _p(m)))
+
+    def measure_layer(self, sites, uniforms, chunk_bits=16, forced=None):
+        sites = np.ascontiguousarray(sites, np.int32)
+        u = np.ascontiguousarray(uniforms, np.float64)
+        f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+        out = np.zeros(max(1, len(sites)), np.int32)
+        sp = np.zeros(1)
+        _check(lib().mipt_gb300_engine_measure_layer(self._h, _p(sites), len(sites), chunk_bits, _p(u), _p(f),
+                                                     _p(out), _p(sp)))
+        return out[: len(sites)].copy(), float(sp[0])
+
+
+# ------------------------------------------------------------------- batch
+class Batch:
+    """Many Haar trajectories of one chain length, run as one device schedule."""
+
+    def __init__(self, n, periods, capacity, closed=True, fp64=False, chunk_bits=16, observables=0,
+                 observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0):
+        cfg = BatchConfig(n, periods, int(closed), int(fp64), chunk_bits, observables, observe_every, int(rho3),
+                          int(fermion_trace), host_threads, tile_qubits)
+        h = ctypes.c_void_p()
+        _check(lib().mipt_gb300_batch_create(ctypes.byref(cfg), capacity, ctypes.byref(h)))
+        self._h = h
+        self.n, self.periods, self.layers = n, periods, 2 * periods
+        self.observe_every = observe_every
+        self.points = (self.layers // observe_every) if observe_every > 0 else 1
+        self.rho3 = rho3
+        self.count = 0
+
+    def close(self):
+        if self._h:
+            lib().mipt_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def prepare(self, seeds, p, forced=None):
+        seeds = np.ascontiguousarray(seeds, np.uint64)
+        p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, np.float64), seeds.shape))
+        f = None if forced is None else np.ascontiguousarray(forced, np.uint64)
+        _check(lib().mipt_gb300_batch_prepare_haar(self._h, _p(seeds), _p(p), len(seeds), _p(f)))
+        self.count = len(seeds)
+
+    def execute(self, stream=None):
+        _check(lib().mipt_gb300_batch_execute(self._h, stream))
+
+    def fetch(self):
+        c, T = self.count, self.layers
+        measured = np.zeros((c, T), np.uint64)
+        outcomes = np.zeros((c, T), np.uint64)
+        surprisal = np.zeros((c, T))
+        obs = np.zeros((c, self.points, 4))
+        rho3 = np.zeros((c, self.n, 128)) if self.rho3 else None
+        _check(lib().mipt_gb300_batch_fetch(self._h, _p(measured), _p(outcomes), _p(surprisal), _p(obs), _p(rho3)))
+        return dict(measured=measured, outcomes=outcomes, surprisal=surprisal, obs=obs, rho3=rho3)
+
+    def run(self, seeds, p, forced=None):
+        self.prepare(seeds, p, forced)
+        self.execute()
+        return self.fetch()
+
+    def state_ptr(self, i):
+        return lib().mipt_gb300_batch_state(self._h, i)
+
+    @property
+    def launches(self):
+        return lib().mipt_gb300_batch_launches(self._h)
+
+    def set_profiling(self, enable=True):
+        _check(lib().mipt_gb300_batch_set_profiling(self._h, int(enable)))
+
+    KERNEL_KINDS = ("pass", "hist", "measure", "observables", "other")
+
+    def kernel_stats(self):
+        ms = np.zeros(5)
+        n = np.zeros(5, np.int64)
+        _check(lib().mipt_gb300_batch_kernel_stats(self._h, _p(ms), _p(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+
+def outcomes_to_mask(sites, outcomes):
+    """Bit mask (bit q = outcome of site q) from per-site outcomes."""
+    m = 0
+    for s, o in zip(sites, outcomes):
+        if s >= 0 and o:
+            m |= 1 << int(s)
+    return m

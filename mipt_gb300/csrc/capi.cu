@@ -1,0 +1,1332 @@
+// C ABI of the GB300 trajectory path: reference-compatible observables,
+// the single-state engine, and the batched trajectory runner.
+#include "mipt_gb300.h"
+
+#include "engine.cuh"
+#include "observables.cuh"
+#include "sampler.hpp"
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+using namespace mg;
+
+namespace
+{
+thread_local std::string g_error;
+thread_local std::string g_measure_error;
+
+int fail(int code, const std::string &what)
+{
+    g_error = what;
+    return code == 0 ? MIPT_GB300_E_INTERNAL : code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return static_cast<int>(e);
+}
+
+#define MG_CUDA(expr)                                                                                            \
+    do                                                                                                           \
+    {                                                                                                            \
+        cudaError_t e_ = (expr);                                                                                 \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);                                                      \
+    } while (0)
+
+// Growable device buffer.
+struct DevBuf
+{
+    void *p = nullptr;
+    std::size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(std::size_t need)
+    {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p)
+        {
+            cudaFree(p);
+            p = nullptr;
+            bytes = 0;
+        }
+        cudaError_t e = cudaMalloc(&p, std::max<std::size_t>(need, 256));
+        if (e == cudaSuccess) bytes = std::max<std::size_t>(need, 256);
+        return e;
+    }
+    template <typename T> T *as() { return static_cast<T *>(p); }
+};
+
+struct PinnedBuf
+{
+    void *p = nullptr;
+    std::size_t bytes = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf()
+    {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t ensure(std::size_t need)
+    {
+        if (need <= bytes && p) return cudaSuccess;
+        if (p)
+        {
+            cudaFreeHost(p);
+            p = nullptr;
+            bytes = 0;
+        }
+        cudaError_t e = cudaMallocHost(&p, std::max<std::size_t>(need, 256));
+        if (e == cudaSuccess) bytes = std::max<std::size_t>(need, 256);
+        return e;
+    }
+    template <typename T> T *as() { return static_cast<T *>(p); }
+};
+
+__global__ void k_fill_double(double *p, std::size_t n, double v)
+{
+    for (std::size_t i = blockIdx.x * static_cast<std::size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<std::size_t>(gridDim.x) * blockDim.x)
+        p[i] = v;
+}
+
+__global__ void k_reset_layers(Collapse *col, LayerResult *res, std::size_t n)
+{
+    for (std::size_t i = blockIdx.x * static_cast<std::size_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<std::size_t>(gridDim.x) * blockDim.x)
+    {
+        col[i] = Collapse{0ull, 0ull, 1.0, 0.0};
+        LayerResult r{};
+        res[i] = r;
+    }
+}
+
+// out[idx[i]] = f(in[i]); f = identity (mode 0) or S_2 from a purity (mode 1).
+__global__ void k_scatter(const double *in, const int *idx, int n, double *out, int mode)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = in[i];
+    out[idx[i]] = mode == 1 ? renyi2_from_purity(v) : v;
+}
+
+// S = -sum lambda log2 lambda over lambda > 1e-15 (fixed-order reduction).
+__global__ void k_entropy_from_eigs(const double *w, int d, double *out)
+{
+    __shared__ double red[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < d; i += blockDim.x)
+    {
+        const double l = w[i];
+        if (l > 1e-15) s -= l * log2(l);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k /= 2)
+    {
+        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[0] = fabs(red[0]) < 1e-12 ? 0.0 : red[0];
+}
+
+// ------------------------------------------------------------ entropies
+
+struct EntReq
+{
+    int traj;
+    int order; // 1 = von Neumann, 2 = Renyi-2
+    int fermion;
+    std::vector<int> kept;
+    int out; // index into the output array
+};
+
+struct Workspace
+{
+    DevBuf jobs, rho, scratch, vals, idx, eig, work, info;
+    cusolverDnHandle_t solver = nullptr;
+    ~Workspace()
+    {
+        if (solver) cusolverDnDestroy(solver);
+    }
+};
+
+constexpr std::size_t kMaxRhoBytes = std::size_t{1} << 31;
+
+// Evaluates every request into d_out[req.out]; all requests share n.
+template <typename Real>
+int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs, const Collapse *col,
+                  std::size_t col_stride, Workspace &ws, cudaStream_t s, double *d_out, long long &launches)
+{
+    // Group by (k, needs_rho).
+    std::map<std::pair<int, int>, std::vector<const EntReq *>> groups;
+    for (const auto &r : reqs)
+    {
+        const int k = static_cast<int>(r.kept.size());
+        if (k == 0)
+        {
+            groups[{0, 0}].push_back(&r);
+            continue;
+        }
+        const bool purity_only = (r.order == 2);
+        groups[{k, purity_only ? 0 : 1}].push_back(&r);
+    }
+    for (auto &kv : groups)
+    {
+        const int k = kv.first.first;
+        const bool vn = kv.first.second == 1;
+        auto &list = kv.second;
+        if (k == 0)
+        {
+            // Empty subsystem: entropy 0.
+            std::vector<double> zeros(list.size(), 0.0);
+            std::vector<int> idx;
+            for (auto *r : list) idx.push_back(r->out);
+            MG_CUDA(ws.vals.ensure(sizeof(double) * zeros.size()));
+            MG_CUDA(ws.idx.ensure(sizeof(int) * idx.size()));
+            MG_CUDA(cudaMemcpyAsync(ws.vals.p, zeros.data(), sizeof(double) * zeros.size(), cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, s));
+            k_scatter<<<(static_cast<int>(idx.size()) + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(),
+                                                                              static_cast<int>(idx.size()), d_out, 0);
+            ++launches;
+            continue;
+        }
+        const int d = 1 << k;
+        const std::size_t rho_bytes = sizeof(double) * 2 * static_cast<std::size_t>(d) * d;
+        const int tiles = gram_tiles(k);
+        // Purity straight from tiles when there are enough tiles to fill the GPU.
+        const bool tile_purity = !vn && tiles * static_cast<long long>(list.size()) >= 2 * 152;
+        std::size_t per_launch = list.size();
+        if (!tile_purity) per_launch = std::max<std::size_t>(1, std::min(list.size(), kMaxRhoBytes / rho_bytes));
+        for (std::size_t b0 = 0; b0 < list.size(); b0 += per_launch)
+        {
+            const std::size_t nb = std::min(per_launch, list.size() - b0);
+            std::vector<GramJob> jobs(nb);
+            std::vector<int> idx(nb);
+            for (std::size_t i = 0; i < nb; ++i)
+            {
+                const EntReq *r = list[b0 + i];
+                jobs[i] = make_gram_job(r->traj, n, r->kept.data(), k, r->fermion != 0);
+                idx[i] = r->out;
+            }
+            MG_CUDA(ws.jobs.ensure(sizeof(GramJob) * nb));
+            MG_CUDA(ws.idx.ensure(sizeof(int) * nb));
+            MG_CUDA(ws.vals.ensure(sizeof(double) * nb));
+            MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
+            MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+            const int nbi = static_cast<int>(nb);
+            if (tile_purity)
+            {
+                MG_CUDA(ws.scratch.ensure(gram_scratch_bytes(n, k, nbi, false)));
+                MG_CUDA(gram_purity<Real>(states, n, ws.jobs.as<GramJob>(), nbi, k, col, col_stride,
+                                          ws.vals.as<double>(), ws.scratch.p, ws.scratch.bytes, s));
+                launches += 2;
+                k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 1);
+                ++launches;
+                continue;
+            }
+            MG_CUDA(ws.rho.ensure(rho_bytes * nb));
+            MG_CUDA(ws.scratch.ensure(gram_scratch_bytes(n, k, nbi, true)));
+            MG_CUDA(gram_rho<Real>(states, n, ws.jobs.as<GramJob>(), nbi, k, col, col_stride, ws.rho.as<double>(),
+                                   ws.scratch.p, ws.scratch.bytes, s));
+            launches += 2;
+            if (!vn)
+            {
+                MG_CUDA(purity_of(ws.rho.as<double>(), d, nbi, ws.vals.as<double>(), s));
+                ++launches;
+                k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 1);
+                ++launches;
+            }
+            else if (d <= 64)
+            {
+                MG_CUDA(jacobi_entropy(ws.rho.as<double>(), d, nbi, ws.vals.as<double>(), nullptr, s));
+                ++launches;
+                k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 0);
+                ++launches;
+            }
+            else
+            {
+                // Large spectra: FP64 divide-and-conquer eigensolver (cuSOLVER),
+                // one matrix at a time.
+                if (!ws.solver)
+                {
+                    if (cusolverDnCreate(&ws.solver) != CUSOLVER_STATUS_SUCCESS)
+                        return fail(MIPT_GB300_E_INTERNAL, "cusolverDnCreate failed");
+                }
+                cusolverDnSetStream(ws.solver, s);
+                int lwork = 0;
+                if (cusolverDnZheevd_bufferSize(ws.solver, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, d,
+                                                ws.rho.as<cuDoubleComplex>(), d, ws.eig.as<double>(), &lwork) !=
+                    CUSOLVER_STATUS_SUCCESS)
+                    return fail(MIPT_GB300_E_INTERNAL, "cusolverDnZheevd_bufferSize failed");
+                MG_CUDA(ws.work.ensure(sizeof(cuDoubleComplex) * static_cast<std::size_t>(std::max(lwork, 1))));
+                MG_CUDA(ws.eig.ensure(sizeof(double) * d));
+                MG_CUDA(ws.info.ensure(sizeof(int)));
+                for (int i = 0; i < nbi; ++i)
+                {
+                    cuDoubleComplex *A = ws.rho.as<cuDoubleComplex>() + static_cast<std::size_t>(i) * d * d;
+                    if (cusolverDnZheevd(ws.solver, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, d, A, d,
+                                         ws.eig.as<double>(), ws.work.as<cuDoubleComplex>(), lwork,
+                                         ws.info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
+                        return fail(MIPT_GB300_E_INTERNAL, "cusolverDnZheevd failed");
+                    k_entropy_from_eigs<<<1, 256, 0, s>>>(ws.eig.as<double>(), d, ws.vals.as<double>() + i);
+                    launches += 2;
+                }
+                k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 0);
+                ++launches;
+            }
+        }
+    }
+    return 0;
+}
+
+// ------------------------------------------------------ compat scratch
+struct CompatCtx
+{
+    Workspace ws;
+    DevBuf out, subs, rho3, scratch, sums;
+};
+thread_local std::unique_ptr<CompatCtx> g_compat;
+CompatCtx &compat()
+{
+    if (!g_compat) g_compat.reset(new CompatCtx());
+    return *g_compat;
+}
+
+template <typename Real>
+int compat_entropy(const void *state, int n, const int *kept, int k, int fermion, int order, double *out)
+{
+    if (!state || !kept || !out || n < 1 || n > 32 || k < 0 || k > n || k > 16)
+        return fail(MIPT_GB300_E_INVALID, "invalid subsystem request");
+    auto &c = compat();
+    EntReq r{0, order, fermion, std::vector<int>(kept, kept + k), 0};
+    for (int i = 0; i < k; ++i)
+        if (kept[i] < 0 || kept[i] >= n) return fail(MIPT_GB300_E_INVALID, "kept mode out of range");
+    MG_CUDA(c.out.ensure(sizeof(double)));
+    long long l = 0;
+    try
+    {
+        const int rc = run_entropies<Real>(static_cast<const Cx<Real> *>(state), n, {r}, nullptr, 0, c.ws, 0,
+                                           c.out.as<double>(), l);
+        if (rc) return rc;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    MG_CUDA(cudaMemcpy(out, c.out.p, sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+template <typename Real>
+int compat_rdm(const void *state, int n, const int *kept, int k, int fermion, double *host_rho)
+{
+    if (!state || !kept || !host_rho || n < 1 || n > 32 || k < 1 || k > n || k > 14)
+        return fail(MIPT_GB300_E_INVALID, "invalid subsystem request");
+    auto &c = compat();
+    GramJob job;
+    try
+    {
+        job = make_gram_job(0, n, kept, k, fermion != 0);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    const std::size_t d = std::size_t{1} << k;
+    MG_CUDA(c.ws.jobs.ensure(sizeof(GramJob)));
+    MG_CUDA(cudaMemcpy(c.ws.jobs.p, &job, sizeof(GramJob), cudaMemcpyHostToDevice));
+    MG_CUDA(c.ws.rho.ensure(sizeof(double) * 2 * d * d));
+    MG_CUDA(c.ws.scratch.ensure(gram_scratch_bytes(n, k, 1, true)));
+    MG_CUDA(gram_rho<Real>(static_cast<const Cx<Real> *>(state), n, c.ws.jobs.as<GramJob>(), 1, k, nullptr, 0,
+                           c.ws.rho.as<double>(), c.ws.scratch.p, c.ws.scratch.bytes, 0));
+    MG_CUDA(cudaMemcpy(host_rho, c.ws.rho.p, sizeof(double) * 2 * d * d, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+template <typename Real>
+int compat_rho3(const void *state, int n, const int *subs, int count, int fermion, double *out)
+{
+    if (!state || !subs || !out || count <= 0 || n < 3 || n > 32)
+        return fail(MIPT_GB300_E_INVALID, "invalid three-site request");
+    for (int s = 0; s < count; ++s)
+    {
+        const int a = subs[3 * s], b = subs[3 * s + 1], c = subs[3 * s + 2];
+        if (a < 0 || a >= n || b < 0 || b >= n || c < 0 || c >= n || a == b || a == c || b == c)
+            return fail(MIPT_GB300_E_INVALID, "three-site subsystem out of range or repeated");
+    }
+    auto &c = compat();
+    MG_CUDA(c.subs.ensure(sizeof(int) * 3 * count));
+    MG_CUDA(cudaMemcpy(c.subs.p, subs, sizeof(int) * 3 * count, cudaMemcpyHostToDevice));
+    MG_CUDA(c.rho3.ensure(sizeof(double) * 128 * count));
+    MG_CUDA(c.scratch.ensure(rho3_scratch_bytes(n, 1, count)));
+    MG_CUDA(rho3_sweep<Real>(static_cast<const Cx<Real> *>(state), n, 1, c.subs.as<int>(), count, fermion, nullptr, 0,
+                             c.rho3.as<double>(), c.scratch.p, c.scratch.bytes, 0));
+    MG_CUDA(cudaMemcpy(out, c.rho3.p, sizeof(double) * 128 * count, cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+// --------------------------------------------- single-site measurement
+constexpr int kNormBlocks = 256;
+
+template <typename Real>
+__global__ void k_branch_norms(const Cx<Real> *psi, std::uint64_t dim, std::uint64_t mask, double *part)
+{
+    __shared__ double r0[256], r1[256];
+    double tot = 0.0, one = 0.0;
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < dim;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const double w = static_cast<double>(psi[i].re) * psi[i].re + static_cast<double>(psi[i].im) * psi[i].im;
+        tot += w;
+        if (i & mask) one += w;
+    }
+    r0[threadIdx.x] = tot;
+    r1[threadIdx.x] = one;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k /= 2)
+    {
+        if (threadIdx.x < k)
+        {
+            r0[threadIdx.x] += r0[threadIdx.x + k];
+            r1[threadIdx.x] += r1[threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+    {
+        part[2 * blockIdx.x] = r0[0];
+        part[2 * blockIdx.x + 1] = r1[0];
+    }
+}
+
+template <typename Real>
+__global__ void k_project(Cx<Real> *psi, std::uint64_t dim, std::uint64_t mask, std::uint64_t value, double scale)
+{
+    const Real s = static_cast<Real>(scale);
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < dim;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        if ((i & mask) != value)
+            psi[i] = Cx<Real>{Real(0), Real(0)};
+        else
+        {
+            psi[i].re *= s;
+            psi[i].im *= s;
+        }
+    }
+}
+
+template <typename Real>
+int measure_collapse(void *state, int n, int q, double u, int *outcome, double *prob)
+{
+    if (!state || n < 1 || n > 34 || q < 0 || q >= n || !(u >= 0.0 && u < 1.0) || !outcome || !prob)
+    {
+        g_measure_error = "Invalid sequential-measurement request.";
+        return fail(MIPT_GB300_E_INVALID, g_measure_error);
+    }
+    auto &c = compat();
+    const std::uint64_t dim = 1ull << n;
+    cudaError_t e = c.sums.ensure(sizeof(double) * 2 * kNormBlocks);
+    if (e != cudaSuccess) return cuda_fail(e, "measure scratch");
+    Cx<Real> *psi = static_cast<Cx<Real> *>(state);
+    k_branch_norms<Real><<<kNormBlocks, 256>>>(psi, dim, 1ull << q, c.sums.as<double>());
+    std::vector<double> h(2 * kNormBlocks);
+    e = cudaMemcpy(h.data(), c.sums.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+    {
+        g_measure_error = cudaGetErrorString(e);
+        return cuda_fail(e, "measure norms");
+    }
+    double tot = 0.0, one = 0.0;
+    for (int i = 0; i < kNormBlocks; ++i)
+    {
+        tot += h[2 * i];
+        one += h[2 * i + 1];
+    }
+    if (!(tot > 0.0) || !std::isfinite(tot) || !std::isfinite(one) || one < 0.0 || one > tot * (1.0 + 1e-10))
+    {
+        g_measure_error = "Sequential measurement received invalid branch norms.";
+        return fail(MIPT_GB300_E_NUMERIC, g_measure_error);
+    }
+    const double p1 = std::clamp(one / tot, 0.0, 1.0);
+    const int bit = u < p1 ? 1 : 0;
+    const double cp = bit ? p1 : 1.0 - p1;
+    const double branch = bit ? one : tot - one;
+    if (!(cp > 0.0) || !(branch > 0.0))
+    {
+        g_measure_error = "Sampled an outcome with invalid conditional probability.";
+        return fail(MIPT_GB300_E_NUMERIC, g_measure_error);
+    }
+    k_project<Real><<<1024, 256>>>(psi, dim, 1ull << q, bit ? (1ull << q) : 0ull, 1.0 / std::sqrt(branch));
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+    {
+        g_measure_error = cudaGetErrorString(e);
+        return cuda_fail(e, "measure collapse");
+    }
+    *outcome = bit;
+    *prob = cp;
+    g_measure_error.clear();
+    return 0;
+}
+
+int default_tile_qubits(bool fp64) { return fp64 ? 13 : 14; }
+constexpr int kCoalesceQubits = 4;
+
+} // namespace
+
+// ======================================================================= engine
+struct mipt_gb300_engine
+{
+    bool fp64 = false;
+    int n = 0;
+    void *owned = nullptr;
+    void *borrowed = nullptr;
+    std::size_t owned_bytes = 0;
+    DevBuf gates, meas, col, res, part, bins, err;
+    ~mipt_gb300_engine()
+    {
+        if (owned) cudaFree(owned);
+    }
+    void *data() { return borrowed ? borrowed : owned; }
+};
+
+// ======================================================================= batch
+struct mipt_gb300_batch
+{
+    mipt_gb300_batch_config cfg{};
+    int capacity = 0;
+    int count = 0;
+    int T = 0, G = 0, kmax = 0, cmin = 0;
+    std::uint64_t dim = 0;
+    std::size_t elem = 0;
+    std::vector<PassPlan> plan[2];
+    DevBuf states, gates, meas, forced, col, res, part, bins, err, ent, subs, rho3, r3scratch;
+    PinnedBuf h_gates, h_meas, h_forced, h_res;
+    std::vector<std::uint64_t> measured;
+    std::vector<char> any_meas, fusable;
+    std::vector<int> max_chunks;
+    bool has_forced = false;
+    int points = 0;
+    int reqs_per_point = 0;
+    std::vector<EntReq> reqs; // for one point, trajectory index filled per launch
+    int col_half_vn = -1, col_half_s2 = -1;
+    std::vector<int> tmi_vn, tmi_s2; // 7 request slots each (A,B,C,D,AB,AC,BC)
+    Workspace ws;
+    long long launches = 0;
+    bool executed = false;
+    // Optional per-category kernel timing with CUDA events on the launch stream.
+    bool profile = false;
+    std::vector<cudaEvent_t> event_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    std::size_t next_event = 0;
+    double kind_ms[5] = {0, 0, 0, 0, 0};
+    long long kind_launches[5] = {0, 0, 0, 0, 0};
+    ~mipt_gb300_batch()
+    {
+        for (auto e : event_pool) cudaEventDestroy(e);
+    }
+    cudaEvent_t take_event()
+    {
+        if (next_event == event_pool.size())
+        {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            event_pool.push_back(e);
+        }
+        return event_pool[next_event++];
+    }
+};
+
+namespace
+{
+// Brackets one launch (or a group) with events when profiling is on.
+struct Mark
+{
+    mipt_gb300_batch *b;
+    int kind;
+    cudaStream_t s;
+    cudaEvent_t start = nullptr;
+    Mark(mipt_gb300_batch *b_, int kind_, cudaStream_t s_) : b(b_), kind(kind_), s(s_)
+    {
+        if (b->profile)
+        {
+            start = b->take_event();
+            cudaEventRecord(start, s);
+        }
+    }
+    ~Mark()
+    {
+        if (b->profile)
+        {
+            cudaEvent_t end = b->take_event();
+            cudaEventRecord(end, s);
+            b->marks.push_back({kind, {start, end}});
+        }
+    }
+};
+enum
+{
+    K_PASS = 0,
+    K_HIST = 1,
+    K_MEASURE = 2,
+    K_OBS = 3,
+    K_OTHER = 4
+};
+} // namespace
+
+extern "C" {
+
+const char *mipt_gb300_last_error(void) { return g_error.c_str(); }
+const char *mipt_gb300_version(void) { return "mipt_gb300 0.1 (sm_103a)"; }
+std::uint64_t mipt_gb300_splitmix64(std::uint64_t v) { return mg::splitmix64(v); }
+std::uint64_t mipt_gb300_trajectory_seed(std::uint64_t m, std::uint64_t i) { return mg::trajectory_seed(m, i); }
+
+int mipt_gb300_draw_haar(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
+                         int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured, double *uniforms,
+                         int *n_uniforms)
+{
+    try
+    {
+        TrajectoryDraw d;
+        draw_haar_trajectory(seed, n, periods, p, closed != 0, chunk_bits, d);
+        for (int t = 0; t < d.layers; ++t)
+        {
+            if (gates_per_layer) gates_per_layer[t] = d.bond_count[t];
+            if (measured) measured[t] = d.measured[t];
+        }
+        if (bond_q) std::copy(d.bond_q.begin(), d.bond_q.end(), bond_q);
+        if (bond_u)
+            for (std::size_t i = 0; i < d.bond_u.size(); ++i)
+            {
+                bond_u[2 * i] = d.bond_u[i].real();
+                bond_u[2 * i + 1] = d.bond_u[i].imag();
+            }
+        if (uniforms) std::copy(d.uniforms.begin(), d.uniforms.end(), uniforms);
+        if (n_uniforms) *n_uniforms = static_cast<int>(d.uniforms.size());
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+}
+
+// ---------------------------------------------------------- compat ABI
+int mipt_cuda_rdm_subsystem_f64(const void *s, int n, const int *kept, int k, int f, double *rho)
+{
+    return compat_rdm<double>(s, n, kept, k, f, rho);
+}
+int mipt_cuda_rdm_subsystem_f32(const void *s, int n, const int *kept, int k, int f, double *rho)
+{
+    return compat_rdm<float>(s, n, kept, k, f, rho);
+}
+int mipt_cuda_entropy_svd_f64(const void *s, int n, const int *kept, int k, int f, double *out)
+{
+    return compat_entropy<double>(s, n, kept, k, f, 1, out);
+}
+int mipt_cuda_entropy_svd_f32(const void *s, int n, const int *kept, int k, int f, double *out)
+{
+    return compat_entropy<float>(s, n, kept, k, f, 1, out);
+}
+int mipt_cuda_renyi2_f64(const void *s, int n, const int *kept, int k, int f, double *out)
+{
+    return compat_entropy<double>(s, n, kept, k, f, 2, out);
+}
+int mipt_cuda_renyi2_f32(const void *s, int n, const int *kept, int k, int f, double *out)
+{
+    return compat_entropy<float>(s, n, kept, k, f, 2, out);
+}
+int mipt_cuda_rho3_subsystems_complex_f64(const void *s, int n, const int *subs, int c, double *o)
+{
+    return compat_rho3<double>(s, n, subs, c, 0, o);
+}
+int mipt_cuda_rho3_subsystems_complex_f32(const void *s, int n, const int *subs, int c, double *o)
+{
+    return compat_rho3<float>(s, n, subs, c, 0, o);
+}
+int mipt_cuda_rho3_subsystems_complex_fermion_f64(const void *s, int n, const int *subs, int c, double *o)
+{
+    return compat_rho3<double>(s, n, subs, c, 1, o);
+}
+int mipt_cuda_rho3_subsystems_complex_fermion_f32(const void *s, int n, const int *subs, int c, double *o)
+{
+    return compat_rho3<float>(s, n, subs, c, 1, o);
+}
+int mipt_cuda_rho3_subsystems_complex_both_f64(const void *s, int n, const int *subs, int c, double *o, double *fo)
+{
+    int rc = compat_rho3<double>(s, n, subs, c, 0, o);
+    return rc ? rc : compat_rho3<double>(s, n, subs, c, 1, fo);
+}
+int mipt_cuda_rho3_subsystems_complex_both_f32(const void *s, int n, const int *subs, int c, double *o, double *fo)
+{
+    int rc = compat_rho3<float>(s, n, subs, c, 0, o);
+    return rc ? rc : compat_rho3<float>(s, n, subs, c, 1, fo);
+}
+int mipt_cuda_measure_collapse_f32(void *s, int n, int q, double u, int *o, double *p)
+{
+    return measure_collapse<float>(s, n, q, u, o, p);
+}
+int mipt_cuda_measure_collapse_f64(void *s, int n, int q, double u, int *o, double *p)
+{
+    return measure_collapse<double>(s, n, q, u, o, p);
+}
+const char *mipt_cuda_measure_collapse_last_error(void) { return g_measure_error.c_str(); }
+
+// ---------------------------------------------------------------- engine
+int mipt_gb300_engine_create(int fp64, mipt_gb300_engine **out)
+{
+    if (!out) return fail(MIPT_GB300_E_INVALID, "null output pointer");
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return fail(MIPT_GB300_E_NODEVICE, "no CUDA device");
+    auto *e = new mipt_gb300_engine();
+    e->fp64 = fp64 != 0;
+    *out = e;
+    return 0;
+}
+
+void mipt_gb300_engine_destroy(mipt_gb300_engine *e) { delete e; }
+
+int mipt_gb300_engine_reset(mipt_gb300_engine *e, int n)
+{
+    if (!e || n < 1 || n > 32) return fail(MIPT_GB300_E_INVALID, "engine supports 1..32 qubits");
+    const std::size_t bytes = (std::size_t{1} << n) * (e->fp64 ? 16u : 8u);
+    e->borrowed = nullptr;
+    if (!e->owned || e->owned_bytes < bytes)
+    {
+        if (e->owned) cudaFree(e->owned);
+        e->owned = nullptr;
+        MG_CUDA(cudaMalloc(&e->owned, bytes));
+        e->owned_bytes = bytes;
+    }
+    e->n = n;
+    if (e->fp64)
+        MG_CUDA(launch_init_zero<double>(static_cast<Cx<double> *>(e->owned), 1ull << n, 1, 0));
+    else
+        MG_CUDA(launch_init_zero<float>(static_cast<Cx<float> *>(e->owned), 1ull << n, 1, 0));
+    MG_CUDA(cudaDeviceSynchronize());
+    return 0;
+}
+
+int mipt_gb300_engine_adopt(mipt_gb300_engine *e, void *ptr, int n)
+{
+    if (!e || !ptr || n < 1 || n > 32) return fail(MIPT_GB300_E_INVALID, "engine adopt got an invalid buffer");
+    e->borrowed = ptr;
+    e->n = n;
+    return 0;
+}
+
+void *mipt_gb300_engine_data(mipt_gb300_engine *e) { return e ? e->data() : nullptr; }
+
+int mipt_gb300_engine_set_from_host(mipt_gb300_engine *e, const double *h, int n)
+{
+    if (!e || !h || n < 1 || n > 32) return fail(MIPT_GB300_E_INVALID, "invalid host state");
+    if (!e->borrowed)
+    {
+        int rc = mipt_gb300_engine_reset(e, n);
+        if (rc) return rc;
+    }
+    e->n = n;
+    const std::size_t dim = std::size_t{1} << n;
+    if (e->fp64)
+    {
+        MG_CUDA(cudaMemcpy(e->data(), h, dim * 16, cudaMemcpyHostToDevice));
+    }
+    else
+    {
+        std::vector<float> f(2 * dim);
+        for (std::size_t i = 0; i < 2 * dim; ++i) f[i] = static_cast<float>(h[i]);
+        MG_CUDA(cudaMemcpy(e->data(), f.data(), dim * 8, cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+int mipt_gb300_engine_to_host(mipt_gb300_engine *e, double *h)
+{
+    if (!e || !h || !e->data()) return fail(MIPT_GB300_E_INVALID, "engine has no state");
+    const std::size_t dim = std::size_t{1} << e->n;
+    if (e->fp64)
+    {
+        MG_CUDA(cudaMemcpy(h, e->data(), dim * 16, cudaMemcpyDeviceToHost));
+    }
+    else
+    {
+        std::vector<float> f(2 * dim);
+        MG_CUDA(cudaMemcpy(f.data(), e->data(), dim * 8, cudaMemcpyDeviceToHost));
+        for (std::size_t i = 0; i < 2 * dim; ++i) h[i] = f[i];
+    }
+    return 0;
+}
+
+int mipt_gb300_engine_apply_bonds(mipt_gb300_engine *e, const int *pairs, int nb, const double *m)
+{
+    if (!e || !e->data() || nb < 0 || (nb > 0 && (!pairs || !m))) return fail(MIPT_GB300_E_INVALID, "bad bonds");
+    if (nb == 0) return 0;
+    std::vector<Bond> bonds(nb);
+    std::uint64_t seen = 0;
+    for (int i = 0; i < nb; ++i)
+    {
+        const int a = pairs[2 * i], b = pairs[2 * i + 1];
+        if (a < 0 || a >= e->n || b < 0 || b >= e->n || a == b || ((seen >> a) & 1ull) || ((seen >> b) & 1ull))
+            return fail(MIPT_GB300_E_INVALID, "bonds must be pairwise disjoint and in range");
+        seen |= (1ull << a) | (1ull << b);
+        bonds[i] = Bond{a, b};
+    }
+    std::vector<PassPlan> plan;
+    try
+    {
+        plan = plan_layer(e->n, bonds, default_tile_qubits(e->fp64), kCoalesceQubits);
+    }
+    catch (const std::exception &ex)
+    {
+        return fail(MIPT_GB300_E_INVALID, ex.what());
+    }
+    if (e->fp64)
+    {
+        MG_CUDA(e->gates.ensure(sizeof(double) * 32 * nb));
+        MG_CUDA(cudaMemcpy(e->gates.p, m, sizeof(double) * 32 * nb, cudaMemcpyHostToDevice));
+        for (const auto &p : plan)
+            MG_CUDA(launch_pass<double>(static_cast<Cx<double> *>(e->data()), 1, p, e->gates.as<Cx<double>>(), 0,
+                                        nullptr, 0, nullptr, 0, nullptr, 0, 0));
+    }
+    else
+    {
+        std::vector<float> f(32 * static_cast<std::size_t>(nb));
+        for (std::size_t i = 0; i < f.size(); ++i) f[i] = static_cast<float>(m[i]);
+        MG_CUDA(e->gates.ensure(sizeof(float) * f.size()));
+        MG_CUDA(cudaMemcpy(e->gates.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+        for (const auto &p : plan)
+            MG_CUDA(launch_pass<float>(static_cast<Cx<float> *>(e->data()), 1, p, e->gates.as<Cx<float>>(), 0, nullptr,
+                                       0, nullptr, 0, nullptr, 0, 0));
+    }
+    MG_CUDA(cudaDeviceSynchronize());
+    return 0;
+}
+
+int mipt_gb300_engine_measure_layer(mipt_gb300_engine *e, const int *sites, int ns, int chunk_bits,
+                                    const double *uniforms, const int *forced, int *outcomes, double *surprisal)
+{
+    if (!e || !e->data() || ns < 0 || chunk_bits < 1 || chunk_bits > 20)
+        return fail(MIPT_GB300_E_INVALID, "bad measurement request");
+    if (surprisal) *surprisal = 0.0;
+    if (ns == 0) return 0;
+    if (!sites || !uniforms) return fail(MIPT_GB300_E_INVALID, "null sites/uniforms");
+    LayerMeas M{};
+    std::uint64_t forced_mask = 0;
+    for (int i = 0; i < ns; ++i)
+    {
+        if (sites[i] < 0 || sites[i] >= e->n || (i > 0 && sites[i] <= sites[i - 1]))
+            return fail(MIPT_GB300_E_INVALID, "sites must be ascending and in range");
+        if (forced) forced_mask |= static_cast<std::uint64_t>(forced[i] & 1) << sites[i];
+    }
+    const int nchunks = (ns + chunk_bits - 1) / chunk_bits;
+    if (nchunks > kMaxChunks) return fail(MIPT_GB300_E_INVALID, "too many measurement chunks");
+    if (e->n - std::min(default_tile_qubits(e->fp64), e->n) + kCoalesceQubits > 20)
+        return fail(MIPT_GB300_E_INVALID, "state too large for the joint-measurement scratch");
+    M.nchunks = nchunks;
+    for (int c = 0; c < nchunks; ++c)
+    {
+        std::uint64_t m = 0;
+        for (int i = c * chunk_bits; i < std::min(ns, (c + 1) * chunk_bits); ++i) m |= 1ull << sites[i];
+        M.chunk[c] = m;
+        M.uniform[c] = uniforms[c];
+    }
+    MG_CUDA(e->meas.ensure(sizeof(LayerMeas)));
+    MG_CUDA(e->col.ensure(sizeof(Collapse)));
+    MG_CUDA(e->res.ensure(sizeof(LayerResult)));
+    MG_CUDA(e->part.ensure(sizeof(double) * kHistScratch));
+    MG_CUDA(e->bins.ensure(sizeof(double) * kHistScratch));
+    MG_CUDA(e->err.ensure(sizeof(int) + sizeof(std::uint64_t)));
+    MG_CUDA(cudaMemcpy(e->meas.p, &M, sizeof(LayerMeas), cudaMemcpyHostToDevice));
+    std::uint64_t *d_forced = nullptr;
+    if (forced)
+    {
+        d_forced = reinterpret_cast<std::uint64_t *>(static_cast<char *>(e->err.p) + 8);
+        MG_CUDA(cudaMemcpy(d_forced, &forced_mask, sizeof(std::uint64_t), cudaMemcpyHostToDevice));
+    }
+    k_reset_layers<<<1, 32>>>(e->col.as<Collapse>(), e->res.as<LayerResult>(), 1);
+    MG_CUDA(cudaMemset(e->err.p, 0, sizeof(int)));
+    const int kmax = default_tile_qubits(e->fp64);
+    for (int c = 0; c < nchunks; ++c)
+    {
+        if (e->fp64)
+            MG_CUDA(launch_hist<double>(static_cast<const Cx<double> *>(e->data()), 1, e->n, kmax, kCoalesceQubits, c,
+                                        e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), 0));
+        else
+            MG_CUDA(launch_hist<float>(static_cast<const Cx<float> *>(e->data()), 1, e->n, kmax, kCoalesceQubits, c,
+                                       e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), 0));
+        MG_CUDA(launch_measure(1, e->n, nullptr, kmax, kCoalesceQubits, c, e->meas.as<LayerMeas>(), 1,
+                               e->part.as<double>(), e->bins.as<double>(), kHistScratch, d_forced, 1,
+                               e->col.as<Collapse>(), 1,
+                               e->res.as<LayerResult>(), 1, e->err.as<int>(), 0));
+    }
+    if (e->fp64)
+        MG_CUDA(launch_collapse<double>(static_cast<Cx<double> *>(e->data()), 1ull << e->n, 1, e->col.as<Collapse>(), 1, 0));
+    else
+        MG_CUDA(launch_collapse<float>(static_cast<Cx<float> *>(e->data()), 1ull << e->n, 1, e->col.as<Collapse>(), 1, 0));
+    LayerResult r{};
+    int err = 0;
+    MG_CUDA(cudaMemcpy(&r, e->res.p, sizeof(LayerResult), cudaMemcpyDeviceToHost));
+    MG_CUDA(cudaMemcpy(&err, e->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(MIPT_GB300_E_NUMERIC, "measurement layer found a zero-norm state or no outcome with weight");
+    if (outcomes)
+        for (int i = 0; i < ns; ++i) outcomes[i] = static_cast<int>((r.outcome >> sites[i]) & 1ull);
+    if (surprisal) *surprisal = r.surprisal;
+    return 0;
+}
+
+// ----------------------------------------------------------------- batch
+int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mipt_gb300_batch **out)
+{
+    if (!cfg || !out || capacity <= 0) return fail(MIPT_GB300_E_INVALID, "null config or capacity <= 0");
+    const int n = cfg->n_qubits;
+    if (n < 4 || n > 30 || (n % 2) != 0) return fail(MIPT_GB300_E_INVALID, "n_qubits must be even, 4..30");
+    if (cfg->periods < 1) return fail(MIPT_GB300_E_INVALID, "periods must be >= 1");
+    if (cfg->chunk_bits < 1 || cfg->chunk_bits > 20) return fail(MIPT_GB300_E_INVALID, "chunk_bits must be 1..20");
+    if ((cfg->observables & (MIPT_GB300_OBS_TMI_VN | MIPT_GB300_OBS_TMI_S2)) && (n % 4) != 0)
+        return fail(MIPT_GB300_E_INVALID, "TMI needs n divisible by 4");
+    if (cfg->observe_every < 0) return fail(MIPT_GB300_E_INVALID, "observe_every must be >= 0");
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return fail(MIPT_GB300_E_NODEVICE, "no CUDA device");
+
+    std::unique_ptr<mipt_gb300_batch> b(new mipt_gb300_batch());
+    b->cfg = *cfg;
+    b->capacity = capacity;
+    b->T = 2 * cfg->periods;
+    b->G = n / 2;
+    b->kmax = cfg->tile_qubits > 0 ? std::min(cfg->tile_qubits, kMaxLocal) : default_tile_qubits(cfg->fp64 != 0);
+    b->cmin = kCoalesceQubits;
+    if (n - std::min(b->kmax, n) + b->cmin > 20) return fail(MIPT_GB300_E_INVALID, "tile too small for this n");
+    b->dim = 1ull << n;
+    b->elem = cfg->fp64 ? 16 : 8;
+    for (int parity = 0; parity < 2; ++parity)
+    {
+        std::vector<Bond> bonds;
+        const int stop = (cfg->closed && parity == 1 && n > 2) ? n : n - 1;
+        for (int i = parity; i < stop; i += 2) bonds.push_back(Bond{i, (i + 1) % n});
+        try
+        {
+            b->plan[parity] = plan_layer(n, bonds, b->kmax, b->cmin);
+        }
+        catch (const std::exception &e)
+        {
+            return fail(MIPT_GB300_E_INVALID, e.what());
+        }
+    }
+    // Observable requests of one evaluation point (trajectory 0; shifted per trajectory).
+    auto range = [n](int a, int c) {
+        std::vector<int> v;
+        for (int i = 0; i < c; ++i) v.push_back((a + i) % n);
+        return v;
+    };
+    auto cat = [](std::vector<int> x, const std::vector<int> &y) {
+        x.insert(x.end(), y.begin(), y.end());
+        return x;
+    };
+    const int ft = cfg->fermion_trace ? 1 : 0;
+    if (cfg->observables & MIPT_GB300_OBS_SVN_HALF)
+    {
+        b->col_half_vn = static_cast<int>(b->reqs.size());
+        b->reqs.push_back(EntReq{0, 1, ft, range(0, n / 2), 0});
+    }
+    if (cfg->observables & MIPT_GB300_OBS_S2_HALF)
+    {
+        b->col_half_s2 = static_cast<int>(b->reqs.size());
+        b->reqs.push_back(EntReq{0, 2, ft, range(0, n / 2), 0});
+    }
+    for (int order = 1; order <= 2; ++order)
+    {
+        const int flag = order == 1 ? MIPT_GB300_OBS_TMI_VN : MIPT_GB300_OBS_TMI_S2;
+        if (!(cfg->observables & flag)) continue;
+        const int q = n / 4;
+        const auto A = range(0, q), B = range(q, q), C = range(2 * q, q), D = range(3 * q, q);
+        const std::vector<std::vector<int>> sets = {A, B, C, D, cat(A, B), cat(A, C), cat(B, C)};
+        auto &slots = order == 1 ? b->tmi_vn : b->tmi_s2;
+        for (const auto &s : sets)
+        {
+            slots.push_back(static_cast<int>(b->reqs.size()));
+            b->reqs.push_back(EntReq{0, order, ft, s, 0});
+        }
+    }
+    b->reqs_per_point = static_cast<int>(b->reqs.size());
+    b->points = cfg->observe_every > 0 ? b->T / cfg->observe_every : 1;
+
+    const std::size_t C = static_cast<std::size_t>(capacity), T = b->T;
+    cudaError_t e;
+    if ((e = b->states.ensure(C * b->dim * b->elem)) != cudaSuccess) return cuda_fail(e, "state allocation");
+    if ((e = b->gates.ensure(C * T * b->G * 16 * b->elem)) != cudaSuccess) return cuda_fail(e, "gate allocation");
+    if ((e = b->meas.ensure(C * T * sizeof(LayerMeas))) != cudaSuccess) return cuda_fail(e, "meas allocation");
+    if ((e = b->forced.ensure(C * T * sizeof(std::uint64_t))) != cudaSuccess) return cuda_fail(e, "forced allocation");
+    if ((e = b->col.ensure(C * T * sizeof(Collapse))) != cudaSuccess) return cuda_fail(e, "collapse allocation");
+    if ((e = b->res.ensure(C * T * sizeof(LayerResult))) != cudaSuccess) return cuda_fail(e, "result allocation");
+    if ((e = b->part.ensure(C * kHistScratch * sizeof(double))) != cudaSuccess) return cuda_fail(e, "partials");
+    if ((e = b->bins.ensure(C * (std::size_t{1} << cfg->chunk_bits) * sizeof(double))) != cudaSuccess)
+        return cuda_fail(e, "bins");
+    if ((e = b->err.ensure(sizeof(int))) != cudaSuccess) return cuda_fail(e, "error flag");
+    if (b->reqs_per_point > 0)
+        if ((e = b->ent.ensure(C * b->points * b->reqs_per_point * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "entropy outputs");
+    if (cfg->rho3)
+    {
+        std::vector<int> subs;
+        for (int s = 0; s < n; ++s)
+        {
+            subs.push_back(s);
+            subs.push_back((s + 1) % n);
+            subs.push_back((s + 2) % n);
+        }
+        if ((e = b->subs.ensure(sizeof(int) * subs.size())) != cudaSuccess) return cuda_fail(e, "subs");
+        if ((e = cudaMemcpy(b->subs.p, subs.data(), sizeof(int) * subs.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail(e, "subs upload");
+        if ((e = b->rho3.ensure(C * n * 128 * sizeof(double))) != cudaSuccess) return cuda_fail(e, "rho3");
+        if ((e = b->r3scratch.ensure(rho3_scratch_bytes(n, capacity, n))) != cudaSuccess)
+            return cuda_fail(e, "rho3 scratch");
+    }
+    if ((e = b->h_gates.ensure(C * T * b->G * 16 * b->elem)) != cudaSuccess) return cuda_fail(e, "pinned gates");
+    if ((e = b->h_meas.ensure(C * T * sizeof(LayerMeas))) != cudaSuccess) return cuda_fail(e, "pinned meas");
+    if ((e = b->h_forced.ensure(C * T * sizeof(std::uint64_t))) != cudaSuccess) return cuda_fail(e, "pinned forced");
+    if ((e = b->h_res.ensure(C * T * sizeof(LayerResult))) != cudaSuccess) return cuda_fail(e, "pinned results");
+    *out = b.release();
+    return 0;
+}
+
+void mipt_gb300_batch_destroy(mipt_gb300_batch *b) { delete b; }
+
+int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seeds, const double *p, int count,
+                                  const std::uint64_t *forced)
+{
+    if (!b || !seeds || !p || count <= 0 || count > b->capacity)
+        return fail(MIPT_GB300_E_INVALID, "bad batch prepare arguments");
+    const int n = b->cfg.n_qubits, T = b->T, G = b->G, cb = b->cfg.chunk_bits;
+    std::vector<TrajectoryDraw> draws;
+    try
+    {
+        draw_haar_batch(seeds, p, count, n, b->cfg.periods, b->cfg.closed != 0, cb, draws, b->cfg.host_threads);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    b->count = count;
+    b->measured.assign(static_cast<std::size_t>(count) * T, 0);
+    b->any_meas.assign(T, 0);
+    b->fusable.assign(T, 1);
+    b->max_chunks.assign(T, 0);
+    b->has_forced = forced != nullptr;
+    LayerMeas *hm = b->h_meas.as<LayerMeas>();
+    std::uint64_t *hf = b->h_forced.as<std::uint64_t>();
+    for (int i = 0; i < count; ++i)
+    {
+        const TrajectoryDraw &d = draws[i];
+        for (int t = 0; t < T; ++t)
+        {
+            const std::size_t slot = static_cast<std::size_t>(i) * T + t;
+            // Gates: the draw's bond list matches the planned brickwork order.
+            const std::complex<double> *src = &d.bond_u[static_cast<std::size_t>(t) * G * 16];
+            if (b->cfg.fp64)
+            {
+                double *dst = b->h_gates.as<double>() + slot * G * 32;
+                for (int e = 0; e < d.bond_count[t] * 16; ++e)
+                {
+                    dst[2 * e] = src[e].real();
+                    dst[2 * e + 1] = src[e].imag();
+                }
+            }
+            else
+            {
+                float *dst = b->h_gates.as<float>() + slot * G * 32;
+                for (int e = 0; e < d.bond_count[t] * 16; ++e)
+                {
+                    dst[2 * e] = static_cast<float>(src[e].real());
+                    dst[2 * e + 1] = static_cast<float>(src[e].imag());
+                }
+            }
+            const std::uint64_t mask = d.measured[t];
+            b->measured[slot] = mask;
+            LayerMeas M{};
+            const int m = __builtin_popcountll(mask);
+            M.nchunks = (m + cb - 1) / cb;
+            if (M.nchunks > kMaxChunks) return fail(MIPT_GB300_E_INVALID, "too many measurement chunks per layer");
+            int site = 0, c = -1, in_chunk = cb;
+            for (int q = 0; q < n; ++q)
+            {
+                if (!((mask >> q) & 1ull)) continue;
+                if (in_chunk == cb)
+                {
+                    ++c;
+                    in_chunk = 0;
+                }
+                M.chunk[c] |= 1ull << q;
+                ++in_chunk;
+                ++site;
+            }
+            for (int cc = 0; cc < M.nchunks; ++cc) M.uniform[cc] = d.uniforms[d.uniform_offset[t] + cc];
+            hm[slot] = M;
+            hf[slot] = forced ? forced[slot] : 0ull;
+            if (M.nchunks > 0)
+            {
+                b->any_meas[t] = 1;
+                b->max_chunks[t] = std::max(b->max_chunks[t], M.nchunks);
+                const PassPlan &last = b->plan[t & 1].back();
+                const int ml = local_measured_count(last.geom, M.chunk[0]);
+                if ((std::size_t{1} << (last.geom.n_nl + ml)) > kHistScratch) b->fusable[t] = 0;
+            }
+        }
+    }
+    const std::size_t C = static_cast<std::size_t>(count);
+    MG_CUDA(cudaMemcpy(b->gates.p, b->h_gates.p, C * T * G * 16 * b->elem, cudaMemcpyHostToDevice));
+    MG_CUDA(cudaMemcpy(b->meas.p, b->h_meas.p, C * T * sizeof(LayerMeas), cudaMemcpyHostToDevice));
+    if (forced) MG_CUDA(cudaMemcpy(b->forced.p, b->h_forced.p, C * T * sizeof(std::uint64_t), cudaMemcpyHostToDevice));
+    b->executed = false;
+    return 0;
+}
+
+} // extern "C"
+
+namespace
+{
+template <typename Real>
+int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
+{
+    const int n = b->cfg.n_qubits, T = b->T, G = b->G, count = b->count;
+    Cx<Real> *states = b->states.as<Cx<Real>>();
+    const Cx<Real> *gates = b->gates.as<Cx<Real>>();
+    LayerMeas *meas = b->meas.as<LayerMeas>();
+    Collapse *col = b->col.as<Collapse>();
+    LayerResult *res = b->res.as<LayerResult>();
+    const std::uint64_t *forced = b->has_forced ? b->forced.as<std::uint64_t>() : nullptr;
+    long long L = 0;
+    b->marks.clear();
+    b->next_event = 0;
+    {
+        Mark m(b, K_OTHER, s);
+        MG_CUDA(launch_init_zero<Real>(states, b->dim, count, s));
+    }
+    ++L;
+    const std::size_t slots = static_cast<std::size_t>(count) * T;
+    k_reset_layers<<<std::min<std::size_t>((slots + 255) / 256, 1024), 256, 0, s>>>(col, res, slots);
+    ++L;
+    MG_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(int), s));
+    if (b->reqs_per_point > 0)
+    {
+        const std::size_t ne = static_cast<std::size_t>(count) * b->points * b->reqs_per_point;
+        k_fill_double<<<std::min<std::size_t>((ne + 255) / 256, 1024), 256, 0, s>>>(b->ent.as<double>(), ne, NAN);
+        ++L;
+    }
+    const std::size_t gstride = static_cast<std::size_t>(T) * G * 16;
+    for (int t = 0; t < T; ++t)
+    {
+        const auto &plan = b->plan[t & 1];
+        const bool fuse = b->any_meas[t] && b->fusable[t];
+        for (std::size_t pi = 0; pi < plan.size(); ++pi)
+        {
+            const Collapse *cin = (pi == 0 && t > 0) ? col + (t - 1) : nullptr;
+            const bool last = pi + 1 == plan.size();
+            Mark m(b, K_PASS, s);
+            MG_CUDA(launch_pass<Real>(states, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
+                                      cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0, s));
+            ++L;
+        }
+        if (b->any_meas[t])
+        {
+            for (int ci = 0; ci < b->max_chunks[t]; ++ci)
+            {
+                const bool fused = ci == 0 && fuse;
+                if (!fused)
+                {
+                    Mark m(b, K_HIST, s);
+                    MG_CUDA(launch_hist<Real>(states, count, n, b->kmax, b->cmin, ci, col + t, T, meas + t, T,
+                                              b->part.as<double>(), s));
+                    ++L;
+                }
+                Mark m(b, K_MEASURE, s);
+                MG_CUDA(launch_measure(count, n, fused ? &plan.back().geom : nullptr, b->kmax, b->cmin, ci, meas + t, T,
+                                       b->part.as<double>(), b->bins.as<double>(),
+                                       std::size_t{1} << b->cfg.chunk_bits, forced ? forced + t : nullptr, T,
+                                       col + t, T, res + t, T, b->err.as<int>(), s));
+                ++L;
+            }
+        }
+        const bool due = b->cfg.observe_every > 0 ? ((t + 1) % b->cfg.observe_every == 0) : (t == T - 1);
+        if (due && b->reqs_per_point > 0 && b->cfg.observe_every > 0)
+        {
+            const int point = (t + 1) / b->cfg.observe_every - 1;
+            std::vector<EntReq> reqs;
+            for (int i = 0; i < count; ++i)
+                for (int r = 0; r < b->reqs_per_point; ++r)
+                {
+                    EntReq q = b->reqs[r];
+                    q.traj = i;
+                    q.out = (i * b->points + point) * b->reqs_per_point + r;
+                    reqs.push_back(q);
+                }
+            Mark m(b, K_OBS, s);
+            const int rc = run_entropies<Real>(states, n, reqs, col + t, T, b->ws, s, b->ent.as<double>(), L);
+            if (rc) return rc;
+        }
+    }
+    // Leave every trajectory in its collapsed, normalised final state.
+    {
+        Mark m(b, K_OTHER, s);
+        MG_CUDA(launch_collapse<Real>(states, b->dim, count, col + (T - 1), T, s));
+    }
+    ++L;
+    if (b->reqs_per_point > 0 && b->cfg.observe_every == 0)
+    {
+        std::vector<EntReq> reqs;
+        for (int i = 0; i < count; ++i)
+            for (int r = 0; r < b->reqs_per_point; ++r)
+            {
+                EntReq q = b->reqs[r];
+                q.traj = i;
+                q.out = i * b->reqs_per_point + r;
+                reqs.push_back(q);
+            }
+        Mark m(b, K_OBS, s);
+        const int rc = run_entropies<Real>(states, n, reqs, nullptr, 0, b->ws, s, b->ent.as<double>(), L);
+        if (rc) return rc;
+    }
+    if (b->cfg.rho3)
+    {
+        Mark m(b, K_OBS, s);
+        MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), n, b->cfg.fermion_trace ? 1 : 0, nullptr, 0,
+                                 b->rho3.as<double>(), b->r3scratch.p, b->r3scratch.bytes, s));
+        L += 2;
+    }
+    b->launches = L;
+    b->executed = true;
+    return 0;
+}
+} // namespace
+
+extern "C" {
+
+int mipt_gb300_batch_execute(mipt_gb300_batch *b, void *stream)
+{
+    if (!b || b->count <= 0) return fail(MIPT_GB300_E_INVALID, "batch has no prepared trajectories");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    try
+    {
+        return b->cfg.fp64 ? batch_execute<double>(b, s) : batch_execute<float>(b, s);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INTERNAL, e.what());
+    }
+}
+
+int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::uint64_t *outcomes, double *surprisal,
+                           double *obs, double *rho3)
+{
+    if (!b || !b->executed) return fail(MIPT_GB300_E_INVALID, "batch not executed");
+    MG_CUDA(cudaDeviceSynchronize());
+    for (int k = 0; k < 5; ++k)
+    {
+        b->kind_ms[k] = 0.0;
+        b->kind_launches[k] = 0;
+    }
+    for (const auto &m : b->marks)
+    {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, m.second.first, m.second.second) == cudaSuccess) b->kind_ms[m.first] += ms;
+        ++b->kind_launches[m.first];
+    }
+    b->marks.clear();
+    int err = 0;
+    MG_CUDA(cudaMemcpy(&err, b->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(MIPT_GB300_E_NUMERIC, "a measurement found a zero-norm state or no outcome with weight");
+    const int count = b->count, T = b->T, n = b->cfg.n_qubits;
+    if (measured) std::copy(b->measured.begin(), b->measured.end(), measured);
+    if (outcomes || surprisal)
+    {
+        LayerResult *hr = b->h_res.as<LayerResult>();
+        MG_CUDA(cudaMemcpy(hr, b->res.p, sizeof(LayerResult) * count * T, cudaMemcpyDeviceToHost));
+        for (std::size_t i = 0; i < static_cast<std::size_t>(count) * T; ++i)
+        {
+            if (outcomes) outcomes[i] = hr[i].outcome;
+            if (surprisal) surprisal[i] = hr[i].surprisal;
+        }
+    }
+    if (obs)
+    {
+        const std::size_t P = b->points, R = b->reqs_per_point;
+        std::vector<double> ent(static_cast<std::size_t>(count) * P * R);
+        if (R > 0) MG_CUDA(cudaMemcpy(ent.data(), b->ent.p, sizeof(double) * ent.size(), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < count; ++i)
+            for (std::size_t pt = 0; pt < P; ++pt)
+            {
+                const double *e = ent.data() + (static_cast<std::size_t>(i) * P + pt) * R;
+                double *o = obs + (static_cast<std::size_t>(i) * P + pt) * 4;
+                o[0] = b->col_half_vn >= 0 ? e[b->col_half_vn] : NAN;
+                o[1] = b->col_half_s2 >= 0 ? e[b->col_half_s2] : NAN;
+                auto tmi = [&](const std::vector<int> &s) {
+                    if (s.empty()) return static_cast<double>(NAN);
+                    return e[s[0]] + e[s[1]] + e[s[2]] + e[s[3]] - e[s[4]] - e[s[5]] - e[s[6]];
+                };
+                o[2] = tmi(b->tmi_vn);
+                o[3] = tmi(b->tmi_s2);
+            }
+    }
+    if (rho3)
+    {
+        if (!b->cfg.rho3) return fail(MIPT_GB300_E_INVALID, "batch was created without rho3");
+        MG_CUDA(cudaMemcpy(rho3, b->rho3.p, sizeof(double) * 128 * n * count, cudaMemcpyDeviceToHost));
+    }
+    return 0;
+}
+
+int mipt_gb300_batch_run_haar(mipt_gb300_batch *b, const std::uint64_t *seeds, const double *p, int count,
+                              const std::uint64_t *forced, std::uint64_t *measured, std::uint64_t *outcomes,
+                              double *surprisal, double *obs, double *rho3)
+{
+    int rc = mipt_gb300_batch_prepare_haar(b, seeds, p, count, forced);
+    if (rc) return rc;
+    rc = mipt_gb300_batch_execute(b, nullptr);
+    if (rc) return rc;
+    return mipt_gb300_batch_fetch(b, measured, outcomes, surprisal, obs, rho3);
+}
+
+void *mipt_gb300_batch_state(mipt_gb300_batch *b, int i)
+{
+    if (!b || i < 0 || i >= b->count) return nullptr;
+    return static_cast<char *>(b->states.p) + static_cast<std::size_t>(i) * b->dim * b->elem;
+}
+
+long long mipt_gb300_batch_launches(mipt_gb300_batch *b) { return b ? b->launches : -1; }
+
+int mipt_gb300_batch_set_profiling(mipt_gb300_batch *b, int enable)
+{
+    if (!b) return fail(MIPT_GB300_E_INVALID, "null batch");
+    b->profile = enable != 0;
+    return 0;
+}
+
+int mipt_gb300_batch_kernel_stats(mipt_gb300_batch *b, double *ms, long long *launches)
+{
+    if (!b) return fail(MIPT_GB300_E_INVALID, "null batch");
+    for (int k = 0; k < 5; ++k)
+    {
+        if (ms) ms[k] = b->kind_ms[k];
+        if (launches) launches[k] = b->kind_launches[k];
+    }
+    return 0;
+}
+
+} // extern "C"

@@ -1,0 +1,704 @@
+// Tiled layer passes, fused Born histograms, on-device outcome sampling and
+// deferred collapse for batches of state vectors.
+//
+// Reference behaviour reproduced (paths inside the reference project):
+//   gate application  = custatevecApplyMatrix with a row-major matrix whose
+//                       index bit k is targets[k]   cpp/include/mipt/cusv/engine.hpp:236-277,
+//                                                   cpp/include/mipt/cusv/matrix.hpp:5-13
+//   layer measurement = Engine::measure_layer: chunks of <= chunk_bits sites,
+//                       joint histogram, one uniform per chunk, linear CDF
+//                       scan, starved-bin fallback to the heaviest bin,
+//                       collapse scaled by 1/sqrt(branch)
+//                                                   cpp/include/mipt/cusv/engine.hpp:293-368
+#include "engine.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <stdexcept>
+
+namespace mg
+{
+
+namespace
+{
+constexpr int kPassThreads = 512;
+constexpr int kMeasureThreads = 1024;
+constexpr int kSmemBins = 4096;
+
+template <typename Real> struct Acc;
+// FP32 amplitudes: per-thread runs of 64 squared magnitudes in FP32,
+// promoted to FP64 (the reference's mixed-precision sweep scheme,
+// cpp/include/mipt/cuda/reduce_sweep.cuh:59-96).
+template <> struct Acc<float>
+{
+    double total = 0.0;
+    float run = 0.f;
+    int count = 0;
+    __device__ void add(float v)
+    {
+        run += v;
+        if (++count == 64)
+        {
+            total += static_cast<double>(run);
+            run = 0.f;
+            count = 0;
+        }
+    }
+    __device__ double value() const { return total + static_cast<double>(run); }
+};
+template <> struct Acc<double>
+{
+    double total = 0.0;
+    __device__ void add(double v) { total += v; }
+    __device__ double value() const { return total; }
+};
+
+template <typename Real>
+__device__ __forceinline__ Real norm2(Cx<Real> v)
+{
+    return v.re * v.re + v.im * v.im;
+}
+
+// Deterministic histogram of a tile in shared memory over the local bit
+// positions lm[0..m_loc): out[bin] = sum of |tile[j]|^2 over j whose bits at
+// lm[i] spell bin. Fixed summation order for a given launch shape.
+template <typename Real>
+__device__ void tile_histogram(const Cx<Real> *tile, int k, const int *lm, int m_loc, double *out, double *red)
+{
+    const int T = blockDim.x;
+    const int tid = threadIdx.x;
+    const std::uint64_t nb = 1ull << m_loc;
+    const std::uint64_t per_bin = 1ull << (k - m_loc);
+    if (nb <= static_cast<std::uint64_t>(T))
+    {
+        const int G = T / static_cast<int>(nb);
+        const std::uint64_t bin = tid / G;
+        const int sub = tid % G;
+        std::uint64_t fixed = 0;
+        for (int i = 0; i < m_loc; ++i) fixed |= ((bin >> i) & 1ull) << lm[i];
+        Acc<Real> acc;
+        for (std::uint64_t r = sub; r < per_bin; r += G)
+        {
+            std::uint64_t j = r;
+            for (int i = 0; i < m_loc; ++i) j = insert_zero(j, lm[i]);
+            acc.add(norm2(tile[j | fixed]));
+        }
+        double v = acc.value();
+        // Tree over the G threads of this bin: shuffles inside a warp, then
+        // a fixed-order sum of warp results.
+        const int width = G < 32 ? G : 32;
+        for (int off = width / 2; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off, width);
+        if (G <= 32)
+        {
+            if (sub == 0) out[bin] = v;
+        }
+        else
+        {
+            if ((tid & 31) == 0) red[tid >> 5] = v;
+            __syncthreads();
+            if (sub == 0)
+            {
+                double s = 0.0;
+                for (int w = 0; w < G / 32; ++w) s += red[(tid >> 5) + w];
+                out[bin] = s;
+            }
+        }
+    }
+    else
+    {
+        for (std::uint64_t bin = tid; bin < nb; bin += T)
+        {
+            std::uint64_t fixed = 0;
+            for (int i = 0; i < m_loc; ++i) fixed |= ((bin >> i) & 1ull) << lm[i];
+            Acc<Real> acc;
+            for (std::uint64_t r = 0; r < per_bin; ++r)
+            {
+                std::uint64_t j = r;
+                for (int i = 0; i < m_loc; ++i) j = insert_zero(j, lm[i]);
+                acc.add(norm2(tile[j | fixed]));
+            }
+            out[bin] = acc.value();
+        }
+    }
+}
+
+template <typename Real>
+__device__ __forceinline__ Cx<Real> collapse_value(Cx<Real> v, std::uint64_t gidx, const Collapse &cl, Real scale)
+{
+    if ((gidx & cl.mask) != cl.value) return Cx<Real>{Real(0), Real(0)};
+    return Cx<Real>{v.re * scale, v.im * scale};
+}
+
+// Loads the tile of geometry g with index tix into shared memory, applying a
+// pending collapse. seg[s] holds the offset of high segment s.
+template <typename Real>
+__device__ void load_tile(Cx<Real> *tile, const Cx<Real> *__restrict__ psi, const PassGeom &g, std::uint64_t base,
+                          const std::uint32_t *seg, const Collapse &cl, bool has_col)
+{
+    const std::uint64_t nloc = 1ull << g.k;
+    const std::uint64_t cmask = (1ull << g.c) - 1ull;
+    const Real scale = static_cast<Real>(cl.scale);
+    for (std::uint64_t j = threadIdx.x; j < nloc; j += blockDim.x)
+    {
+        const std::uint64_t gidx = base | seg[j >> g.c] | (j & cmask);
+        Cx<Real> v = psi[gidx];
+        if (has_col) v = collapse_value(v, gidx, cl, scale);
+        tile[j] = v;
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kPassThreads) k_pass(Cx<Real> *__restrict__ states, PassGeom g, PassGates pg,
+                                                       const Cx<Real> *__restrict__ gates, std::size_t gate_stride,
+                                                       const Collapse *__restrict__ col_in, std::size_t col_stride,
+                                                       const LayerMeas *__restrict__ meas, std::size_t meas_stride,
+                                                       double *__restrict__ partials, int fuse_hist)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
+    std::uint32_t *seg = reinterpret_cast<std::uint32_t *>(smem_raw + (sizeof(Cx<Real>) << g.k));
+    __shared__ Cx<Real> U[kMaxPassGates][16];
+    __shared__ double red[kPassThreads / 32];
+
+    const int b = blockIdx.y;
+    const std::uint64_t tix = blockIdx.x;
+    const std::uint64_t dim = 1ull << g.n;
+    Cx<Real> *psi = states + static_cast<std::size_t>(b) * dim;
+    const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+    const int h = g.k - g.c;
+    for (std::uint32_t s = threadIdx.x; s < (1u << h); s += blockDim.x)
+        seg[s] = static_cast<std::uint32_t>(scatter_bits(s, g.pos + g.c, h));
+    for (int i = threadIdx.x; i < pg.count * 16; i += blockDim.x)
+        U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(pg.gate[i / 16]) * 16 + (i % 16)];
+    Collapse cl{0, 0, 1.0, 0.0};
+    const bool has_col = col_in != nullptr;
+    if (has_col) cl = col_in[b * col_stride];
+    __syncthreads();
+
+    load_tile(tile, psi, g, base, seg, cl, has_col);
+    __syncthreads();
+
+    const std::uint64_t groups = 1ull << (g.k - 2);
+    for (int gi = 0; gi < pg.count; ++gi)
+    {
+        const int a = pg.la[gi], bb = pg.lb[gi];
+        const int lo = a < bb ? a : bb, hi = a < bb ? bb : a;
+        Cx<Real> u[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) u[e] = U[gi][e];
+        const std::uint64_t ma = 1ull << a, mb = 1ull << bb;
+        for (std::uint64_t grp = threadIdx.x; grp < groups; grp += blockDim.x)
+        {
+            const std::uint64_t j0 = insert_zero(insert_zero(grp, lo), hi);
+            const std::uint64_t idx[4] = {j0, j0 | ma, j0 | mb, j0 | ma | mb};
+            Cx<Real> in[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) in[c] = tile[idx[c]];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+            {
+                Cx<Real> acc = cmul(u[4 * r], in[0]);
+                acc = cfma(u[4 * r + 1], in[1], acc);
+                acc = cfma(u[4 * r + 2], in[2], acc);
+                acc = cfma(u[4 * r + 3], in[3], acc);
+                tile[idx[r]] = acc;
+            }
+        }
+        __syncthreads();
+    }
+
+    const std::uint64_t nloc = 1ull << g.k;
+    const std::uint64_t cmask = (1ull << g.c) - 1ull;
+    for (std::uint64_t j = threadIdx.x; j < nloc; j += blockDim.x)
+        psi[base | seg[j >> g.c] | (j & cmask)] = tile[j];
+
+    if (fuse_hist)
+    {
+        const LayerMeas &M = meas[b * meas_stride];
+        if (M.nchunks > 0)
+        {
+            const std::uint64_t chunk = M.chunk[0];
+            int lm[kMaxLocal + 1];
+            int m_loc = 0;
+            for (int i = 0; i < g.k; ++i)
+                if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
+            double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+            tile_histogram(tile, g.k, lm, m_loc, part, red);
+        }
+    }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restrict__ states, int n, int kmax, int cmin,
+                                                       int ci, const Collapse *__restrict__ col_in,
+                                                       std::size_t col_stride, const LayerMeas *__restrict__ meas,
+                                                       std::size_t meas_stride, double *__restrict__ partials)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ PassGeom g;
+    __shared__ double red[kPassThreads / 32];
+    const int b = blockIdx.y;
+    const LayerMeas &M = meas[b * meas_stride];
+    if (ci >= M.nchunks) return;
+    const std::uint64_t chunk = M.chunk[ci];
+    if (threadIdx.x == 0) histogram_geometry(n, kmax, cmin, chunk, g);
+    __syncthreads();
+    Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
+    std::uint32_t *seg = reinterpret_cast<std::uint32_t *>(smem_raw + (sizeof(Cx<Real>) << g.k));
+    const std::uint64_t tix = blockIdx.x;
+    const std::uint64_t dim = 1ull << n;
+    const Cx<Real> *psi = states + static_cast<std::size_t>(b) * dim;
+    const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+    const int h = g.k - g.c;
+    for (std::uint32_t s = threadIdx.x; s < (1u << h); s += blockDim.x)
+        seg[s] = static_cast<std::uint32_t>(scatter_bits(s, g.pos + g.c, h));
+    Collapse cl{0, 0, 1.0, 0.0};
+    const bool has_col = col_in != nullptr;
+    if (has_col) cl = col_in[b * col_stride];
+    __syncthreads();
+    load_tile(tile, psi, g, base, seg, cl, has_col);
+    __syncthreads();
+    int lm[kMaxLocal + 1];
+    int m_loc = 0;
+    for (int i = 0; i < g.k; ++i)
+        if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
+    double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+    tile_histogram(tile, g.k, lm, m_loc, part, red);
+}
+
+// One block per trajectory: gather the chunk's joint histogram from the tile
+// partials in a fixed order, sample the outcome exactly as the reference's
+// host CDF scan does, and record the collapse.
+__global__ void __launch_bounds__(kMeasureThreads)
+    k_measure(int n, PassGeom fg, int fused, int kmax, int cmin, int ci, const LayerMeas *__restrict__ meas,
+              std::size_t meas_stride, const double *__restrict__ partials, double *__restrict__ bins_scratch,
+              std::size_t bins_stride, const std::uint64_t *__restrict__ forced, std::size_t forced_stride, Collapse *__restrict__ col,
+              std::size_t col_stride, LayerResult *__restrict__ res, std::size_t res_stride, int *__restrict__ err)
+{
+    __shared__ PassGeom g;
+    __shared__ double sbins[kSmemBins];
+    __shared__ double seg_sum[kMeasureThreads];
+    __shared__ int lm_bit[kMaxLocal + 1], hm_pos[kMaxQubits], hm_bit[kMaxQubits];
+    __shared__ int s_mloc, s_mhi;
+    __shared__ std::uint64_t s_chosen;
+    __shared__ double s_branch, s_total;
+
+    const int b = blockIdx.x;
+    const LayerMeas &M = meas[b * meas_stride];
+    if (ci >= M.nchunks) return;
+    const std::uint64_t chunk = M.chunk[ci];
+    const int m = __popcll(chunk);
+    const int tid = threadIdx.x;
+    const int T = blockDim.x;
+    if (tid == 0)
+    {
+        if (fused)
+            g = fg;
+        else
+            histogram_geometry(n, kmax, cmin, chunk, g);
+        int ml = 0, mh = 0;
+        for (int i = 0; i < g.k; ++i)
+            if ((chunk >> g.pos[i]) & 1ull) lm_bit[ml++] = __popcll(chunk & ((1ull << g.pos[i]) - 1ull));
+        for (int i = 0; i < g.n_nl; ++i)
+            if ((chunk >> g.nl[i]) & 1ull)
+            {
+                hm_pos[mh] = i;
+                hm_bit[mh++] = __popcll(chunk & ((1ull << g.nl[i]) - 1ull));
+            }
+        s_mloc = ml;
+        s_mhi = mh;
+    }
+    __syncthreads();
+    const int m_loc = s_mloc, m_hi = s_mhi;
+    const std::uint64_t NB = 1ull << m;
+    const std::uint64_t per_bin_tiles = 1ull << (g.n_nl - m_hi);
+    const double *part = partials + static_cast<std::size_t>(b) * kHistScratch;
+    double *bins = NB <= kSmemBins ? sbins : bins_scratch + static_cast<std::size_t>(b) * bins_stride;
+
+    for (std::uint64_t B = tid; B < NB; B += T)
+    {
+        std::uint64_t bl = 0, th = 0;
+        for (int i = 0; i < m_loc; ++i) bl |= ((B >> lm_bit[i]) & 1ull) << i;
+        for (int i = 0; i < m_hi; ++i) th |= ((B >> hm_bit[i]) & 1ull) << hm_pos[i];
+        double s = 0.0;
+        for (std::uint64_t r = 0; r < per_bin_tiles; ++r)
+        {
+            std::uint64_t t = r;
+            for (int i = 0; i < m_hi; ++i) t = insert_zero(t, hm_pos[i]);
+            s += part[((t | th) << m_loc) + bl];
+        }
+        bins[B] = s;
+    }
+    __syncthreads();
+
+    // Contiguous segments of bins, one per participating thread.
+    const std::uint64_t P = NB < static_cast<std::uint64_t>(T) ? NB : static_cast<std::uint64_t>(T);
+    const std::uint64_t S = (NB + P - 1) / P;
+    if (static_cast<std::uint64_t>(tid) < P)
+    {
+        double s = 0.0;
+        const std::uint64_t lo = tid * S, hi = (tid + 1) * S < NB ? (tid + 1) * S : NB;
+        for (std::uint64_t i = lo; i < hi; ++i) s += bins[i];
+        seg_sum[tid] = s;
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        double total = 0.0;
+        for (std::uint64_t i = 0; i < P; ++i) total += seg_sum[i];
+        std::uint64_t chosen = NB - 1;
+        bool bad = !(total > 0.0) || !isfinite(total);
+        if (forced != nullptr)
+        {
+            const std::uint64_t f = forced[b * forced_stride];
+            chosen = 0;
+            int j = 0;
+            for (int q = 0; q < n; ++q)
+                if ((chunk >> q) & 1ull) chosen |= ((f >> q) & 1ull) << j++;
+        }
+        else if (!bad)
+        {
+            const double draw = M.uniform[ci] * total;
+            double run = 0.0;
+            std::uint64_t segi = P;
+            for (std::uint64_t i = 0; i < P; ++i)
+            {
+                if (draw < run + seg_sum[i])
+                {
+                    segi = i;
+                    break;
+                }
+                run += seg_sum[i];
+            }
+            if (segi < P)
+            {
+                const std::uint64_t lo = segi * S, hi = (segi + 1) * S < NB ? (segi + 1) * S : NB;
+                for (std::uint64_t i = lo; i < hi; ++i)
+                {
+                    run += bins[i];
+                    if (draw < run)
+                    {
+                        chosen = i;
+                        break;
+                    }
+                }
+            }
+        }
+        double branch = bins[chosen];
+        if (!bad && !(branch > 0.0) && forced == nullptr)
+        {
+            // Numerically starved bin: take the heaviest (first on ties).
+            std::uint64_t best = 0;
+            for (std::uint64_t i = 1; i < NB; ++i)
+                if (bins[i] > bins[best]) best = i;
+            chosen = best;
+            branch = bins[best];
+        }
+        if (!(branch > 0.0)) bad = true;
+        s_chosen = chosen;
+        s_branch = branch;
+        s_total = total;
+        if (bad) atomicOr(err, 1);
+    }
+    __syncthreads();
+    if (tid == 0)
+    {
+        const std::uint64_t chosen = s_chosen;
+        const double branch = s_branch, total = s_total;
+        std::uint64_t val = 0;
+        int j = 0;
+        for (int q = 0; q < n; ++q)
+            if ((chunk >> q) & 1ull) val |= ((chosen >> j++) & 1ull) << q;
+        const bool ok = branch > 0.0 && total > 0.0 && isfinite(total);
+        const double scale = ok ? 1.0 / sqrt(branch) : 1.0;
+        Collapse &c = col[b * col_stride];
+        if (ci == 0)
+        {
+            c.mask = chunk;
+            c.value = val;
+            c.scale = scale;
+        }
+        else
+        {
+            c.mask |= chunk;
+            c.value |= val;
+            c.scale *= scale;
+        }
+        LayerResult &r = res[b * res_stride];
+        r.outcome |= val;
+        const double pr = ok ? branch / total : 0.0;
+        r.prob[ci] = pr;
+        r.surprisal += ok ? -log(pr) : 0.0;
+    }
+}
+
+template <typename Real>
+__global__ void k_init_zero(Cx<Real> *states, std::uint64_t dim, std::uint64_t total)
+{
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+        states[i] = Cx<Real>{(i % dim) == 0 ? Real(1) : Real(0), Real(0)};
+}
+
+template <typename Real>
+__global__ void k_collapse(Cx<Real> *states, std::uint64_t dim, std::uint64_t total, const Collapse *col,
+                           std::size_t col_stride)
+{
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const Collapse cl = col[(i / dim) * col_stride];
+        states[i] = collapse_value(states[i], i % dim, cl, static_cast<Real>(cl.scale));
+    }
+}
+
+int grid_for(std::uint64_t total, int threads)
+{
+    const std::uint64_t blocks = (total + threads - 1) / threads;
+    return static_cast<int>(std::min<std::uint64_t>(blocks, 152ull * 32ull));
+}
+
+template <typename Real>
+std::size_t pass_smem(int k)
+{
+    return (sizeof(Cx<Real>) << k) + (sizeof(std::uint32_t) << k);
+}
+
+template <typename Real>
+cudaError_t ensure_smem_attr(const void *fn, std::size_t bytes)
+{
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+} // namespace
+
+__host__ __device__ void histogram_geometry(int n, int kmax, int cmin, std::uint64_t chunk, PassGeom &g)
+{
+    const int k = kmax < n ? kmax : n;
+    const int c0 = cmin < k ? cmin : k;
+    std::uint64_t used = (c0 >= 64) ? ~0ull : ((1ull << c0) - 1ull);
+    int cnt = c0;
+    for (int q = c0; q < n && cnt < k; ++q)
+        if (!((chunk >> q) & 1ull))
+        {
+            used |= 1ull << q;
+            ++cnt;
+        }
+    for (int q = c0; q < n && cnt < k; ++q)
+        if (!((used >> q) & 1ull))
+        {
+            used |= 1ull << q;
+            ++cnt;
+        }
+    g.n = n;
+    g.k = k;
+    int a = 0, z = 0;
+    for (int q = 0; q < n; ++q)
+    {
+        if ((used >> q) & 1ull)
+            g.pos[a++] = static_cast<std::int8_t>(q);
+        else
+            g.nl[z++] = static_cast<std::int8_t>(q);
+    }
+    int c = 0;
+    while (c < k && g.pos[c] == c) ++c;
+    g.c = c;
+    g.n_nl = n - k;
+}
+
+int local_measured_count(const PassGeom &g, std::uint64_t chunk)
+{
+    int m = 0;
+    for (int i = 0; i < g.k; ++i)
+        if ((chunk >> g.pos[i]) & 1ull) ++m;
+    return m;
+}
+
+namespace
+{
+PassGeom make_geom(int n, std::uint64_t local)
+{
+    PassGeom g{};
+    g.n = n;
+    int a = 0, z = 0;
+    for (int q = 0; q < n; ++q)
+    {
+        if ((local >> q) & 1ull)
+            g.pos[a++] = static_cast<std::int8_t>(q);
+        else
+            g.nl[z++] = static_cast<std::int8_t>(q);
+    }
+    g.k = a;
+    g.n_nl = z;
+    int c = 0;
+    while (c < a && g.pos[c] == c) ++c;
+    g.c = c;
+    return g;
+}
+
+int local_index(const PassGeom &g, int q)
+{
+    for (int i = 0; i < g.k; ++i)
+        if (g.pos[i] == q) return i;
+    return -1;
+}
+
+// Greedy packing of `todo` bonds into passes that each keep qubits
+// 0..cmin-1 local; returns the passes and fills their gate lists.
+std::vector<PassPlan> pack(int n, const std::vector<Bond> &bonds, std::vector<int> todo, int kmax, int cmin,
+                           std::uint64_t first_local)
+{
+    std::vector<PassPlan> out;
+    std::uint64_t local = first_local;
+    bool first = first_local != 0;
+    while (!todo.empty())
+    {
+        if (!first) local = (1ull << std::min(cmin, n)) - 1ull;
+        std::vector<int> taken, rest;
+        for (int i : todo)
+        {
+            const std::uint64_t need = local | (1ull << bonds[i].q0) | (1ull << bonds[i].q1);
+            if (__builtin_popcountll(need) <= kmax && (taken.size() < static_cast<std::size_t>(kMaxPassGates)))
+            {
+                if (first && (need != local))
+                {
+                    rest.push_back(i);
+                    continue;
+                }
+                local = need;
+                taken.push_back(i);
+            }
+            else
+            {
+                rest.push_back(i);
+            }
+        }
+        if (taken.empty() && !first) throw std::runtime_error("bond does not fit a pass");
+        // Widen the tile with further low qubits (longer contiguous runs).
+        for (int q = 0; q < n && __builtin_popcountll(local) < kmax; ++q) local |= 1ull << q;
+        PassPlan p{};
+        p.geom = make_geom(n, local);
+        p.gates.count = static_cast<int>(taken.size());
+        for (std::size_t j = 0; j < taken.size(); ++j)
+        {
+            p.gates.gate[j] = static_cast<std::int16_t>(taken[j]);
+            p.gates.la[j] = static_cast<std::int8_t>(local_index(p.geom, bonds[taken[j]].q0));
+            p.gates.lb[j] = static_cast<std::int8_t>(local_index(p.geom, bonds[taken[j]].q1));
+        }
+        if (!taken.empty()) out.push_back(p);
+        todo = rest;
+        first = false;
+    }
+    return out;
+}
+} // namespace
+
+std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin)
+{
+    if (n > 32) throw std::invalid_argument("engine supports at most 32 qubits");
+    kmax = std::min(kmax, n);
+    std::vector<int> all(bonds.size());
+    for (std::size_t i = 0; i < bonds.size(); ++i) all[i] = static_cast<int>(i);
+    if (bonds.empty())
+    {
+        PassPlan p{};
+        p.geom = make_geom(n, (1ull << kmax) - 1ull);
+        p.gates.count = 0;
+        return {p};
+    }
+    // Try first tiles made of a low contiguous block, optionally with the top
+    // qubit (for a ring-closing bond), and keep the plan with fewest passes.
+    std::vector<PassPlan> best;
+    for (int c0 = kmax; c0 >= std::max(1, kmax - 3); --c0)
+    {
+        for (int wrap = 0; wrap < 2; ++wrap)
+        {
+            std::uint64_t local = (1ull << c0) - 1ull;
+            if (wrap)
+            {
+                if (c0 >= kmax || c0 >= n) continue;
+                local |= 1ull << (n - 1);
+            }
+            auto plan = pack(n, bonds, all, kmax, cmin, local);
+            if (best.empty() || plan.size() < best.size()) best = plan;
+        }
+    }
+    return best;
+}
+
+template <typename Real>
+cudaError_t launch_init_zero(Cx<Real> *states, std::uint64_t dim, int batch, cudaStream_t s)
+{
+    const std::uint64_t total = dim * static_cast<std::uint64_t>(batch);
+    k_init_zero<Real><<<grid_for(total, 256), 256, 0, s>>>(states, dim, total);
+    return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
+                        std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
+                        const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
+                        cudaStream_t s)
+{
+    const std::size_t smem = pass_smem<Real>(plan.geom.k);
+    cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass<Real>), smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(1u << plan.geom.n_nl, batch);
+    k_pass<Real><<<grid, kPassThreads, smem, s>>>(states, plan.geom, plan.gates, layer_gates, gate_stride,
+                                                  collapse_in, collapse_stride, meas, meas_stride, partials,
+                                                  fuse_hist);
+    return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
+                        const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
+                        std::size_t meas_stride, double *partials, cudaStream_t s)
+{
+    const int k = std::min(kmax, n);
+    const std::size_t smem = pass_smem<Real>(k);
+    cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_hist<Real>), smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(1u << (n - k), batch);
+    k_hist<Real><<<grid, kPassThreads, smem, s>>>(states, n, kmax, cmin, chunk_index, collapse_in, collapse_stride,
+                                                  meas, meas_stride, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_measure(int batch, int n, const PassGeom *fused_geom, int kmax, int cmin, int chunk_index,
+                           const LayerMeas *meas, std::size_t meas_stride, const double *partials,
+                           double *bins_scratch, std::size_t bins_stride, const std::uint64_t *forced,
+                           std::size_t forced_stride, Collapse *collapse_out, std::size_t collapse_stride,
+                           LayerResult *result, std::size_t result_stride, int *error_flag, cudaStream_t s)
+{
+    PassGeom fg{};
+    if (fused_geom) fg = *fused_geom;
+    k_measure<<<batch, kMeasureThreads, 0, s>>>(n, fg, fused_geom != nullptr, kmax, cmin, chunk_index, meas,
+                                                meas_stride, partials, bins_scratch, bins_stride, forced,
+                                                forced_stride,
+                                                collapse_out, collapse_stride, result, result_stride, error_flag);
+    return cudaGetLastError();
+}
+
+template <typename Real>
+cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, const Collapse *collapse,
+                            std::size_t collapse_stride, cudaStream_t s)
+{
+    const std::uint64_t total = dim * static_cast<std::uint64_t>(batch);
+    k_collapse<Real><<<grid_for(total, 256), 256, 0, s>>>(states, dim, total, collapse, collapse_stride);
+    return cudaGetLastError();
+}
+
+#define MG_INSTANTIATE(R)                                                                                        \
+    template cudaError_t launch_init_zero<R>(Cx<R> *, std::uint64_t, int, cudaStream_t);                         \
+    template cudaError_t launch_pass<R>(Cx<R> *, int, const PassPlan &, const Cx<R> *, std::size_t,              \
+                                        const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
+                                        int, cudaStream_t);                                                      \
+    template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
+                                        const LayerMeas *, std::size_t, double *, cudaStream_t);                 \
+    template cudaError_t launch_collapse<R>(Cx<R> *, std::uint64_t, int, const Collapse *, std::size_t,          \
+                                            cudaStream_t);
+MG_INSTANTIATE(float)
+MG_INSTANTIATE(double)
+#undef MG_INSTANTIATE
+
+} // namespace mg

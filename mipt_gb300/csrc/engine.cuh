@@ -1,0 +1,104 @@
+// State-vector engine for batches of monitored-circuit trajectories.
+//
+// Layout in HBM: trajectory b's state is the contiguous array
+// states[b * 2^n .. (b+1) * 2^n) of interleaved complex amplitudes (float2 for
+// the FP32 path, double2 for FP64); qubit q is bit q of the amplitude index
+// (the little-endian convention of the reference, cpp/include/mipt/cusv/matrix.hpp:5-13).
+//
+// One brickwork layer is applied in one or more tiled passes. A pass loads a
+// tile of 2^k amplitudes whose local qubits hold every bond the pass applies,
+// applies those bonds in shared memory and stores the tile back, so each pass
+// is one read and one write of the state. The last pass of a layer also
+// accumulates the Born histogram of the layer's measured sites; the measured
+// outcome is sampled on the device and the collapse is applied while the next
+// pass loads its tiles, so a measurement costs no extra sweep of the state.
+#pragma once
+
+#include "common.cuh"
+
+#include <cuda_runtime.h>
+#include <vector>
+
+namespace mg
+{
+
+struct Bond
+{
+    int q0, q1; // matrix index bit 0 <-> q0, bit 1 <-> q1
+};
+
+struct PassPlan
+{
+    PassGeom geom;
+    PassGates gates;
+};
+
+// Splits one layer's bonds into tiled passes of at most kmax local qubits
+// with at least cmin contiguous low qubits per tile (for coalescing).
+std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin);
+
+// Tile geometry used for a stand-alone histogram of the sites in `chunk`:
+// low contiguous qubits, then as many unmeasured qubits as fit, so that few
+// measured sites are tile-local.
+__host__ __device__ void histogram_geometry(int n, int kmax, int cmin, std::uint64_t chunk, PassGeom &g);
+
+// Device scratch needed per trajectory for histogram partials.
+constexpr std::size_t kHistScratch = std::size_t{1} << 20; // doubles
+constexpr int kMaxChunks = 8;
+
+// Per-(trajectory, layer) measurement record on the device.
+struct LayerMeas
+{
+    std::uint64_t chunk[kMaxChunks]; // measured sites of each chunk (bit = qubit)
+    double uniform[kMaxChunks];
+    int nchunks;
+    int pad;
+};
+
+struct LayerResult
+{
+    std::uint64_t outcome;   // bit q = measured value of site q (0 where unmeasured)
+    double surprisal;        // -log P(joint outcome of the layer)
+    double prob[kMaxChunks]; // branch / total of each chunk
+};
+
+template <typename Real>
+struct EngineLaunch
+{
+    Cx<Real> *states;
+    std::uint64_t dim;
+    int batch;
+};
+
+// Kernel launchers (engine.cu).
+template <typename Real>
+cudaError_t launch_init_zero(Cx<Real> *states, std::uint64_t dim, int batch, cudaStream_t s);
+
+template <typename Real>
+cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
+                        std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
+                        const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
+                        cudaStream_t s);
+
+template <typename Real>
+cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
+                        const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
+                        std::size_t meas_stride, double *partials, cudaStream_t s);
+
+// Samples (or replays) the outcome of chunk `chunk_index` from the partial
+// histograms, writes the combined collapse of the layer and the outcome.
+cudaError_t launch_measure(int batch, int n, const PassGeom *fused_geom, int kmax, int cmin, int chunk_index,
+                           const LayerMeas *meas, std::size_t meas_stride, const double *partials,
+                           double *bins_scratch, std::size_t bins_stride, const std::uint64_t *forced,
+                           std::size_t forced_stride,
+                           Collapse *collapse_out, std::size_t collapse_stride, LayerResult *result,
+                           std::size_t result_stride, int *error_flag, cudaStream_t s);
+
+template <typename Real>
+cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, const Collapse *collapse,
+                            std::size_t collapse_stride, cudaStream_t s);
+
+// Host helper: local positions of `chunk` within geometry g.
+int local_measured_count(const PassGeom &g, std::uint64_t chunk);
+
+} // namespace mg

@@ -1,0 +1,82 @@
+// Reduced density matrices, purities, entropies and three-site blocks of
+// batched state vectors.
+#pragma once
+
+#include "common.cuh"
+
+#include <cuda_runtime.h>
+#include <vector>
+
+namespace mg
+{
+
+// One reduced-density-matrix request: rho = M M^H over the retained modes
+// kept[0..k) (row index bit i <-> kept[i]); the environment is the
+// complement in ascending mode order (the reference's Schmidt layout,
+// cpp/include/mipt/cuda/schmidt_gram.cuh:13-19). With `fermion`, M[r][e]
+// changes sign once per occupied environment mode below each occupied kept
+// mode (schmidt_gram.cuh:196-249).
+struct GramJob
+{
+    int traj;
+    int k;
+    int fermion;
+    int rows_fastest; // kept set contains qubit 0 -> gather along rows
+    std::int8_t kept[32];
+    std::int8_t env[32];
+    std::uint64_t below[32];
+};
+
+GramJob make_gram_job(int traj, int n, const int *kept, int k, bool fermion);
+
+constexpr int kGramTile = 64;
+
+// Number of lower-triangle 64x64 tiles of a d x d matrix.
+inline int gram_tiles(int k)
+{
+    const int t = (k >= 6) ? (1 << (k - 6)) : 1;
+    return t * (t + 1) / 2;
+}
+
+// rho for every job (all jobs share k): full FP64 d x d Hermitian matrices
+// written to rho_out[job][d][d] (row-major complex).
+template <typename Real>
+cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                     const Collapse *collapse, std::size_t collapse_stride, double *rho_out, void *scratch,
+                     std::size_t scratch_bytes, cudaStream_t s);
+
+// Purity Tr(rho^2) of every job without materialising rho.
+template <typename Real>
+cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                        const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
+                        std::size_t scratch_bytes, cudaStream_t s);
+
+std::size_t gram_scratch_bytes(int n, int k, int njobs, bool rho);
+
+// Purity of full matrices rho[job][d][d].
+cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, cudaStream_t s);
+
+// Von Neumann entropies (bits) of Hermitian matrices rho[job][d][d] for
+// d <= 64, by a parallel-order complex Jacobi eigensolver in FP64.
+cudaError_t jacobi_entropy(const double *rho, int d, int njobs, double *entropy_out, double *eig_out,
+                           cudaStream_t s);
+
+// Three-site RDMs of every trajectory, for `count` triples subs[3*i..].
+// out[traj][i][8][8] complex row-major. fermion selects the fermionic trace
+// of the reference's three-site sweep (cpp/src/cuda/rho_reduce.cu:49-110).
+template <typename Real>
+cudaError_t rho3_sweep(const Cx<Real> *states, int n, int batch, const int *d_subs, int count, int fermion,
+                       const Collapse *collapse, std::size_t collapse_stride, double *out, void *scratch,
+                       std::size_t scratch_bytes, cudaStream_t s);
+std::size_t rho3_scratch_bytes(int n, int batch, int count);
+
+// S_2 = -log2(purity) with the reference's clamps (purity >= 1 -> 0,
+// |S| < 1e-12 -> 0; cpp/include/mipt/tmi/linalg.hpp:134-141,201-208).
+__host__ __device__ inline double renyi2_from_purity(double purity)
+{
+    if (!(purity > 0.0) || purity >= 1.0) return 0.0;
+    const double s = -log2(purity);
+    return (s < 1e-12 && s > -1e-12) ? 0.0 : s;
+}
+
+} // namespace mg

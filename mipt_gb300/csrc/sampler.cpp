@@ -1,0 +1,180 @@
+#include "sampler.hpp"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <random>
+#include <stdexcept>
+#include <thread>
+
+namespace mg
+{
+
+std::uint64_t splitmix64(std::uint64_t v)
+{
+    v += 0x9e3779b97f4a7c15ull;
+    v = (v ^ (v >> 30)) * 0xbf58476d1ce4e5b9ull;
+    v = (v ^ (v >> 27)) * 0x94d049bb133111ebull;
+    return v ^ (v >> 31);
+}
+
+std::uint64_t trajectory_seed(std::uint64_t master, std::uint64_t index)
+{
+    return splitmix64(master + 0x2545f4914f6cdd1dull * (index + 1ull));
+}
+
+namespace
+{
+using C = std::complex<double>;
+
+void seed_mt(std::mt19937 &rng, std::uint64_t v)
+{
+    std::seed_seq seq{static_cast<std::uint32_t>(v & 0xffffffffu), static_cast<std::uint32_t>(v >> 32)};
+    rng.seed(seq);
+}
+
+// Gram-Schmidt of four complex Gaussian columns into a Haar unitary,
+// row-major; writes into u[16]. Each column entry takes two normal draws,
+// imaginary part first (the order the g++-built reference evaluates
+// ComplexD(normal(rng), normal(rng)) in).
+void gram_schmidt_u4(std::mt19937 &rng, std::normal_distribution<double> &gauss, C *u)
+{
+    int col = 0;
+    while (col < 4)
+    {
+        C v[4];
+        for (auto &x : v)
+        {
+            const double im = gauss(rng);
+            const double re = gauss(rng);
+            x = C(re, im);
+        }
+        for (int k = 0; k < col; ++k)
+        {
+            C proj(0.0, 0.0);
+            for (int r = 0; r < 4; ++r) proj += std::conj(u[4 * r + k]) * v[r];
+            for (int r = 0; r < 4; ++r) v[r] -= u[4 * r + k] * proj;
+        }
+        double norm2 = 0.0;
+        for (const auto &x : v) norm2 += std::norm(x);
+        const double len = std::sqrt(norm2);
+        if (len < 1e-14) continue; // redraw this column
+        for (int r = 0; r < 4; ++r) u[4 * r + col] = v[r] / len;
+        ++col;
+    }
+}
+
+// The reference splits each drawn unitary with a cosine-sine decomposition
+// and redraws when a cosine or sine of the split falls below 1e-12. The
+// cosines squared are the eigenvalues of X^H X for the top-left block X.
+bool csd_is_singular(const C *u)
+{
+    const double a = std::norm(u[0]) + std::norm(u[4]);
+    const double d = std::norm(u[1]) + std::norm(u[5]);
+    const C b = std::conj(u[0]) * u[1] + std::conj(u[4]) * u[5];
+    const double root = std::sqrt(std::max(0.0, (a - d) * (a - d) + 4.0 * std::norm(b)));
+    const double hi = std::clamp(0.5 * (a + d + root), 0.0, 1.0);
+    const double lo = std::clamp(0.5 * (a + d - root), 0.0, 1.0);
+    const double tiny = 1e-12;
+    return std::sqrt(hi) < tiny || std::sqrt(lo) < tiny || std::sqrt(std::max(0.0, 1.0 - hi)) < tiny ||
+           std::sqrt(std::max(0.0, 1.0 - lo)) < tiny;
+}
+} // namespace
+
+void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool closed, int chunk_bits,
+                          TrajectoryDraw &out)
+{
+    if (n < 2 || n % 2 != 0 || n > 62) throw std::invalid_argument("Haar brickwork needs even 2 <= n <= 62");
+    if (chunk_bits < 1) throw std::invalid_argument("chunk_bits must be positive");
+    std::mt19937 gates_rng, meas_rng;
+    seed_mt(gates_rng, seed);
+    seed_mt(meas_rng, splitmix64(seed ^ 0xa0761d0dull));
+
+    const int T = 2 * periods;
+    const int mb = n / 2;
+    out.n = n;
+    out.layers = T;
+    out.max_bonds = mb;
+    out.bond_count.assign(T, 0);
+    out.bond_q.assign(static_cast<std::size_t>(T) * mb * 2, 0);
+    out.bond_u.assign(static_cast<std::size_t>(T) * mb * 16, C(0.0, 0.0));
+    out.measured.assign(T, 0);
+    out.uniforms.clear();
+    out.uniform_offset.assign(T + 1, 0);
+
+    std::uniform_real_distribution<double> unif(0.0, 1.0);
+    for (int t = 0; t < T; ++t)
+    {
+        const int start = t & 1;
+        const int stop = (closed && start == 1 && n > 2) ? n : n - 1;
+        int j = 0;
+        for (int i = start; i < stop; i += 2, ++j)
+        {
+            C *u = &out.bond_u[(static_cast<std::size_t>(t) * mb + j) * 16];
+            do
+            {
+                // A fresh distribution per draw, as the reference constructs one
+                // inside haar_unitary_4 (its cached second normal is dropped).
+                std::normal_distribution<double> gauss(0.0, 1.0);
+                gram_schmidt_u4(gates_rng, gauss, u);
+            } while (csd_is_singular(u));
+            out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2] = i;
+            out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2 + 1] = (i + 1) % n;
+        }
+        out.bond_count[t] = j;
+        std::uint64_t mask = 0;
+        if (p >= 1.0)
+        {
+            mask = (n == 64) ? ~0ull : ((1ull << n) - 1ull);
+        }
+        else if (p > 0.0)
+        {
+            std::bernoulli_distribution flag(p);
+            for (int s = 0; s < n; ++s)
+                if (flag(gates_rng)) mask |= 1ull << s;
+        }
+        out.measured[t] = mask;
+        out.uniform_offset[t] = static_cast<int>(out.uniforms.size());
+        const int m = __builtin_popcountll(mask);
+        for (int c = 0; c < m; c += chunk_bits) out.uniforms.push_back(unif(meas_rng));
+    }
+    out.uniform_offset[T] = static_cast<int>(out.uniforms.size());
+}
+
+void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, bool closed,
+                     int chunk_bits, std::vector<TrajectoryDraw> &out, int threads)
+{
+    out.resize(count);
+    if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    threads = std::min(threads, std::max(1, count));
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto work = [&]() {
+        for (;;)
+        {
+            const int i = next.fetch_add(1);
+            if (i >= count) return;
+            try
+            {
+                draw_haar_trajectory(seeds[i], n, periods, p[i], closed, chunk_bits, out[i]);
+            }
+            catch (...)
+            {
+                failed = true;
+            }
+        }
+    };
+    if (threads == 1)
+    {
+        work();
+    }
+    else
+    {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; ++t) pool.emplace_back(work);
+        for (auto &th : pool) th.join();
+    }
+    if (failed) throw std::runtime_error("trajectory draw failed");
+}
+
+} // namespace mg

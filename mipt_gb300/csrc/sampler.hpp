@@ -1,0 +1,52 @@
+// Host-side trajectory sampler: seeded Haar brickwork layer draws and the
+// measurement uniforms, reproducing the reference's random streams.
+//
+// Reference behaviour this follows (paths inside the reference project):
+//   seeding::splitmix64, trajectory_seed          cpp/include/mipt/types.hpp:262-273
+//   Circuit1D::seed (layer and measurement mt19937 streams)
+//                                                 cpp/include/mipt/circuit.hpp:129-140
+//   fill_haar_layer / build_haar_layers            cpp/include/mipt/circuits/haar.hpp:226-305
+//   haar_unitary_4                                 cpp/include/mipt/circuits/haar.hpp:39-85
+//   random_haar_bond_gate retry rule               cpp/include/mipt/circuits/haar.hpp:171-181,211-224
+//   Engine::measure_layer uniform draws            cpp/include/mipt/cusv/engine.hpp:300-327
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <vector>
+
+namespace mg
+{
+
+std::uint64_t splitmix64(std::uint64_t v);
+std::uint64_t trajectory_seed(std::uint64_t master, std::uint64_t index);
+
+// One trajectory's complete random record. Layer t has gate_count(t) bonds;
+// bond j of layer t occupies qubits bond_q[2*(t*max_bonds+j) + {0,1}] and its
+// row-major 4x4 unitary (index bit 0 = first qubit) starts at
+// bond_u[16*(t*max_bonds+j)]. Measured sites of layer t are the set bits of
+// measured[t]; uniforms are consumed one per chunk of `chunk_bits` measured
+// sites, layer by layer, in order.
+struct TrajectoryDraw
+{
+    int n = 0;
+    int layers = 0;
+    int max_bonds = 0;
+    std::vector<int> bond_count;
+    std::vector<int> bond_q;
+    std::vector<std::complex<double>> bond_u;
+    std::vector<std::uint64_t> measured;
+    std::vector<double> uniforms;
+    std::vector<int> uniform_offset; // first uniform of layer t
+};
+
+// Draws a 1-D Haar brickwork trajectory (2*periods layers; odd layers close
+// the ring with bond (n-1, 0) when `closed`).
+void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool closed, int chunk_bits,
+                          TrajectoryDraw &out);
+
+// Draws many trajectories on `threads` host threads (0 = hardware count).
+void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, bool closed,
+                     int chunk_bits, std::vector<TrajectoryDraw> &out, int threads);
+
+} // namespace mg

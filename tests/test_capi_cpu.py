@@ -1,0 +1,63 @@
+"""CPU checks of the C-ABI library: it loads, exports every symbol the header
+declares, and its host sampler reproduces the reference's random record."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = np.load(os.path.join(ROOT, "tests", "golden", "ref_fixtures.npz"))
+
+
+@pytest.fixture(scope="module")
+def mg():
+    from mipt_gb300 import build
+    if not os.path.exists(build.LIB):
+        build.build()
+    import mipt_gb300
+    mipt_gb300.lib()
+    return mipt_gb300
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "mipt_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(mipt_(?:cuda|gb300)_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(mg):
+    lib = mg.lib()
+    names = header_symbols()
+    assert len(names) >= 35
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_seeding_matches_reference(mg):
+    for s, want in zip(GOLD["splitmix_in"], GOLD["splitmix_out"]):
+        assert mg.splitmix64(int(s)) == int(want)
+    for row, m in zip(GOLD["trajseed_out"], (0, 1, 0xDEADBEEF)):
+        assert [mg.trajectory_seed(m, i) for i in range(5)] == [int(x) for x in row]
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["draw_params"])))
+def test_host_sampler_matches_reference(mg, k):
+    seed, n, periods, p, closed, chunk = GOLD["draw_params"][k]
+    n, periods, chunk = int(n), int(periods), int(chunk)
+    d = mg.draw_haar(int(seed), n, periods, float(p), bool(closed), chunk)
+    np.testing.assert_array_equal(d["gates_per_layer"], GOLD[f"draw{k}_gates_per_layer"])
+    np.testing.assert_array_equal(d["bond_q"], GOLD[f"draw{k}_gate_q"])
+    np.testing.assert_allclose(d["bond_u"], GOLD[f"draw{k}_gate_m"], rtol=0, atol=1e-12)
+    sites = GOLD[f"draw{k}_sites"]
+    spl = GOLD[f"draw{k}_sites_per_layer"]
+    for t in range(2 * periods):
+        want = 0
+        for s in sites[t, : spl[t]]:
+            want |= 1 << int(s)
+        assert int(d["measured"][t]) == want
+    np.testing.assert_array_equal(d["uniforms"], GOLD[f"draw{k}_uniforms"])
+
+
+def test_bad_arguments_fail_loudly(mg):
+    with pytest.raises(mg.MiptError):
+        mg.draw_haar(1, 7, 2, 0.2)  # odd chain
