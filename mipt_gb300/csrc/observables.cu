@@ -96,11 +96,15 @@ __device__ __forceinline__ Cx<Real> gather(const Cx<Real> *__restrict__ psi, std
 
 // mode 0: write split partials of rho (full tile) to part_out;
 // mode 1: reduce the tile's contribution to Tr(rho^2) into pur_out.
-template <typename Real>
+// Acc is the accumulation type: FP64 whenever rho is materialised (its
+// small eigenvalues feed -lambda log lambda, so accumulation rounding must
+// stay below the state's own second-order error), the operand type for the
+// purity-only mode.
+template <typename Real, typename Acc>
 __global__ void __launch_bounds__(kGramThreads)
     k_gram(const Cx<Real> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
            const Collapse *__restrict__ col, std::size_t col_stride, int splits, std::uint64_t kchunk, int mode,
-           Real *__restrict__ part_out, double *__restrict__ pur_out)
+           Acc *__restrict__ part_out, double *__restrict__ pur_out)
 {
     constexpr int TK = GramK<Real>::TK;
     constexpr int KB = GramK<Real>::BITS;
@@ -163,11 +167,11 @@ __global__ void __launch_bounds__(kGramThreads)
 
     const Cx<Real> *psi = states + (static_cast<std::size_t>(J.traj) << n);
     const int ty = tid / 16, tx = tid % 16;
-    Real accr[4][4], acci[4][4];
+    Acc accr[4][4], acci[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) accr[i][j] = acci[i][j] = Real(0);
+        for (int j = 0; j < 4; ++j) accr[i][j] = acci[i][j] = Acc(0);
 
     for (std::uint64_t e0 = ebeg; e0 < eend; e0 += TK)
     {
@@ -216,11 +220,11 @@ __global__ void __launch_bounds__(kGramThreads)
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                 {
-                    // a * conj(b)
-                    accr[i][j] = fma(a[i].re, b[j].re, accr[i][j]);
-                    accr[i][j] = fma(a[i].im, b[j].im, accr[i][j]);
-                    acci[i][j] = fma(a[i].im, b[j].re, acci[i][j]);
-                    acci[i][j] = fma(-a[i].re, b[j].im, acci[i][j]);
+                    // a * conj(b); FP32 x FP32 products are exact in FP64
+                    accr[i][j] = fma(Acc(a[i].re), Acc(b[j].re), accr[i][j]);
+                    accr[i][j] = fma(Acc(a[i].im), Acc(b[j].im), accr[i][j]);
+                    acci[i][j] = fma(Acc(a[i].im), Acc(b[j].re), acci[i][j]);
+                    acci[i][j] = fma(-Acc(a[i].re), Acc(b[j].im), acci[i][j]);
                 }
         }
         __syncthreads();
@@ -228,7 +232,7 @@ __global__ void __launch_bounds__(kGramThreads)
 
     if (mode == 0)
     {
-        Real *out = part_out + (static_cast<std::size_t>(job) * splits + blockIdx.y) * static_cast<std::size_t>(d) * d * 2;
+        Acc *out = part_out + (static_cast<std::size_t>(job) * splits + blockIdx.y) * static_cast<std::size_t>(d) * d * 2;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -270,8 +274,7 @@ __global__ void __launch_bounds__(kGramThreads)
     }
 }
 
-template <typename Real>
-__global__ void k_gram_finalize(const Real *__restrict__ part, int d, int splits, int njobs, double *__restrict__ rho)
+__global__ void k_gram_finalize(const double *__restrict__ part, int d, int splits, int njobs, double *__restrict__ rho)
 {
     const std::uint64_t per = static_cast<std::uint64_t>(d) * d;
     const std::uint64_t total = per * njobs;
@@ -284,7 +287,7 @@ __global__ void k_gram_finalize(const Real *__restrict__ part, int d, int splits
         double sr = 0.0, si = 0.0;
         for (int z = 0; z < splits; ++z)
         {
-            const Real *p = part + ((job * splits + z) * per + rc) * 2;
+            const double *p = part + ((job * splits + z) * per + rc) * 2;
             sr += static_cast<double>(p[0]);
             si += static_cast<double>(p[1]);
         }
@@ -680,19 +683,19 @@ cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int n
 {
     if (njobs <= 0) return cudaSuccess;
     const int splits = gram_splits(n, k, njobs, true);
-    const std::size_t need = sizeof(Real) * 2 * static_cast<std::size_t>(splits) * njobs * (std::size_t{1} << (2 * k));
+    const std::size_t need = sizeof(double) * 2 * static_cast<std::size_t>(splits) * njobs * (std::size_t{1} << (2 * k));
     if (need > scratch_bytes) return cudaErrorInvalidValue;
     const std::uint64_t E = 1ull << (n - k);
     const std::uint64_t kchunk = (E + splits - 1) / splits;
     dim3 grid(gram_tiles(k), splits, njobs);
-    k_gram<Real><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0,
-                                               static_cast<Real *>(scratch), nullptr);
+    k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits, kchunk,
+                                                       0, static_cast<double *>(scratch), nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int d = 1 << k;
     const std::uint64_t total = static_cast<std::uint64_t>(d) * d * njobs;
     const int blocks = static_cast<int>(std::min<std::uint64_t>((total + 255) / 256, 152ull * 16));
-    k_gram_finalize<Real><<<blocks, 256, 0, s>>>(static_cast<const Real *>(scratch), d, splits, njobs, rho_out);
+    k_gram_finalize<<<blocks, 256, 0, s>>>(static_cast<const double *>(scratch), d, splits, njobs, rho_out);
     return cudaGetLastError();
 }
 
@@ -706,8 +709,8 @@ cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, in
     if (sizeof(double) * static_cast<std::size_t>(tiles) * njobs > scratch_bytes) return cudaErrorInvalidValue;
     const std::uint64_t E = 1ull << (n - k);
     dim3 grid(tiles, 1, njobs);
-    k_gram<Real><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, 1, E, 1, nullptr,
-                                               static_cast<double *>(scratch));
+    k_gram<Real, Real><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, 1, E, 1, nullptr,
+                                                     static_cast<double *>(scratch));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
