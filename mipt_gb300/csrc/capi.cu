@@ -792,7 +792,8 @@ int mipt_gb300_engine_apply_bonds(mipt_gb300_engine *e, const int *pairs, int nb
     std::vector<PassPlan> plan;
     try
     {
-        plan = plan_layer(e->n, bonds, default_tile_qubits(e->fp64), kCoalesceQubits);
+        plan = plan_layer(e->n, bonds, default_tile_qubits(e->fp64), kCoalesceQubits,
+                          e->fp64 ? register_bits<double>() : register_bits<float>());
     }
     catch (const std::exception &ex)
     {
@@ -923,7 +924,8 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
         for (int i = parity; i < stop; i += 2) bonds.push_back(Bond{i, (i + 1) % n});
         try
         {
-            b->plan[parity] = plan_layer(n, bonds, b->kmax, b->cmin);
+            b->plan[parity] = plan_layer(n, bonds, b->kmax, b->cmin,
+                                         cfg->fp64 ? register_bits<double>() : register_bits<float>());
         }
         catch (const std::exception &e)
         {

@@ -228,6 +228,250 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(Cx<Real> *__restrict__ st
     }
 }
 
+
+// Deterministic histogram over an array of squared magnitudes in shared
+// memory (same traversal as tile_histogram).
+template <typename T>
+__device__ void value_histogram(const T *val, int k, const int *lm, int m_loc, double *out, double *red)
+{
+    const int T_ = blockDim.x;
+    const int tid = threadIdx.x;
+    const std::uint64_t nb = 1ull << m_loc;
+    const std::uint64_t per_bin = 1ull << (k - m_loc);
+    if (nb <= static_cast<std::uint64_t>(T_))
+    {
+        const int G = T_ / static_cast<int>(nb);
+        const std::uint64_t bin = tid / G;
+        const int sub = tid % G;
+        std::uint64_t fixed = 0;
+        for (int i = 0; i < m_loc; ++i) fixed |= ((bin >> i) & 1ull) << lm[i];
+        Acc<T> acc;
+        for (std::uint64_t r = sub; r < per_bin; r += G)
+        {
+            std::uint64_t j = r;
+            for (int i = 0; i < m_loc; ++i) j = insert_zero(j, lm[i]);
+            acc.add(val[j | fixed]);
+        }
+        double v = acc.value();
+        const int width = G < 32 ? G : 32;
+        for (int off = width / 2; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off, width);
+        if (G <= 32)
+        {
+            if (sub == 0) out[bin] = v;
+        }
+        else
+        {
+            if ((tid & 31) == 0) red[tid >> 5] = v;
+            __syncthreads();
+            if (sub == 0)
+            {
+                double s = 0.0;
+                for (int w = 0; w < G / 32; ++w) s += red[(tid >> 5) + w];
+                out[bin] = s;
+            }
+        }
+    }
+    else
+    {
+        for (std::uint64_t bin = tid; bin < nb; bin += T_)
+        {
+            std::uint64_t fixed = 0;
+            for (int i = 0; i < m_loc; ++i) fixed |= ((bin >> i) & 1ull) << lm[i];
+            Acc<T> acc;
+            for (std::uint64_t r = 0; r < per_bin; ++r)
+            {
+                std::uint64_t j = r;
+                for (int i = 0; i < m_loc; ++i) j = insert_zero(j, lm[i]);
+                acc.add(val[j | fixed]);
+            }
+            out[bin] = acc.value();
+        }
+    }
+}
+
+// XOR swizzle of one local tile bit: bits >= 5 also flip low bit (p mod 5),
+// so any five lanes whose tile bits have distinct residues mod 5 touch
+// distinct shared-memory banks. Linear over GF(2): swz(a ^ b) = swz(a) ^ swz(b).
+__device__ __forceinline__ std::uint32_t swz1(int p)
+{
+    return (1u << p) ^ (p >= 5 ? (1u << (p % 5)) : 0u);
+}
+
+// Applies a 4x4 gate on register-index bits (2S, 2S+1); matrix index bit 0
+// is register bit 2S. All register indices are compile-time constants.
+template <int S, typename Real, int NA>
+__device__ __forceinline__ void apply_slot(Cx<Real> (&a)[NA], const Cx<Real> *__restrict__ Us)
+{
+    constexpr int lo = 2 * S;
+    Cx<Real> u[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) u[e] = Us[e];
+#pragma unroll
+    for (int g = 0; g < NA / 4; ++g)
+    {
+        const int base = ((g >> lo) << (lo + 2)) | (g & ((1 << lo) - 1));
+        const Cx<Real> in0 = a[base], in1 = a[base | (1 << lo)], in2 = a[base | (2 << lo)], in3 = a[base | (3 << lo)];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            Cx<Real> acc = cmul(u[4 * r], in0);
+            acc = cfma(u[4 * r + 1], in1, acc);
+            acc = cfma(u[4 * r + 2], in2, acc);
+            acc = cfma(u[4 * r + 3], in3, acc);
+            a[base | (r << lo)] = acc;
+        }
+    }
+}
+
+// One tiled pass with register rounds: global -> registers (lanes on the
+// contiguous low qubits), gates applied in registers, swizzled shared-memory
+// transposes between rounds, registers -> global, optional fused histogram.
+template <typename Real, int RB>
+__global__ void __launch_bounds__(256)
+    k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
+                  std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
+                  const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
+                  int fuse_hist)
+{
+    constexpr int NA = 1 << RB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
+    __shared__ Cx<Real> U[kMaxPassGates][16];
+    __shared__ double red[8];
+
+    const PassGeom &g = P.geom;
+    const int TB = g.k - RB;
+    const int tid = threadIdx.x;
+    const int b = blockIdx.y;
+    const std::uint64_t tix = blockIdx.x;
+    Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
+    const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+    for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
+        U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
+    Collapse cl{0, 0, 1.0, 0.0};
+    const bool has_col = col_in != nullptr;
+    if (has_col) cl = col_in[b * col_stride];
+    const Real scale = static_cast<Real>(cl.scale);
+
+    Cx<Real> amp[NA];
+    {
+        const Round &R = P.round[0];
+        std::uint64_t gt = base;
+        for (int i = 0; i < TB; ++i)
+            if ((tid >> i) & 1) gt |= 1ull << g.pos[R.tid[i]];
+        std::uint64_t gr[RB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[R.reg[i]];
+#pragma unroll
+        for (int r = 0; r < NA; ++r)
+        {
+            std::uint64_t gi = gt;
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+                if ((r >> i) & 1) gi |= gr[i];
+            Cx<Real> v = psi[gi];
+            if (has_col) v = collapse_value(v, gi, cl, scale);
+            amp[r] = v;
+        }
+    }
+    __syncthreads(); // gate matrices visible
+
+    for (int ri = 0; ri < P.rounds; ++ri)
+    {
+        const Round &R = P.round[ri];
+        if (ri > 0)
+        {
+            const Round &A = P.round[ri - 1];
+            std::uint32_t sa = 0, sb = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1)
+                {
+                    sa ^= swz1(A.tid[i]);
+                    sb ^= swz1(R.tid[i]);
+                }
+            std::uint32_t ra[RB], rb_[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+            {
+                ra[i] = swz1(A.reg[i]);
+                rb_[i] = swz1(R.reg[i]);
+            }
+            if (ri > 1) __syncthreads(); // previous round's reads are complete
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t p = sa;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) p ^= ra[i];
+                tile[p] = amp[r];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t p = sb;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) p ^= rb_[i];
+                amp[r] = tile[p];
+            }
+        }
+        if (R.slot[0] >= 0) apply_slot<0>(amp, U[R.slot[0]]);
+        if (RB >= 4 && R.slot[1] >= 0) apply_slot<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]]);
+        if (RB >= 6 && R.slot[2] >= 0) apply_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]]);
+    }
+
+    const Round &Z = P.round[P.rounds - 1];
+    {
+        std::uint64_t gt = base;
+        for (int i = 0; i < TB; ++i)
+            if ((tid >> i) & 1) gt |= 1ull << g.pos[Z.tid[i]];
+        std::uint64_t gr[RB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[Z.reg[i]];
+#pragma unroll
+        for (int r = 0; r < NA; ++r)
+        {
+            std::uint64_t gi = gt;
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+                if ((r >> i) & 1) gi |= gr[i];
+            psi[gi] = amp[r];
+        }
+    }
+
+    if (fuse_hist)
+    {
+        const LayerMeas &M = meas[b * meas_stride];
+        if (M.nchunks > 0)
+        {
+            __syncthreads(); // the tile buffer is free
+            Real *val = reinterpret_cast<Real *>(smem_raw);
+            std::uint32_t jt = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1) jt |= 1u << Z.tid[i];
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t j = jt;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) j |= 1u << Z.reg[i];
+                val[j] = norm2(amp[r]);
+            }
+            __syncthreads();
+            const std::uint64_t chunk = M.chunk[0];
+            int lm[kMaxLocal + 1];
+            int m_loc = 0;
+            for (int i = 0; i < g.k; ++i)
+                if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
+            double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+            value_histogram(val, g.k, lm, m_loc, part, red);
+        }
+    }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restrict__ states, int n, int kmax, int cmin,
                                                        int ci, const Collapse *__restrict__ col_in,
@@ -592,7 +836,145 @@ std::vector<PassPlan> pack(int n, const std::vector<Bond> &bonds, std::vector<in
 }
 } // namespace
 
-std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin)
+
+namespace
+{
+// Lane sets usable for the global load/store rounds: the four lowest tile
+// bits (contiguous qubits) plus one bit of residue 4 mod 5.
+std::uint32_t io_lanes(int k, std::uint32_t regmask)
+{
+    const std::uint32_t opts[2] = {0x1Fu, 0x20Fu};
+    for (std::uint32_t o : opts)
+    {
+        if ((o >> k) != 0) continue;
+        if ((o & regmask) == 0) return o;
+    }
+    return 0;
+}
+
+// Any five tile bits outside regmask with residues 0..4 mod 5 (one each).
+std::uint32_t mid_lanes(int k, std::uint32_t regmask)
+{
+    std::uint32_t out = 0;
+    for (int res = 0; res < 5; ++res)
+    {
+        int pick = -1;
+        for (int p = res; p < k; p += 5)
+            if (!((regmask >> p) & 1u))
+            {
+                pick = p;
+                break;
+            }
+        if (pick < 0) return 0;
+        out |= 1u << pick;
+    }
+    return out;
+}
+
+struct RoundSearch
+{
+    int k, rb, slots, nr;
+    std::vector<std::pair<int, int>> bonds;
+    std::vector<int> assign;
+    std::vector<int> load;
+};
+
+bool rounds_feasible(RoundSearch &S, std::vector<std::uint32_t> &lanes)
+{
+    lanes.assign(S.nr, 0);
+    for (int r = 0; r < S.nr; ++r)
+    {
+        std::uint32_t reg = 0;
+        for (std::size_t b = 0; b < S.bonds.size(); ++b)
+            if (S.assign[b] == r) reg |= (1u << S.bonds[b].first) | (1u << S.bonds[b].second);
+        const bool io = (r == 0 || r == S.nr - 1);
+        lanes[r] = io ? io_lanes(S.k, reg) : mid_lanes(S.k, reg);
+        if (lanes[r] == 0) return false;
+        if (S.nr == 1) lanes[r] = io_lanes(S.k, reg);
+    }
+    return true;
+}
+
+bool rounds_dfs(RoundSearch &S, std::size_t b, std::vector<std::uint32_t> &lanes)
+{
+    if (b == S.bonds.size()) return rounds_feasible(S, lanes);
+    for (int r = 0; r < S.nr; ++r)
+    {
+        if (S.load[r] >= S.slots) continue;
+        S.assign[b] = r;
+        ++S.load[r];
+        if (rounds_dfs(S, b + 1, lanes)) return true;
+        --S.load[r];
+    }
+    return false;
+}
+
+// Schedules a pass's bonds into register rounds; returns false when the tile
+// is too small or no schedule fits kMaxRounds.
+bool plan_rounds(PassPlan &p, int rb)
+{
+    const int k = p.geom.k;
+    p.rounds = 0;
+    p.rb = rb;
+    if (k < rb + 5 || k > 15) return false;
+    RoundSearch S;
+    S.k = k;
+    S.rb = rb;
+    S.slots = rb / 2;
+    for (int i = 0; i < p.gates.count; ++i) S.bonds.push_back({p.gates.la[i], p.gates.lb[i]});
+    const int nb = static_cast<int>(S.bonds.size());
+    std::vector<std::uint32_t> lanes;
+    for (int nr = std::max(1, (nb + S.slots - 1) / S.slots); nr <= kMaxRounds; ++nr)
+    {
+        S.nr = nr;
+        S.assign.assign(nb, -1);
+        S.load.assign(nr, 0);
+        if (!rounds_dfs(S, 0, lanes)) continue;
+        for (int r = 0; r < nr; ++r)
+        {
+            Round &R = p.round[r];
+            std::uint32_t used = lanes[r];
+            int slot = 0;
+            for (int s = 0; s < 3; ++s) R.slot[s] = -1;
+            for (int bI = 0; bI < nb; ++bI)
+                if (S.assign[bI] == r)
+                {
+                    R.reg[2 * slot] = static_cast<std::int8_t>(S.bonds[bI].first);
+                    R.reg[2 * slot + 1] = static_cast<std::int8_t>(S.bonds[bI].second);
+                    used |= (1u << S.bonds[bI].first) | (1u << S.bonds[bI].second);
+                    R.slot[slot] = static_cast<std::int16_t>(bI);
+                    ++slot;
+                }
+            // Fill the remaining register bits with free tile bits.
+            for (int i = 2 * slot; i < rb; ++i)
+                for (int q = 0; q < k; ++q)
+                    if (!((used >> q) & 1u))
+                    {
+                        R.reg[i] = static_cast<std::int8_t>(q);
+                        used |= 1u << q;
+                        break;
+                    }
+            // Lanes ordered by residue, then the warp bits.
+            int t = 0;
+            for (int res = 0; res < 5; ++res)
+                for (int q = res; q < k; q += 5)
+                    if ((lanes[r] >> q) & 1u)
+                    {
+                        R.tid[t++] = static_cast<std::int8_t>(q);
+                        break;
+                    }
+            for (int q = 0; q < k; ++q)
+                if (!((used >> q) & 1u)) R.tid[t++] = static_cast<std::int8_t>(q);
+            if (t != k - rb) return false;
+        }
+        p.rounds = nr;
+        return true;
+    }
+    return false;
+}
+} // namespace
+
+std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin, int rb)
 {
     if (n > 32) throw std::invalid_argument("engine supports at most 32 qubits");
     kmax = std::min(kmax, n);
@@ -603,6 +985,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
         PassPlan p{};
         p.geom = make_geom(n, (1ull << kmax) - 1ull);
         p.gates.count = 0;
+        plan_rounds(p, rb);
         return {p};
     }
     // Try first tiles made of a low contiguous block, optionally with the top
@@ -622,6 +1005,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
             if (best.empty() || plan.size() < best.size()) best = plan;
         }
     }
+    for (auto &p : best) plan_rounds(p, rb);
     return best;
 }
 
@@ -639,10 +1023,22 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
                         cudaStream_t s)
 {
+    dim3 grid(1u << plan.geom.n_nl, batch);
+    if (plan.rounds > 0)
+    {
+        constexpr int RB = register_bits<Real>();
+        if (plan.rb != RB) return cudaErrorInvalidValue;
+        const std::size_t smem = sizeof(Cx<Real>) << plan.geom.k;
+        cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, RB>), smem);
+        if (e != cudaSuccess) return e;
+        k_pass_rounds<Real, RB><<<grid, 1u << (plan.geom.k - RB), smem, s>>>(
+            states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
+            fuse_hist);
+        return cudaGetLastError();
+    }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
     cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass<Real>), smem);
     if (e != cudaSuccess) return e;
-    dim3 grid(1u << plan.geom.n_nl, batch);
     k_pass<Real><<<grid, kPassThreads, smem, s>>>(states, plan.geom, plan.gates, layer_gates, gate_stride,
                                                   collapse_in, collapse_stride, meas, meas_stride, partials,
                                                   fuse_hist);

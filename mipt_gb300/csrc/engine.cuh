@@ -27,15 +27,35 @@ struct Bond
     int q0, q1; // matrix index bit 0 <-> q0, bit 1 <-> q1
 };
 
+// One register round of a pass: every thread holds 2^rb amplitudes whose
+// register-index bit i is local tile bit reg[i]; thread-index bit i is local
+// bit tid[i] (the first five, one per residue mod 5, are the warp lanes).
+// slot[s] >= 0 applies pass gate slot[s] on register bits (2s, 2s+1).
+struct Round
+{
+    std::int8_t reg[6];
+    std::int8_t tid[10];
+    std::int16_t slot[3];
+};
+
+constexpr int kMaxRounds = 8;
+
 struct PassPlan
 {
     PassGeom geom;
     PassGates gates;
+    int rounds; // 0: tile too small for register rounds (shared-memory kernel)
+    int rb;     // register bits per thread
+    Round round[kMaxRounds];
 };
 
 // Splits one layer's bonds into tiled passes of at most kmax local qubits
-// with at least cmin contiguous low qubits per tile (for coalescing).
-std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin);
+// with at least cmin contiguous low qubits per tile (for coalescing), and
+// schedules each pass's bonds into register rounds of rb register bits.
+std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin, int rb);
+
+// Register bits per thread of the register-round pass kernel.
+template <typename Real> constexpr int register_bits() { return sizeof(Real) == 4 ? 6 : 5; }
 
 // Tile geometry used for a stand-alone histogram of the sites in `chunk`:
 // low contiguous qubits, then as many unmeasured qubits as fit, so that few
