@@ -1086,9 +1086,9 @@ int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seed
             {
                 b->any_meas[t] = 1;
                 b->max_chunks[t] = std::max(b->max_chunks[t], M.nchunks);
-                const PassPlan &last = b->plan[t & 1].back();
-                const int ml = local_measured_count(last.geom, M.chunk[0]);
-                if ((std::size_t{1} << (last.geom.n_nl + ml)) > kHistScratch) b->fusable[t] = 0;
+                const PassGeom &hg = fused_hist_geometry(b->plan[t & 1].back(), b->cfg.fp64 == 0);
+                const int ml = local_measured_count(hg, M.chunk[0]);
+                if ((std::size_t{1} << (hg.n_nl + ml)) > kHistScratch) b->fusable[t] = 0;
             }
         }
     }
@@ -1159,7 +1159,8 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                     ++L;
                 }
                 Mark m(b, K_MEASURE, s);
-                MG_CUDA(launch_measure(count, n, fused ? &plan.back().geom : nullptr, b->kmax, b->cmin, ci, meas + t, T,
+                MG_CUDA(launch_measure(count, n, fused ? &fused_hist_geometry(plan.back(), sizeof(Real) == 4) : nullptr,
+                                       b->kmax, b->cmin, ci, meas + t, T,
                                        b->part.as<double>(), b->bins.as<double>(),
                                        std::size_t{1} << b->cfg.chunk_bits, forced ? forced + t : nullptr, T,
                                        col + t, T, res + t, T, b->err.as<int>(), s));

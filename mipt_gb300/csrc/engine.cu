@@ -13,8 +13,12 @@
 #include "engine.cuh"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
+#include <cstdlib>
 #include <stdexcept>
+
+#include <cooperative_groups.h>
 
 namespace mg
 {
@@ -289,6 +293,9 @@ __device__ void value_histogram(const T *val, int k, const int *lm, int m_loc, d
     }
 }
 
+// Position of tile bit p once tile bit x is removed (CTA-local offset).
+__device__ __forceinline__ int opos_d(int p, int x) { return p > x ? p - 1 : p; }
+
 // XOR swizzle of one local tile bit: bits >= 5 also flip low bit (p mod 5),
 // so any five lanes whose tile bits have distinct residues mod 5 touch
 // distinct shared-memory banks. Linear over GF(2): swz(a ^ b) = swz(a) ^ swz(b).
@@ -468,6 +475,188 @@ __global__ void __launch_bounds__(256)
                 if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
             double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
             value_histogram(val, g.k, lm, m_loc, part, red);
+        }
+    }
+}
+
+
+// One tiled pass of a 2^14-amplitude tile split across the two CTAs of a
+// thread-block cluster (tile bit x = CTA rank): 256 threads x 32 amplitudes
+// per CTA, 64 KB of shared memory and at most 128 registers per thread, so two
+// CTAs fit on an SM and the load, gate and store phases of different CTAs
+// overlap. Transposes go through distributed shared memory.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256, 2)
+    k_pass_cluster(Cx<float> *__restrict__ states, PassPlan P, const Cx<float> *__restrict__ gates,
+                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
+                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
+                   int fuse_hist)
+{
+    constexpr int RB = 5, NA = 32, TB = 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Cx<float> *tile = reinterpret_cast<Cx<float> *>(smem_raw);
+    __shared__ Cx<float> U[kMaxPassGates][16];
+    __shared__ double red[8];
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank();
+    Cx<float> *peer = cluster.map_shared_rank(tile, static_cast<int>(rank ^ 1u));
+
+    const PassGeom &g = P.geom;
+    const int tid = threadIdx.x;
+    const int b = blockIdx.y;
+    const std::uint64_t tix = blockIdx.x >> 1;
+    Cx<float> *psi = states + (static_cast<std::size_t>(b) << g.n);
+    const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+    for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
+        U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
+    Collapse cl{0, 0, 1.0, 0.0};
+    const bool has_col = col_in != nullptr;
+    if (has_col) cl = col_in[b * col_stride];
+    const float scale = static_cast<float>(cl.scale);
+
+    Cx<float> amp[NA];
+    {
+        const ClusterRound &R = P.cround[0];
+        std::uint64_t gt = base | (static_cast<std::uint64_t>(rank) << g.pos[R.x]);
+        for (int i = 0; i < TB; ++i)
+            if ((tid >> i) & 1) gt |= 1ull << g.pos[R.tid[i]];
+        std::uint64_t gr[RB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[R.reg[i]];
+#pragma unroll
+        for (int r = 0; r < NA; ++r)
+        {
+            std::uint64_t gi = gt;
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+                if ((r >> i) & 1) gi |= gr[i];
+            Cx<float> v = psi[gi];
+            if (has_col) v = collapse_value(v, gi, cl, scale);
+            amp[r] = v;
+        }
+    }
+    __syncthreads();
+
+    for (int ri = 0; ri < P.cluster_rounds; ++ri)
+    {
+        const ClusterRound &R = P.cround[ri];
+        if (ri > 0)
+        {
+            const ClusterRound &A = P.cround[ri - 1];
+            const int xa = A.x;
+            // write: my elements have bit xa == rank, so they are all home here
+            std::uint32_t sa = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1) sa ^= swz1(opos_d(A.tid[i], xa));
+            std::uint32_t ra[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) ra[i] = swz1(opos_d(A.reg[i], xa));
+            if (ri > 1) cluster.sync(); // the peer has finished reading my buffer
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t p = sa;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) p ^= ra[i];
+                tile[p] = amp[r];
+            }
+            cluster.sync();
+            // read in the storage coordinates of round A; home CTA = bit xa
+            std::uint32_t sb = 0;
+            unsigned hb = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1)
+                {
+                    if (R.tid[i] == xa)
+                        hb ^= 1u;
+                    else
+                        sb ^= swz1(opos_d(R.tid[i], xa));
+                }
+            if (rank)
+            {
+                if (R.x == xa)
+                    hb ^= 1u;
+                else
+                    sb ^= swz1(opos_d(R.x, xa));
+            }
+            std::uint32_t rbv[RB];
+            unsigned rh[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+            {
+                rh[i] = R.reg[i] == xa ? 1u : 0u;
+                rbv[i] = R.reg[i] == xa ? 0u : swz1(opos_d(R.reg[i], xa));
+            }
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t p = sb;
+                unsigned h = hb;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1)
+                    {
+                        p ^= rbv[i];
+                        h ^= rh[i];
+                    }
+                amp[r] = (h == rank) ? tile[p] : peer[p];
+            }
+        }
+        if (R.slot[0] >= 0) apply_slot<0>(amp, U[R.slot[0]]);
+        if (R.slot[1] >= 0) apply_slot<1>(amp, U[R.slot[1]]);
+    }
+
+    const ClusterRound &Z = P.cround[P.cluster_rounds - 1];
+    {
+        std::uint64_t gt = base | (static_cast<std::uint64_t>(rank) << g.pos[Z.x]);
+        for (int i = 0; i < TB; ++i)
+            if ((tid >> i) & 1) gt |= 1ull << g.pos[Z.tid[i]];
+        std::uint64_t gr[RB];
+#pragma unroll
+        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[Z.reg[i]];
+#pragma unroll
+        for (int r = 0; r < NA; ++r)
+        {
+            std::uint64_t gi = gt;
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+                if ((r >> i) & 1) gi |= gr[i];
+            psi[gi] = amp[r];
+        }
+    }
+
+    // The peer may still read my buffer for the last transpose.
+    if (P.cluster_rounds > 1) cluster.sync();
+    if (fuse_hist)
+    {
+        const LayerMeas &M = meas[b * meas_stride];
+        if (M.nchunks > 0)
+        {
+            float *val = reinterpret_cast<float *>(smem_raw);
+            const int xz = Z.x;
+            std::uint32_t jt = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1) jt |= 1u << opos_d(Z.tid[i], xz);
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t j = jt;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) j |= 1u << opos_d(Z.reg[i], xz);
+                val[j] = norm2(amp[r]);
+            }
+            __syncthreads();
+            const std::uint64_t chunk = M.chunk[0];
+            const PassGeom &h = P.hgeom;
+            int lm[kMaxLocal + 1];
+            int m_loc = 0;
+            for (int i = 0; i < h.k; ++i)
+                if ((chunk >> h.pos[i]) & 1ull) lm[m_loc++] = i;
+            const std::uint64_t t2 = (tix << 1) | rank;
+            double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (t2 << m_loc);
+            value_histogram(val, h.k, lm, m_loc, part, red);
         }
     }
 }
@@ -696,6 +885,16 @@ __global__ void k_collapse(Cx<Real> *states, std::uint64_t dim, std::uint64_t to
     }
 }
 
+// MIPT_GB300_CLUSTER_PASS=0 selects the single-CTA register-round kernel.
+bool use_cluster_kernel()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_CLUSTER_PASS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 int grid_for(std::uint64_t total, int threads)
 {
     const std::uint64_t blocks = (total + threads - 1) / threads;
@@ -747,6 +946,11 @@ __host__ __device__ void histogram_geometry(int n, int kmax, int cmin, std::uint
     while (c < k && g.pos[c] == c) ++c;
     g.c = c;
     g.n_nl = n - k;
+}
+
+const PassGeom &fused_hist_geometry(const PassPlan &p, bool fp32)
+{
+    return (fp32 && p.cluster_rounds > 0 && use_cluster_kernel()) ? p.hgeom : p.geom;
 }
 
 int local_measured_count(const PassGeom &g, std::uint64_t chunk)
@@ -974,6 +1178,170 @@ bool plan_rounds(PassPlan &p, int rb)
 }
 } // namespace
 
+namespace
+{
+// Position of tile bit p once tile bit x is removed (the CTA-local offset).
+inline int opos(int p, int x) { return p > x ? p - 1 : p; }
+
+// Lanes 0..3 must flip the four low shared-memory bank bits (residues
+// {0,1,2,3} mod 5 of their offset positions) for conflict-free 8-byte access.
+bool lanes_ok(const int *l, int x)
+{
+    int seen = 0;
+    for (int i = 0; i < 4; ++i)
+    {
+        const int r = opos(l[i], x) % 5;
+        if (r > 3 || ((seen >> r) & 1)) return false;
+        seen |= 1 << r;
+    }
+    return true;
+}
+
+struct CSearch
+{
+    int k, nr;
+    std::vector<std::pair<int, int>> bonds;
+    std::vector<int> assign, load;
+    std::vector<ClusterRound> out;
+};
+
+// Chooses x and lanes for rounds in order; the read side of round i uses the
+// storage coordinates of round i-1's x.
+bool cluster_choose(CSearch &S, int r, int prev_x)
+{
+    if (r == S.nr) return true;
+    const int k = S.k;
+    std::uint32_t reg = 0;
+    std::vector<int> mine;
+    for (std::size_t b = 0; b < S.bonds.size(); ++b)
+        if (S.assign[b] == r)
+        {
+            reg |= (1u << S.bonds[b].first) | (1u << S.bonds[b].second);
+            mine.push_back(static_cast<int>(b));
+        }
+    const bool first = r == 0, last = r == S.nr - 1;
+    for (int x = k - 1; x >= 0; --x)
+    {
+        if ((reg >> x) & 1u) continue;
+        // candidate lane sets: {0,1,2,3} first, then any four free bits
+        std::vector<std::array<int, 4>> cands;
+        if (!(reg & 0xFu) && x > 3) cands.push_back({0, 1, 2, 3});
+        if (!first && !last)
+        {
+            std::vector<int> freeb;
+            for (int q = 0; q < k; ++q)
+                if (!((reg >> q) & 1u) && q != x) freeb.push_back(q);
+            const int F = static_cast<int>(freeb.size());
+            for (int a = 0; a < F; ++a)
+                for (int b2 = a + 1; b2 < F; ++b2)
+                    for (int c = b2 + 1; c < F; ++c)
+                        for (int d = c + 1; d < F; ++d)
+                            cands.push_back({freeb[a], freeb[b2], freeb[c], freeb[d]});
+        }
+        for (auto l : cands)
+        {
+            // order lanes so lane i has residue i in the read coordinates
+            const int xr = first ? x : prev_x; // read (or load) coordinates
+            std::array<int, 4> ord{};
+            bool ok = true;
+            int seen = 0;
+            for (int q : l)
+            {
+                const int rr = opos(q, xr) % 5;
+                if (rr > 3 || ((seen >> rr) & 1)) { ok = false; break; }
+                seen |= 1 << rr;
+                ord[rr] = q;
+            }
+            if (!ok) continue;
+            if (!first && !lanes_ok(ord.data(), prev_x)) continue;
+            if (!last && !lanes_ok(ord.data(), x)) continue;
+            if ((first || last) && !(ord[0] == 0 && ord[1] == 1 && ord[2] == 2 && ord[3] == 3)) continue;
+            ClusterRound R{};
+            int slot = 0;
+            R.slot[0] = R.slot[1] = -1;
+            std::uint32_t used = (1u << x) | (1u << ord[0]) | (1u << ord[1]) | (1u << ord[2]) | (1u << ord[3]);
+            for (int b : mine)
+            {
+                R.reg[2 * slot] = static_cast<std::int8_t>(S.bonds[b].first);
+                R.reg[2 * slot + 1] = static_cast<std::int8_t>(S.bonds[b].second);
+                used |= (1u << S.bonds[b].first) | (1u << S.bonds[b].second);
+                R.slot[slot] = static_cast<std::int16_t>(b);
+                ++slot;
+            }
+            for (int i = 2 * slot; i < 5; ++i)
+                for (int q = 0; q < k; ++q)
+                    if (!((used >> q) & 1u))
+                    {
+                        R.reg[i] = static_cast<std::int8_t>(q);
+                        used |= 1u << q;
+                        break;
+                    }
+            int t = 0;
+            for (int i = 0; i < 4; ++i) R.tid[t++] = static_cast<std::int8_t>(ord[i]);
+            for (int q = 0; q < k; ++q)
+                if (!((used >> q) & 1u)) R.tid[t++] = static_cast<std::int8_t>(q);
+            if (t != 8) continue;
+            R.x = static_cast<std::int8_t>(x);
+            S.out[r] = R;
+            if (cluster_choose(S, r + 1, x)) return true;
+        }
+    }
+    return false;
+}
+
+bool cluster_dfs(CSearch &S, std::size_t b)
+{
+    if (b == S.bonds.size()) return cluster_choose(S, 0, -1);
+    for (int r = 0; r < S.nr; ++r)
+    {
+        if (S.load[r] >= 2) continue;
+        S.assign[b] = r;
+        ++S.load[r];
+        if (cluster_dfs(S, b + 1)) return true;
+        --S.load[r];
+    }
+    return false;
+}
+
+bool plan_cluster_rounds(PassPlan &p)
+{
+    p.cluster_rounds = 0;
+    if (p.geom.k != 14) return false;
+    CSearch S;
+    S.k = 14;
+    for (int i = 0; i < p.gates.count; ++i) S.bonds.push_back({p.gates.la[i], p.gates.lb[i]});
+    const int nb = static_cast<int>(S.bonds.size());
+    for (int nr = std::max(1, (nb + 1) / 2); nr <= kMaxRounds; ++nr)
+    {
+        S.nr = nr;
+        S.assign.assign(nb, -1);
+        S.load.assign(nr, 0);
+        S.out.assign(nr, ClusterRound{});
+        if (!cluster_dfs(S, 0)) continue;
+        for (int r = 0; r < nr; ++r) p.cround[r] = S.out[r];
+        p.cluster_rounds = nr;
+        // Histogram geometry of a half tile: the tile bits other than the last
+        // round's x are local; tile-index bit 0 is the CTA rank (qubit of x).
+        const int xz = p.cround[nr - 1].x;
+        PassGeom h{};
+        h.n = p.geom.n;
+        h.k = 13;
+        int a = 0;
+        for (int q = 0; q < 14; ++q)
+            if (q != xz) h.pos[a++] = p.geom.pos[q];
+        h.n_nl = p.geom.n_nl + 1;
+        h.nl[0] = p.geom.pos[xz];
+        for (int i = 0; i < p.geom.n_nl; ++i) h.nl[i + 1] = p.geom.nl[i];
+        int c = 0;
+        while (c < 13 && h.pos[c] == c) ++c;
+        h.c = c;
+        p.hgeom = h;
+        return true;
+    }
+    return false;
+}
+} // namespace
+
 std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin, int rb)
 {
     if (n > 32) throw std::invalid_argument("engine supports at most 32 qubits");
@@ -986,6 +1354,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
         p.geom = make_geom(n, (1ull << kmax) - 1ull);
         p.gates.count = 0;
         plan_rounds(p, rb);
+        if (rb == 6) plan_cluster_rounds(p);
         return {p};
     }
     // Try first tiles made of a low contiguous block, optionally with the top
@@ -1005,7 +1374,11 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
             if (best.empty() || plan.size() < best.size()) best = plan;
         }
     }
-    for (auto &p : best) plan_rounds(p, rb);
+    for (auto &p : best)
+    {
+        plan_rounds(p, rb);
+        if (rb == 6) plan_cluster_rounds(p);
+    }
     return best;
 }
 
@@ -1024,6 +1397,20 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
                         cudaStream_t s)
 {
     dim3 grid(1u << plan.geom.n_nl, batch);
+    if constexpr (sizeof(Real) == 4)
+    {
+        if (plan.cluster_rounds > 0 && use_cluster_kernel())
+        {
+            const std::size_t smem = sizeof(Cx<float>) << 13;
+            cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_pass_cluster),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+            if (e != cudaSuccess) return e;
+            dim3 cgrid(2u << plan.geom.n_nl, batch);
+            k_pass_cluster<<<cgrid, 256, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
+                                                     collapse_stride, meas, meas_stride, partials, fuse_hist);
+            return cudaGetLastError();
+        }
+    }
     if (plan.rounds > 0)
     {
         constexpr int RB = register_bits<Real>();

@@ -40,6 +40,19 @@ struct Round
 
 constexpr int kMaxRounds = 8;
 
+// Register round of the two-CTA cluster kernel: the 2^14-amplitude tile is
+// split between the two CTAs of a cluster by tile bit x (CTA rank = bit x);
+// each thread holds 32 amplitudes (register bits reg[0..5)), thread-index bit
+// i is tile bit tid[i]. slot[s] >= 0 applies pass gate slot[s] on register
+// bits (2s, 2s+1).
+struct ClusterRound
+{
+    std::int8_t reg[5];
+    std::int8_t tid[8];
+    std::int8_t x;
+    std::int16_t slot[2];
+};
+
 struct PassPlan
 {
     PassGeom geom;
@@ -47,12 +60,19 @@ struct PassPlan
     int rounds; // 0: tile too small for register rounds (shared-memory kernel)
     int rb;     // register bits per thread
     Round round[kMaxRounds];
+    int cluster_rounds; // > 0: FP32 two-CTA cluster schedule available
+    ClusterRound cround[kMaxRounds];
+    PassGeom hgeom; // histogram geometry of one CTA's half tile (cluster kernel)
 };
 
 // Splits one layer's bonds into tiled passes of at most kmax local qubits
 // with at least cmin contiguous low qubits per tile (for coalescing), and
 // schedules each pass's bonds into register rounds of rb register bits.
 std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax, int cmin, int rb);
+
+// Geometry of the per-tile histogram partials a pass writes when it fuses
+// the layer's Born histogram (a half tile for the cluster kernel).
+const PassGeom &fused_hist_geometry(const PassPlan &p, bool fp32);
 
 // Register bits per thread of the register-round pass kernel.
 template <typename Real> constexpr int register_bits() { return sizeof(Real) == 4 ? 6 : 5; }
