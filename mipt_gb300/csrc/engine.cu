@@ -330,6 +330,65 @@ __device__ __forceinline__ void apply_slot(Cx<Real> (&a)[NA], const Cx<Real> *__
     }
 }
 
+
+// FP32 variant of apply_slot on Blackwell's packed FP32x2 FMA: for
+// acc += u * in, acc = fma2({u.re, u.re}, {in.re, in.im}, acc) then
+// acc = fma2({-u.im, u.im}, {in.im, in.re}, acc) -- two packed FMAs per
+// complex multiply-add instead of four scalar ones.
+template <int S, int NA>
+__device__ __forceinline__ void apply_slot_f2(Cx<float> (&a)[NA], const Cx<float> *__restrict__ Us)
+{
+    constexpr int lo = 2 * S;
+    float2 ur[16], ui[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e)
+    {
+        const Cx<float> u = Us[e];
+        ur[e] = make_float2(u.re, u.re);
+        ui[e] = make_float2(-u.im, u.im);
+    }
+#pragma unroll
+    for (int g = 0; g < NA / 4; ++g)
+    {
+        const int base = ((g >> lo) << (lo + 2)) | (g & ((1 << lo) - 1));
+        float2 in[4], sw[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+        {
+            const Cx<float> v = a[base | (c << lo)];
+            in[c] = make_float2(v.re, v.im);
+            sw[c] = make_float2(v.im, v.re);
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            float2 acc = __fmul2_rn(ur[4 * r], in[0]);
+            acc = __ffma2_rn(ui[4 * r], sw[0], acc);
+#pragma unroll
+            for (int c = 1; c < 4; ++c)
+            {
+                acc = __ffma2_rn(ur[4 * r + c], in[c], acc);
+                acc = __ffma2_rn(ui[4 * r + c], sw[c], acc);
+            }
+            a[base | (r << lo)] = Cx<float>{acc.x, acc.y};
+        }
+    }
+}
+
+template <int S, typename Real, int NA>
+__device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real> *__restrict__ Us, bool packed)
+{
+    if constexpr (sizeof(Real) == 4)
+    {
+        if (packed)
+        {
+            apply_slot_f2<S>(a, Us);
+            return;
+        }
+    }
+    apply_slot<S>(a, Us);
+}
+
 // One tiled pass with register rounds: global -> registers (lanes on the
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
@@ -338,7 +397,7 @@ __global__ void __launch_bounds__(256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
-                  int fuse_hist)
+                  int fuse_hist, int packed)
 {
     constexpr int NA = 1 << RB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -424,9 +483,9 @@ __global__ void __launch_bounds__(256)
                 amp[r] = tile[p];
             }
         }
-        if (R.slot[0] >= 0) apply_slot<0>(amp, U[R.slot[0]]);
-        if (RB >= 4 && R.slot[1] >= 0) apply_slot<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]]);
-        if (RB >= 6 && R.slot[2] >= 0) apply_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]]);
+        if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+        if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
+        if (RB >= 6 && R.slot[2] >= 0) apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
     }
 
     const Round &Z = P.round[P.rounds - 1];
@@ -885,11 +944,22 @@ __global__ void k_collapse(Cx<Real> *states, std::uint64_t dim, std::uint64_t to
     }
 }
 
-// MIPT_GB300_CLUSTER_PASS=0 selects the single-CTA register-round kernel.
+// MIPT_GB300_CLUSTER_PASS=1 selects the two-CTA cluster kernel for FP32
+// passes (default: the single-CTA register-round kernel).
 bool use_cluster_kernel()
 {
     static const bool on = [] {
         const char *v = std::getenv("MIPT_GB300_CLUSTER_PASS");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+// MIPT_GB300_PACKED_FMA=0 disables the packed FP32x2 gate arithmetic.
+bool use_packed_fma()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_PACKED_FMA");
         return !(v && v[0] == '0');
     }();
     return on;
@@ -1420,7 +1490,7 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
         if (e != cudaSuccess) return e;
         k_pass_rounds<Real, RB><<<grid, 1u << (plan.geom.k - RB), smem, s>>>(
             states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-            fuse_hist);
+            fuse_hist, use_packed_fma() ? 1 : 0);
         return cudaGetLastError();
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
