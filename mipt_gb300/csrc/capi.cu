@@ -159,7 +159,7 @@ struct EntReq
 
 struct Workspace
 {
-    DevBuf jobs, rho, scratch, vals, idx, eig, work, info;
+    DevBuf jobs, rho, scratch, vals, idx, eig, work, info, err;
     cusolverDnHandle_t solver = nullptr;
     ~Workspace()
     {
@@ -210,6 +210,38 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
         const int d = 1 << k;
         const std::size_t rho_bytes = sizeof(double) * 2 * static_cast<std::size_t>(d) * d;
         const int tiles = gram_tiles(k);
+        if constexpr (sizeof(Real) == 4)
+        {
+            // Renyi-2 of FP32 states on the tensor cores (3xTF32 tcgen05 Gram).
+            if (!vn && gram_tc_supported(n, k))
+            {
+                const int nb = static_cast<int>(list.size());
+                std::vector<GramJob> jobs(nb);
+                std::vector<int> idx(nb);
+                for (int i = 0; i < nb; ++i)
+                {
+                    jobs[i] = make_gram_job(list[i]->traj, n, list[i]->kept.data(), k, list[i]->fermion != 0);
+                    idx[i] = list[i]->out;
+                }
+                MG_CUDA(ws.jobs.ensure(sizeof(GramJob) * nb));
+                MG_CUDA(ws.idx.ensure(sizeof(int) * nb));
+                MG_CUDA(ws.vals.ensure(sizeof(double) * nb));
+                MG_CUDA(ws.scratch.ensure(gram_tc_scratch_bytes(k, nb)));
+                if (!ws.err.p)
+                {
+                    MG_CUDA(ws.err.ensure(sizeof(int)));
+                    MG_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), s));
+                }
+                MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
+                MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+                MG_CUDA(gram_purity_tc(states, n, ws.jobs.as<GramJob>(), nb, k, col, col_stride, ws.vals.as<double>(),
+                                       ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s));
+                launches += 2;
+                k_scatter<<<(nb + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nb, d_out, 1);
+                ++launches;
+                continue;
+            }
+        }
         // Purity straight from tiles when there are enough tiles to fill the GPU.
         const bool tile_purity = !vn && tiles * static_cast<long long>(list.size()) >= 2 * 152;
         std::size_t per_launch = list.size();
@@ -331,6 +363,12 @@ int compat_entropy(const void *state, int n, const int *kept, int k, int fermion
         return fail(MIPT_GB300_E_INVALID, e.what());
     }
     MG_CUDA(cudaMemcpy(out, c.out.p, sizeof(double), cudaMemcpyDeviceToHost));
+    if (c.ws.err.p)
+    {
+        int err = 0;
+        MG_CUDA(cudaMemcpy(&err, c.ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return fail(MIPT_GB300_E_INTERNAL, "tensor-core Gram pipeline wait timed out");
+    }
     return 0;
 }
 
@@ -1255,6 +1293,11 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
     int err = 0;
     MG_CUDA(cudaMemcpy(&err, b->err.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return fail(MIPT_GB300_E_NUMERIC, "a measurement found a zero-norm state or no outcome with weight");
+    if (b->ws.err.p)
+    {
+        MG_CUDA(cudaMemcpy(&err, b->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return fail(MIPT_GB300_E_INTERNAL, "tensor-core Gram pipeline wait timed out");
+    }
     const int count = b->count, T = b->T, n = b->cfg.n_qubits;
     if (measured) std::copy(b->measured.begin(), b->measured.end(), measured);
     if (outcomes || surprisal)

@@ -544,13 +544,14 @@ __global__ void __launch_bounds__(256)
 // per CTA, 64 KB of shared memory and at most 128 registers per thread, so two
 // CTAs fit on an SM and the load, gate and store phases of different CTAs
 // overlap. Transposes go through distributed shared memory.
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256, 2)
+template <int RB>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(1 << (13 - RB), 2)
     k_pass_cluster(Cx<float> *__restrict__ states, PassPlan P, const Cx<float> *__restrict__ gates,
                    std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                    const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
                    int fuse_hist)
 {
-    constexpr int RB = 5, NA = 32, TB = 8;
+    constexpr int NA = 1 << RB, TB = 13 - RB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<float> *tile = reinterpret_cast<Cx<float> *>(smem_raw);
     __shared__ Cx<float> U[kMaxPassGates][16];
@@ -573,24 +574,31 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256, 2)
     if (has_col) cl = col_in[b * col_stride];
     const float scale = static_cast<float>(cl.scale);
 
+    // n <= 32: every amplitude index fits in 32 bits.
+    const std::uint32_t cmask = static_cast<std::uint32_t>(cl.mask), cval = static_cast<std::uint32_t>(cl.value);
     Cx<float> amp[NA];
     {
         const ClusterRound &R = P.cround[0];
-        std::uint64_t gt = base | (static_cast<std::uint64_t>(rank) << g.pos[R.x]);
+        std::uint32_t gt = static_cast<std::uint32_t>(base) | (rank << g.pos[R.x]);
         for (int i = 0; i < TB; ++i)
-            if ((tid >> i) & 1) gt |= 1ull << g.pos[R.tid[i]];
-        std::uint64_t gr[RB];
+            if ((tid >> i) & 1) gt |= 1u << g.pos[R.tid[i]];
+        std::uint32_t gr[RB];
 #pragma unroll
-        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[R.reg[i]];
+        for (int i = 0; i < RB; ++i) gr[i] = 1u << g.pos[R.reg[i]];
 #pragma unroll
         for (int r = 0; r < NA; ++r)
         {
-            std::uint64_t gi = gt;
+            std::uint32_t gi = gt;
 #pragma unroll
             for (int i = 0; i < RB; ++i)
                 if ((r >> i) & 1) gi |= gr[i];
             Cx<float> v = psi[gi];
-            if (has_col) v = collapse_value(v, gi, cl, scale);
+            if (has_col)
+            {
+                const float f = ((gi & cmask) == cval) ? scale : 0.f;
+                v.re *= f;
+                v.im *= f;
+            }
             amp[r] = v;
         }
     }
@@ -664,20 +672,21 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(256, 2)
         }
         if (R.slot[0] >= 0) apply_slot<0>(amp, U[R.slot[0]]);
         if (R.slot[1] >= 0) apply_slot<1>(amp, U[R.slot[1]]);
+        if (RB >= 6 && R.slot[2] >= 0) apply_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]]);
     }
 
     const ClusterRound &Z = P.cround[P.cluster_rounds - 1];
     {
-        std::uint64_t gt = base | (static_cast<std::uint64_t>(rank) << g.pos[Z.x]);
+        std::uint32_t gt = static_cast<std::uint32_t>(base) | (rank << g.pos[Z.x]);
         for (int i = 0; i < TB; ++i)
-            if ((tid >> i) & 1) gt |= 1ull << g.pos[Z.tid[i]];
-        std::uint64_t gr[RB];
+            if ((tid >> i) & 1) gt |= 1u << g.pos[Z.tid[i]];
+        std::uint32_t gr[RB];
 #pragma unroll
-        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[Z.reg[i]];
+        for (int i = 0; i < RB; ++i) gr[i] = 1u << g.pos[Z.reg[i]];
 #pragma unroll
         for (int r = 0; r < NA; ++r)
         {
-            std::uint64_t gi = gt;
+            std::uint32_t gi = gt;
 #pragma unroll
             for (int i = 0; i < RB; ++i)
                 if ((r >> i) & 1) gi |= gr[i];
@@ -944,13 +953,13 @@ __global__ void k_collapse(Cx<Real> *states, std::uint64_t dim, std::uint64_t to
     }
 }
 
-// MIPT_GB300_CLUSTER_PASS=1 selects the two-CTA cluster kernel for FP32
-// passes (default: the single-CTA register-round kernel).
+// MIPT_GB300_CLUSTER_PASS=0 selects the single-CTA register-round kernel for
+// FP32 passes instead of the two-CTA cluster kernel.
 bool use_cluster_kernel()
 {
     static const bool on = [] {
         const char *v = std::getenv("MIPT_GB300_CLUSTER_PASS");
-        return v && v[0] == '1';
+        return !(v && v[0] == '0');
     }();
     return on;
 }
@@ -1250,6 +1259,17 @@ bool plan_rounds(PassPlan &p, int rb)
 
 namespace
 {
+// MIPT_GB300_CLUSTER_RB=5 selects 32 amplitudes per thread (256 threads per
+// CTA) for the cluster kernel instead of 64 (128 threads).
+int cluster_register_bits()
+{
+    static const int rb = [] {
+        const char *v = std::getenv("MIPT_GB300_CLUSTER_RB");
+        return (v && v[0] == '5') ? 5 : 6;
+    }();
+    return rb;
+}
+
 // Position of tile bit p once tile bit x is removed (the CTA-local offset).
 inline int opos(int p, int x) { return p > x ? p - 1 : p; }
 
@@ -1269,7 +1289,7 @@ bool lanes_ok(const int *l, int x)
 
 struct CSearch
 {
-    int k, nr;
+    int k, nr, rb;
     std::vector<std::pair<int, int>> bonds;
     std::vector<int> assign, load;
     std::vector<ClusterRound> out;
@@ -1328,7 +1348,7 @@ bool cluster_choose(CSearch &S, int r, int prev_x)
             if ((first || last) && !(ord[0] == 0 && ord[1] == 1 && ord[2] == 2 && ord[3] == 3)) continue;
             ClusterRound R{};
             int slot = 0;
-            R.slot[0] = R.slot[1] = -1;
+            R.slot[0] = R.slot[1] = R.slot[2] = -1;
             std::uint32_t used = (1u << x) | (1u << ord[0]) | (1u << ord[1]) | (1u << ord[2]) | (1u << ord[3]);
             for (int b : mine)
             {
@@ -1338,7 +1358,7 @@ bool cluster_choose(CSearch &S, int r, int prev_x)
                 R.slot[slot] = static_cast<std::int16_t>(b);
                 ++slot;
             }
-            for (int i = 2 * slot; i < 5; ++i)
+            for (int i = 2 * slot; i < S.rb; ++i)
                 for (int q = 0; q < k; ++q)
                     if (!((used >> q) & 1u))
                     {
@@ -1350,7 +1370,7 @@ bool cluster_choose(CSearch &S, int r, int prev_x)
             for (int i = 0; i < 4; ++i) R.tid[t++] = static_cast<std::int8_t>(ord[i]);
             for (int q = 0; q < k; ++q)
                 if (!((used >> q) & 1u)) R.tid[t++] = static_cast<std::int8_t>(q);
-            if (t != 8) continue;
+            if (t != k - 1 - S.rb) continue;
             R.x = static_cast<std::int8_t>(x);
             S.out[r] = R;
             if (cluster_choose(S, r + 1, x)) return true;
@@ -1364,7 +1384,7 @@ bool cluster_dfs(CSearch &S, std::size_t b)
     if (b == S.bonds.size()) return cluster_choose(S, 0, -1);
     for (int r = 0; r < S.nr; ++r)
     {
-        if (S.load[r] >= 2) continue;
+        if (S.load[r] >= S.rb / 2) continue;
         S.assign[b] = r;
         ++S.load[r];
         if (cluster_dfs(S, b + 1)) return true;
@@ -1373,15 +1393,18 @@ bool cluster_dfs(CSearch &S, std::size_t b)
     return false;
 }
 
-bool plan_cluster_rounds(PassPlan &p)
+bool plan_cluster_rounds(PassPlan &p, int rb)
 {
     p.cluster_rounds = 0;
+    p.cluster_rb = rb;
     if (p.geom.k != 14) return false;
     CSearch S;
     S.k = 14;
+    S.rb = rb;
     for (int i = 0; i < p.gates.count; ++i) S.bonds.push_back({p.gates.la[i], p.gates.lb[i]});
     const int nb = static_cast<int>(S.bonds.size());
-    for (int nr = std::max(1, (nb + 1) / 2); nr <= kMaxRounds; ++nr)
+    const int slots = rb / 2;
+    for (int nr = std::max(1, (nb + slots - 1) / slots); nr <= kMaxRounds; ++nr)
     {
         S.nr = nr;
         S.assign.assign(nb, -1);
@@ -1424,7 +1447,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
         p.geom = make_geom(n, (1ull << kmax) - 1ull);
         p.gates.count = 0;
         plan_rounds(p, rb);
-        if (rb == 6) plan_cluster_rounds(p);
+        if (rb == 6) plan_cluster_rounds(p, cluster_register_bits());
         return {p};
     }
     // Try first tiles made of a low contiguous block, optionally with the top
@@ -1447,7 +1470,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
     for (auto &p : best)
     {
         plan_rounds(p, rb);
-        if (rb == 6) plan_cluster_rounds(p);
+        if (rb == 6) plan_cluster_rounds(p, cluster_register_bits());
     }
     return best;
 }
@@ -1472,12 +1495,24 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
         if (plan.cluster_rounds > 0 && use_cluster_kernel())
         {
             const std::size_t smem = sizeof(Cx<float>) << 13;
-            cudaError_t e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_pass_cluster),
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-            if (e != cudaSuccess) return e;
             dim3 cgrid(2u << plan.geom.n_nl, batch);
-            k_pass_cluster<<<cgrid, 256, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
-                                                     collapse_stride, meas, meas_stride, partials, fuse_hist);
+            cudaError_t e;
+            if (plan.cluster_rb == 6)
+            {
+                e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_pass_cluster<6>),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                if (e != cudaSuccess) return e;
+                k_pass_cluster<6><<<cgrid, 128, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
+                                                           collapse_stride, meas, meas_stride, partials, fuse_hist);
+            }
+            else
+            {
+                e = cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_pass_cluster<5>),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+                if (e != cudaSuccess) return e;
+                k_pass_cluster<5><<<cgrid, 256, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
+                                                           collapse_stride, meas, meas_stride, partials, fuse_hist);
+            }
             return cudaGetLastError();
         }
     }

@@ -47,10 +47,10 @@ constexpr int kMaxRounds = 8;
 // bits (2s, 2s+1).
 struct ClusterRound
 {
-    std::int8_t reg[5];
+    std::int8_t reg[6];
     std::int8_t tid[8];
     std::int8_t x;
-    std::int16_t slot[2];
+    std::int16_t slot[3];
 };
 
 struct PassPlan
@@ -61,6 +61,7 @@ struct PassPlan
     int rb;     // register bits per thread
     Round round[kMaxRounds];
     int cluster_rounds; // > 0: FP32 two-CTA cluster schedule available
+    int cluster_rb;     // register bits per thread of that schedule
     ClusterRound cround[kMaxRounds];
     PassGeom hgeom; // histogram geometry of one CTA's half tile (cluster kernel)
 };

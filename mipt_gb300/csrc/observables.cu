@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <stdexcept>
 
 namespace mg
@@ -757,6 +758,371 @@ cudaError_t rho3_sweep(const Cx<Real> *states, int n, int batch, const int *d_su
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_rho3_finalize<<<count * batch, 64, 0, s>>>(static_cast<const double *>(scratch), chunks, count * batch, out);
+    return cudaGetLastError();
+}
+
+
+// ===================================================================
+// Tensor-core Gram (tcgen05, FP32 states): purity Tr(rho^2) of
+// rho = M M^H without materialising rho.
+//
+// One real GEMM per 128x128 tile of rho: D[128 x 256] = X_r [128 x K] *
+// [X_c ; Y_c]^T, where row i of X holds the Schmidt row as interleaved
+// (re, im) reals and Y holds (-im, re): D[:, :128] = Re rho, D[:, 128:] = Im rho.
+// Operands are split into TF32 hi/lo parts and D accumulates
+// hi*hi + hi*lo + lo*hi in FP32 tensor memory (3xTF32). Producer warps gather
+// the Schmidt rows straight from the state (pending collapse and fermionic
+// signs applied), split them and write the 128B-swizzled K-major layout the
+// MMA descriptors describe; one thread issues tcgen05.mma; the epilogue
+// reads D with tcgen05.ld and reduces the weighted squares.
+namespace
+{
+constexpr int TCM = 128;                 // rows of a rho tile
+constexpr int TCN = 256;                 // X rows + Y rows of the column block
+constexpr int TC_PWARPS = 8;             // producer warps (warps 0-3 also run the epilogue)
+constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
+constexpr int TC_A_BYTES = TCM * 128;    // one 128-row operand half: 16 KB
+constexpr int TC_B_BYTES = TCN * 128;    // 32 KB
+constexpr int TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
+constexpr int TC_STAGES = 2;
+constexpr std::size_t TC_SMEM = static_cast<std::size_t>(TC_STAGES) * TC_STAGE + 1024;
+constexpr long long TC_SPIN = 1ll << 24;
+
+__device__ __forceinline__ std::uint32_t sm_addr(const void *p)
+{
+    return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(std::uint64_t *bar, std::uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(sm_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(std::uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(sm_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(std::uint64_t *bar, std::uint32_t parity)
+{
+    std::uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(sm_addr(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: gives up after TC_SPIN polls, raises the error flag and the
+// block-wide abort flag (so every later wait returns at once).
+__device__ __forceinline__ bool mbar_wait(std::uint64_t *bar, std::uint32_t parity, volatile int *abort_flag,
+                                          int *err)
+{
+    for (long long i = 0; i < TC_SPIN; ++i)
+    {
+        if (*abort_flag) return false;
+        if (mbar_try(bar, parity)) return true;
+    }
+    *abort_flag = 1;
+    atomicOr(err, 4);
+    return false;
+}
+
+__device__ __forceinline__ float tf32_round(float x)
+{
+    std::uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ std::uint64_t sw128_desc(std::uint32_t saddr)
+{
+    return static_cast<std::uint64_t>((saddr >> 4) & 0x3FFFu) | (1ull << 16) | (64ull << 32) | (1ull << 46) |
+           (2ull << 61);
+}
+
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128.
+constexpr std::uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCN >> 3) << 17) | ((TCM >> 4) << 24);
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_gram_tc(const Cx<float> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
+              const Collapse *__restrict__ col, std::size_t col_stride, double *__restrict__ pur_out,
+              int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char tc_raw[];
+    __shared__ GramJob J;
+    __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], done_bar;
+    __shared__ std::uint32_t tmem_base;
+    __shared__ std::uint64_t roffA[TCM], roffB[TCM], crossA[TCM], crossB[TCM], elo[16];
+    __shared__ double red[4];
+    __shared__ volatile int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // 1024-byte aligned stage buffers (swizzle atoms).
+    const std::uint32_t raw_s = sm_addr(tc_raw);
+    unsigned char *smem = tc_raw + ((1024u - (raw_s & 1023u)) & 1023u);
+    const int job = blockIdx.z;
+    int tr, tc;
+    tile_coords(blockIdx.x, tr, tc);
+
+    if (tid == 0)
+    {
+        J = jobs[job];
+        for (int s = 0; s < TC_STAGES; ++s)
+        {
+            mbar_init(&full_bar[s], TC_PWARPS);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&done_bar, 1);
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_PWARPS)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(sm_addr(&tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    const int k = J.k;
+    const int d = 1 << k;
+    const int nenv = n - k;
+    const int r0 = tr * TCM, c0 = tc * TCM;
+    if (tid < TCM)
+    {
+        std::uint64_t oa = 0, ob = 0, xa = 0, xb = 0;
+        const int r = r0 + tid, c = c0 + tid;
+        for (int i = 0; i < k; ++i)
+        {
+            if ((r >> i) & 1)
+            {
+                oa |= 1ull << J.kept[i];
+                xa ^= J.below[i];
+            }
+            if ((c >> i) & 1)
+            {
+                ob |= 1ull << J.kept[i];
+                xb ^= J.below[i];
+            }
+        }
+        roffA[tid] = oa;
+        roffB[tid] = ob;
+        crossA[tid] = J.fermion ? xa : 0ull;
+        crossB[tid] = J.fermion ? xb : 0ull;
+    }
+    else if (tid < TCM + 16)
+    {
+        const int i = tid - TCM;
+        std::uint64_t o = 0;
+        for (int b = 0; b < 4; ++b)
+            if ((i >> b) & 1) o |= 1ull << J.env[b];
+        elo[i] = o;
+    }
+    Collapse cl{0, 0, 1.0, 0.0};
+    const bool has_col = col != nullptr;
+    if (has_col) cl = col[J.traj * col_stride];
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    const std::uint32_t tmem = tmem_base;
+    const Cx<float> *psi = states + (static_cast<std::size_t>(J.traj) << n);
+    const int nchunks = 1 << (nenv - 4); // 16 complex environment columns per stage
+
+    if (warp < TC_PWARPS)
+    {
+        const int ptid = tid;
+        for (int chunk = 0; chunk < nchunks; ++chunk)
+        {
+            const int st = chunk & 1;
+            if (chunk >= TC_STAGES && !mbar_wait(&empty_bar[st], ((chunk >> 1) - 1) & 1, &abort_flag, err)) break;
+            unsigned char *stage = smem + st * TC_STAGE;
+            unsigned char *Ahi = stage, *Alo = stage + TC_A_BYTES;
+            unsigned char *Bhi = stage + 2 * TC_A_BYTES, *Blo = Bhi + TC_B_BYTES;
+            const std::uint64_t e0 = static_cast<std::uint64_t>(chunk) << 4;
+            std::uint64_t ehi = 0;
+            for (int b = 4; b < nenv; ++b)
+                if ((e0 >> b) & 1ull) ehi |= 1ull << J.env[b];
+            for (int item = ptid; item < 2 * TCM * 8; item += TC_PWARPS * 32)
+            {
+                const int which = item >= TCM * 8;
+                const int rem = item & (TCM * 8 - 1);
+                int row, q;
+                if (J.rows_fastest)
+                {
+                    row = rem & (TCM - 1);
+                    q = rem >> 7;
+                }
+                else
+                {
+                    q = rem & 7;
+                    row = rem >> 3;
+                }
+                const std::uint64_t ro = which ? roffB[row] : roffA[row];
+                const std::uint64_t cx = which ? crossB[row] : crossA[row];
+                const std::uint64_t ea = e0 + 2 * q, eb = ea + 1;
+                const Cx<float> v0 =
+                    gather(psi, ehi | elo[2 * q] | ro, cl, has_col, (__popcll(ea & cx) & 1) != 0);
+                const Cx<float> v1 =
+                    gather(psi, ehi | elo[2 * q + 1] | ro, cl, has_col, (__popcll(eb & cx) & 1) != 0);
+                const float4 X = make_float4(v0.re, v0.im, v1.re, v1.im);
+                auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 v) {
+                    const int off = (rr >> 3) * 1024 + (rr & 7) * 128 + ((q ^ (rr & 7)) << 4);
+                    float4 h, l;
+                    h.x = tf32_round(v.x);
+                    h.y = tf32_round(v.y);
+                    h.z = tf32_round(v.z);
+                    h.w = tf32_round(v.w);
+                    l.x = tf32_round(v.x - h.x);
+                    l.y = tf32_round(v.y - h.y);
+                    l.z = tf32_round(v.z - h.z);
+                    l.w = tf32_round(v.w - h.w);
+                    *reinterpret_cast<float4 *>(hi_buf + off) = h;
+                    *reinterpret_cast<float4 *>(lo_buf + off) = l;
+                };
+                if (!which)
+                {
+                    put(Ahi, Alo, row, X);
+                }
+                else
+                {
+                    put(Bhi, Blo, row, X);
+                    put(Bhi, Blo, TCM + row, make_float4(-v0.im, v0.re, -v1.im, v1.re));
+                }
+            }
+            // Make the generic-proxy stores visible to the tensor core.
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full_bar[st]);
+        }
+    }
+    else if (lane == 0)
+    {
+        for (int chunk = 0; chunk < nchunks; ++chunk)
+        {
+            const int st = chunk & 1;
+            if (!mbar_wait(&full_bar[st], (chunk >> 1) & 1, &abort_flag, err)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const std::uint32_t base = sm_addr(smem + st * TC_STAGE);
+            const std::uint32_t Ahi = base, Alo = base + TC_A_BYTES;
+            const std::uint32_t Bhi = base + 2 * TC_A_BYTES, Blo = Bhi + TC_B_BYTES;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks)
+            {
+                const std::uint32_t koff = ks * 32;
+                const std::uint64_t ah = sw128_desc(Ahi + koff), al = sw128_desc(Alo + koff);
+                const std::uint64_t bh = sw128_desc(Bhi + koff), bl = sw128_desc(Blo + koff);
+                const std::uint32_t acc0 = (chunk | ks) ? 1u : 0u;
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             "l"(ah), "l"(bh), "r"(kTcIdesc), "r"(acc0)
+                             : "memory");
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             "l"(ah), "l"(bl), "r"(kTcIdesc), "r"(1u)
+                             : "memory");
+                asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             "l"(al), "l"(bh), "r"(kTcIdesc), "r"(1u)
+                             : "memory");
+            }
+            // Stage st may be overwritten once these MMAs have read it.
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             sm_addr(&empty_bar[st]))
+                         : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         sm_addr(&done_bar))
+                     : "memory");
+    }
+
+    if (warp < 4)
+    {
+        const bool ok = mbar_wait(&done_bar, 0, &abort_flag, err);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int row = warp * 32 + lane;
+        const int r = r0 + row;
+        double acc = 0.0;
+        if (ok)
+        {
+            for (int cb = 0; cb < 8; ++cb)
+            {
+                std::uint32_t v[32];
+                const std::uint32_t taddr = tmem + (static_cast<std::uint32_t>(warp * 32) << 16) + cb * 32;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                const int cbase = c0 + (cb & 3) * 32;
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                {
+                    const int c = cbase + i;
+                    const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
+                    const double x = static_cast<double>(__uint_as_float(v[i]));
+                    acc += w * x * x;
+                }
+            }
+        }
+        for (int off = 16; off > 0; off /= 2) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (lane == 0) red[warp] = acc;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0)
+        pur_out[static_cast<std::size_t>(job) * gridDim.x + blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    if (warp == TC_PWARPS)
+    {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+    }
+}
+} // namespace
+
+bool gram_tc_supported(int n, int k)
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_TC_GRAM");
+        return !(v && v[0] == '0');
+    }();
+    return on && k >= 7 && k <= 16 && (n - k) >= 4;
+}
+
+int gram_tc_tiles(int k)
+{
+    const int t = 1 << (k - 7);
+    return t * (t + 1) / 2;
+}
+
+std::size_t gram_tc_scratch_bytes(int k, int njobs)
+{
+    return sizeof(double) * static_cast<std::size_t>(gram_tc_tiles(k)) * njobs;
+}
+
+cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                           const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
+                           std::size_t scratch_bytes, int *err, cudaStream_t s)
+{
+    if (njobs <= 0) return cudaSuccess;
+    if (!gram_tc_supported(n, k)) return cudaErrorInvalidValue;
+    const int tiles = gram_tc_tiles(k);
+    if (gram_tc_scratch_bytes(k, njobs) > scratch_bytes) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(TC_SMEM));
+    if (e != cudaSuccess) return e;
+    dim3 grid(tiles, 1, njobs);
+    k_gram_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(states, n, d_jobs, collapse, collapse_stride,
+                                                static_cast<double *>(scratch), err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
     return cudaGetLastError();
 }
 

@@ -53,6 +53,15 @@ cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, in
 
 std::size_t gram_scratch_bytes(int n, int k, int njobs, bool rho);
 
+// Purity through the tensor-core (tcgen05, 3xTF32) Gram, FP32 states only;
+// needs 7 <= k <= 16 and n - k >= 4. err receives bit 4 if a pipeline wait
+// timed out (the kernel then returns without a result).
+bool gram_tc_supported(int n, int k);
+std::size_t gram_tc_scratch_bytes(int k, int njobs);
+cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                           const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
+                           std::size_t scratch_bytes, int *err, cudaStream_t s);
+
 // Purity of full matrices rho[job][d][d].
 cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, cudaStream_t s);
 

@@ -247,3 +247,17 @@ def test_full_size_chain_L24(mg, orc):
     assert abs(got["obs"][0, 0, 1] - s2) < 1e-5
     subs = np.array([[s, (s + 1) % n, (s + 2) % n] for s in range(n)])
     np.testing.assert_allclose(got["rho3"][0].ravel(), orc.rho3(r["psi"], subs), rtol=0, atol=2e-6)
+
+
+@pytest.mark.parametrize("n,kept,ferm", [(14, list(range(7)), False), (16, list(range(8)), False),
+                                         (18, [17, 3, 9, 0, 12, 5, 8, 1, 14], True), (20, list(range(10, 20)), False),
+                                         (16, [15, 14, 13, 12, 11, 10, 9, 8], True)])
+def test_tensor_core_renyi2(mg, orc, n, kept, ferm):
+    """FP32 Renyi-2 through the tcgen05 3xTF32 Gram (cuts with >= 128 rows)
+    against the FP64 oracle's RDM purity."""
+    psi = random_state(n, 77 + n)
+    e = device_state(mg, psi, False)
+    got = mg.renyi2(e.data, n, kept, ferm, False)
+    rho = orc.rdm(psi, kept, ferm)
+    want = -np.log2(np.sum(np.abs(rho) ** 2))
+    assert abs(got - want) < 1e-5, (got, want)
