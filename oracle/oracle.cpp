@@ -423,6 +423,218 @@ std::vector<int> half_chain(int n)
 }
 } // namespace
 
+
+// ---------------------------------------------------------------------------
+// Free-fermion (Gaussian) monitored circuit on the Majorana covariance
+// matrix. The reference has no code for this path (it simulates fermionic
+// circuits only as Jordan-Wigner state vectors); this is a restatement from
+// the mathematics, cross-checked in the tests against the state-vector
+// restatement above with the fermionic trace.
+//
+//   Gamma_ab = (i/2) <[g_a, g_b]>, real antisymmetric, Gamma^2 = -1 (pure)
+//   product state: Gamma_{2j,2j+1} = 1 (i g_{2j} g_{2j+1} = +1 on every mode)
+//   gate on modes (k, k+1 mod N): Haar SO(4) rotation O on Majoranas
+//     (2k, 2k+1, 2k', 2k'+1), Gamma <- O Gamma O^T
+//   measurement of P_j = i g_{2j} g_{2j+1}: outcome s = +1 with probability
+//     (1 + Gamma_ab)/2 (a = 2j, b = 2j+1); then for k, l outside {a, b}
+//     Gamma_kl += (Gamma_kb Gamma_la - Gamma_ka Gamma_lb) / (Gamma_ab + s),
+//     rows/columns a, b are cleared and Gamma_ab = s.
+//   re-purification: Gamma <- Gamma (3 + Gamma^2) / 2 (Newton-Schulz step of
+//     the matrix sign of i Gamma).
+//   entropy of a mode set M (bits): eigenvalues +-nu of i Gamma_M,
+//     S = sum_{pairs} H2((1 + nu)/2).
+namespace ff
+{
+using Mat = std::vector<double>;
+
+void so4_haar(std::mt19937 &rng, double *O)
+{
+    std::normal_distribution<double> gauss(0.0, 1.0);
+    double q[16];
+    for (int c = 0; c < 4; ++c)
+    {
+        double v[4];
+        for (int r = 0; r < 4; ++r) v[r] = gauss(rng);
+        for (int k = 0; k < c; ++k)
+        {
+            double dot = 0.0;
+            for (int r = 0; r < 4; ++r) dot += q[r * 4 + k] * v[r];
+            for (int r = 0; r < 4; ++r) v[r] -= q[r * 4 + k] * dot;
+        }
+        double nn = 0.0;
+        for (int r = 0; r < 4; ++r) nn += v[r] * v[r];
+        const double len = std::sqrt(nn);
+        for (int r = 0; r < 4; ++r) q[r * 4 + c] = v[r] / len;
+    }
+    // determinant sign by cofactor expansion
+    auto det3 = [&](int r0, int r1, int r2, int c0, int c1, int c2) {
+        return q[r0 * 4 + c0] * (q[r1 * 4 + c1] * q[r2 * 4 + c2] - q[r1 * 4 + c2] * q[r2 * 4 + c1]) -
+               q[r0 * 4 + c1] * (q[r1 * 4 + c0] * q[r2 * 4 + c2] - q[r1 * 4 + c2] * q[r2 * 4 + c0]) +
+               q[r0 * 4 + c2] * (q[r1 * 4 + c0] * q[r2 * 4 + c1] - q[r1 * 4 + c1] * q[r2 * 4 + c0]);
+    };
+    const double det = q[0] * det3(1, 2, 3, 1, 2, 3) - q[1] * det3(1, 2, 3, 0, 2, 3) + q[2] * det3(1, 2, 3, 0, 1, 3) -
+                       q[3] * det3(1, 2, 3, 0, 1, 2);
+    if (det < 0)
+        for (int r = 0; r < 4; ++r) q[r * 4] = -q[r * 4];
+    std::copy(q, q + 16, O);
+}
+
+struct Layer
+{
+    std::vector<int> modes;   // first mode of each gate (gate on (m, m+1 mod N))
+    std::vector<double> rot;  // 16 per gate, row-major
+    std::vector<int> sites;   // measured modes, ascending
+};
+
+void draw(std::vector<Layer> &layers, std::uint64_t seed, int N, int depth, double p, bool closed,
+          std::mt19937 &meas)
+{
+    std::mt19937 g;
+    seed_pair(seed, g, meas);
+    layers.resize(depth);
+    for (int t = 0; t < depth; ++t)
+    {
+        Layer &L = layers[t];
+        L.modes.clear();
+        L.rot.clear();
+        L.sites.clear();
+        const int start = t & 1;
+        const int stop = (closed && start == 1 && N > 2) ? N : N - 1;
+        for (int m = start; m < stop; m += 2)
+        {
+            double O[16];
+            so4_haar(g, O);
+            L.modes.push_back(m);
+            L.rot.insert(L.rot.end(), O, O + 16);
+        }
+        if (p >= 1.0)
+            for (int j = 0; j < N; ++j) L.sites.push_back(j);
+        else if (p > 0.0)
+        {
+            std::bernoulli_distribution flag(p);
+            for (int j = 0; j < N; ++j)
+                if (flag(g)) L.sites.push_back(j);
+        }
+    }
+}
+
+void rotate(Mat &G, int N, int m, const double *O)
+{
+    const int M = 2 * N;
+    const int m2 = (m + 1) % N;
+    const int idx[4] = {2 * m, 2 * m + 1, 2 * m2, 2 * m2 + 1};
+    // rows: G[idx, :] = O G[idx, :]
+    std::vector<double> tmp(4 * M);
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < M; ++c)
+        {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += O[r * 4 + k] * G[idx[k] * M + c];
+            tmp[r * M + c] = s;
+        }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < M; ++c) G[idx[r] * M + c] = tmp[r * M + c];
+    // columns: G[:, idx] = G[:, idx] O^T
+    for (int r = 0; r < M; ++r)
+    {
+        double row[4];
+        for (int k = 0; k < 4; ++k) row[k] = G[r * M + idx[k]];
+        for (int c = 0; c < 4; ++c)
+        {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += row[k] * O[c * 4 + k];
+            G[r * M + idx[c]] = s;
+        }
+    }
+}
+
+// Returns the outcome s and the probability of it.
+int measure(Mat &G, int N, int j, double u, const int *forced, double &prob)
+{
+    const int M = 2 * N, a = 2 * j, b = 2 * j + 1;
+    const double g = G[a * M + b];
+    const double p_plus = std::clamp((1.0 + g) / 2.0, 0.0, 1.0);
+    int s = forced ? (*forced > 0 ? 1 : -1) : (u < p_plus ? 1 : -1);
+    prob = s > 0 ? p_plus : 1.0 - p_plus;
+    const double denom = g + s;
+    std::vector<double> ua(M), vb(M);
+    for (int k = 0; k < M; ++k)
+    {
+        ua[k] = G[k * M + a];
+        vb[k] = G[k * M + b];
+    }
+    for (int k = 0; k < M; ++k)
+    {
+        if (k == a || k == b) continue;
+        for (int l = 0; l < M; ++l)
+        {
+            if (l == a || l == b) continue;
+            G[k * M + l] += (vb[k] * ua[l] - ua[k] * vb[l]) / denom;
+        }
+    }
+    for (int k = 0; k < M; ++k)
+    {
+        G[k * M + a] = G[a * M + k] = 0.0;
+        G[k * M + b] = G[b * M + k] = 0.0;
+    }
+    G[a * M + b] = s;
+    G[b * M + a] = -s;
+    return s;
+}
+
+void repurify(Mat &G, int N)
+{
+    const int M = 2 * N;
+    Mat G2(M * M, 0.0), out(M * M, 0.0);
+    for (int i = 0; i < M; ++i)
+        for (int k = 0; k < M; ++k)
+        {
+            const double gik = G[i * M + k];
+            if (gik == 0.0) continue;
+            for (int j = 0; j < M; ++j) G2[i * M + j] += gik * G[k * M + j];
+        }
+    for (int i = 0; i < M; ++i) G2[i * M + i] += 3.0;
+    for (int i = 0; i < M; ++i)
+        for (int k = 0; k < M; ++k)
+        {
+            const double gik = G[i * M + k];
+            if (gik == 0.0) continue;
+            for (int j = 0; j < M; ++j) out[i * M + j] += 0.5 * gik * G2[k * M + j];
+        }
+    G.swap(out);
+}
+
+double h2(double x)
+{
+    double s = 0.0;
+    if (x > 1e-15) s -= x * std::log2(x);
+    if (1.0 - x > 1e-15) s -= (1.0 - x) * std::log2(1.0 - x);
+    return s;
+}
+
+double block_entropy(const Mat &G, int N, const std::vector<int> &modes)
+{
+    const int m = static_cast<int>(modes.size());
+    if (m == 0) return 0.0;
+    const int M = 2 * N, d = 2 * m;
+    std::vector<int> maj;
+    for (int q : modes)
+    {
+        maj.push_back(2 * q);
+        maj.push_back(2 * q + 1);
+    }
+    // i * Gamma_M is Hermitian; its eigenvalues come in +-nu pairs.
+    std::vector<cd> H(d * d);
+    for (int r = 0; r < d; ++r)
+        for (int c = 0; c < d; ++c) H[r * d + c] = cd(0.0, G[maj[r] * M + maj[c]]);
+    std::vector<double> w;
+    eig_hermitian(H, d, w);
+    double s = 0.0;
+    for (double l : w) s += 0.5 * h2(std::clamp((1.0 + l) / 2.0, 0.0, 1.0));
+    return std::abs(s) < 1e-12 ? 0.0 : s;
+}
+} // namespace ff
+
 extern "C" {
 
 std::uint64_t orc_splitmix64(std::uint64_t v) { return mix64(v); }
@@ -671,6 +883,121 @@ int orc_run_batch(std::uint64_t master, int first, int count, int n, int periods
         if (s2_out) s2_out[i] = obs[4 * (2 * periods - 1) + 1];
     }
     return failed;
+}
+
+
+// Free-fermion trajectory: N modes, `depth` layers, measurement rate p.
+//   forced[depth][N] (optional, +-1 per measured mode in ascending order)
+//   outcomes[depth][N] receives +-1 (0 padding); probs likewise
+//   gamma_out[2N x 2N] final covariance (optional)
+//   block_len[nb] -> S of modes [0, len) in s_blocks[nb]; tmi_out: TMI of
+//   contiguous quarters (N % 4 == 0), both in bits, final state.
+int orc_ff_trajectory(std::uint64_t seed, int N, int depth, double p, int closed, int repurify_every,
+                      const int *forced, int *outcomes, double *probs, double *gamma_out, const int *block_len,
+                      int nb, double *s_blocks, double *tmi_out)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<ff::Layer> layers;
+        ff::draw(layers, seed, N, depth, p, closed != 0, meas);
+        const int M = 2 * N;
+        ff::Mat G(M * M, 0.0);
+        for (int j = 0; j < N; ++j)
+        {
+            G[(2 * j) * M + 2 * j + 1] = 1.0;
+            G[(2 * j + 1) * M + 2 * j] = -1.0;
+        }
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        for (int t = 0; t < depth; ++t)
+        {
+            const ff::Layer &L = layers[t];
+            for (std::size_t g = 0; g < L.modes.size(); ++g) ff::rotate(G, N, L.modes[g], &L.rot[16 * g]);
+            if (outcomes)
+                for (int j = 0; j < N; ++j) outcomes[t * N + j] = 0;
+            for (std::size_t i = 0; i < L.sites.size(); ++i)
+            {
+                const double u = unif(meas);
+                double pr = 0.0;
+                const int *f = forced ? &forced[t * N + i] : nullptr;
+                const int s = ff::measure(G, N, L.sites[i], u, f, pr);
+                if (outcomes) outcomes[t * N + i] = s;
+                if (probs) probs[t * N + i] = pr;
+            }
+            if (repurify_every > 0 && (t + 1) % repurify_every == 0) ff::repurify(G, N);
+        }
+        if (gamma_out) std::copy(G.begin(), G.end(), gamma_out);
+        for (int i = 0; i < nb; ++i)
+        {
+            std::vector<int> modes;
+            for (int q = 0; q < block_len[i]; ++q) modes.push_back(q);
+            s_blocks[i] = ff::block_entropy(G, N, modes);
+        }
+        if (tmi_out && N % 4 == 0)
+        {
+            const int b = N / 4;
+            auto rng_ = [&](int a, int c) {
+                std::vector<int> v;
+                for (int i = 0; i < c; ++i) v.push_back(a + i);
+                return v;
+            };
+            auto cat = [](std::vector<int> x, const std::vector<int> &y) {
+                x.insert(x.end(), y.begin(), y.end());
+                return x;
+            };
+            const auto A = rng_(0, b), B = rng_(b, b), C = rng_(2 * b, b), D = rng_(3 * b, b);
+            *tmi_out = ff::block_entropy(G, N, A) + ff::block_entropy(G, N, B) + ff::block_entropy(G, N, C) +
+                       ff::block_entropy(G, N, D) - ff::block_entropy(G, N, cat(A, B)) -
+                       ff::block_entropy(G, N, cat(A, C)) - ff::block_entropy(G, N, cat(B, C));
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Layer draw of a free-fermion trajectory: gate first modes, rotations
+// (16 per gate, row-major), measured-mode lists and measurement uniforms.
+int orc_ff_draw(std::uint64_t seed, int N, int depth, double p, int closed, int *gates_per_layer, int *gate_mode,
+                double *rot, int *sites_per_layer, int *sites, double *uniforms)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<ff::Layer> layers;
+        ff::draw(layers, seed, N, depth, p, closed != 0, meas);
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        const int mg = N / 2 + 1;
+        int u = 0;
+        for (int t = 0; t < depth; ++t)
+        {
+            gates_per_layer[t] = static_cast<int>(layers[t].modes.size());
+            for (std::size_t g = 0; g < layers[t].modes.size(); ++g)
+            {
+                gate_mode[t * mg + g] = layers[t].modes[g];
+                std::copy(&layers[t].rot[16 * g], &layers[t].rot[16 * g] + 16, &rot[(t * mg + g) * 16]);
+            }
+            sites_per_layer[t] = static_cast<int>(layers[t].sites.size());
+            for (std::size_t i = 0; i < layers[t].sites.size(); ++i)
+            {
+                sites[t * N + i] = layers[t].sites[i];
+                uniforms[u++] = unif(meas);
+            }
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+double orc_ff_block_entropy(const double *gamma, int N, const int *modes, int m)
+{
+    ff::Mat G(gamma, gamma + 4 * N * N);
+    return ff::block_entropy(G, N, std::vector<int>(modes, modes + m));
 }
 
 int orc_max_threads()

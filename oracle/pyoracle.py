@@ -173,3 +173,53 @@ def run_batch(master, first, count, n, periods, p, closed=True, chunk_bits=16, o
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+# ------------------------------------------------------------ free fermions
+def _ff_bind():
+    L = lib()
+    if getattr(L, "_ff_bound", False):
+        return L
+    vp, ci, cd, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+    L.orc_ff_trajectory.argtypes = [u64, ci, ci, cd, ci, ci, vp, vp, vp, vp, vp, ci, vp, vp]
+    L.orc_ff_draw.argtypes = [u64, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
+    L.orc_ff_block_entropy.restype = cd
+    L.orc_ff_block_entropy.argtypes = [vp, ci, vp, ci]
+    L._ff_bound = True
+    return L
+
+
+def ff_trajectory(seed, N, depth, p, closed=True, repurify_every=0, forced=None, blocks=(), want_gamma=True):
+    L = _ff_bind()
+    outcomes = np.zeros((depth, N), np.int32)
+    probs = np.zeros((depth, N))
+    gamma = np.zeros((2 * N, 2 * N)) if want_gamma else None
+    bl = np.ascontiguousarray(blocks, np.int32)
+    sb = np.zeros(max(1, len(bl)))
+    tmi = np.zeros(1)
+    f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+    if L.orc_ff_trajectory(seed, N, depth, p, int(closed), repurify_every, _p(f), _p(outcomes), _p(probs),
+                           _p(gamma), _p(bl), len(bl), _p(sb), _p(tmi) if N % 4 == 0 else None):
+        raise RuntimeError("orc_ff_trajectory failed")
+    return dict(outcomes=outcomes, probs=probs, gamma=gamma, s_blocks=sb[: len(bl)], tmi=float(tmi[0]))
+
+
+def ff_draw(seed, N, depth, p, closed=True):
+    L = _ff_bind()
+    mg = N // 2 + 1
+    gpl = np.zeros(depth, np.int32)
+    gm = np.zeros((depth, mg), np.int32)
+    rot = np.zeros((depth, mg, 16))
+    spl = np.zeros(depth, np.int32)
+    sites = np.full((depth, N), -1, np.int32)
+    uni = np.zeros(depth * N + 1)
+    if L.orc_ff_draw(seed, N, depth, p, int(closed), _p(gpl), _p(gm), _p(rot), _p(spl), _p(sites), _p(uni)):
+        raise RuntimeError("orc_ff_draw failed")
+    return dict(gates_per_layer=gpl, gate_mode=gm, rot=rot, sites_per_layer=spl, sites=sites, uniforms=uni)
+
+
+def ff_block_entropy(gamma, modes):
+    L = _ff_bind()
+    g = np.ascontiguousarray(gamma, np.float64)
+    m = np.ascontiguousarray(modes, np.int32)
+    return L.orc_ff_block_entropy(_p(g), g.shape[0] // 2, _p(m), len(m))
