@@ -846,6 +846,12 @@ __device__ __forceinline__ std::uint64_t sw128_desc(std::uint32_t saddr)
 // Instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128.
 constexpr std::uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCN >> 3) << 17) | ((TCM >> 4) << 24);
 
+// Chunks (of 32 real K) accumulated in one tensor-memory buffer before the
+// producer warps drain it into registers: the tensor core's FP32 accumulation
+// carries a relative bias of order 2^-23 per accumulation step, so long
+// in-TMEM sums drift (measured: linear in K); short segments bound it.
+constexpr int TC_SEG = 2;
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gram_tc(const Cx<float> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
               const Collapse *__restrict__ col, std::size_t col_stride, double *__restrict__ pur_out,
@@ -853,14 +859,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 {
     extern __shared__ __align__(1024) unsigned char tc_raw[];
     __shared__ GramJob J;
-    __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], done_bar;
+    __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], seg_bar[2], drained_bar[2];
     __shared__ std::uint32_t tmem_base;
     __shared__ std::uint64_t roffA[TCM], roffB[TCM], crossA[TCM], crossB[TCM], elo[16];
-    __shared__ double red[4];
+    __shared__ double red[TC_PWARPS];
     __shared__ volatile int abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // 1024-byte aligned stage buffers (swizzle atoms).
     const std::uint32_t raw_s = sm_addr(tc_raw);
     unsigned char *smem = tc_raw + ((1024u - (raw_s & 1023u)) & 1023u);
     const int job = blockIdx.z;
@@ -870,25 +875,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (tid == 0)
     {
         J = jobs[job];
-        for (int s = 0; s < TC_STAGES; ++s)
+        for (int st = 0; st < TC_STAGES; ++st)
         {
-            mbar_init(&full_bar[s], TC_PWARPS);
-            mbar_init(&empty_bar[s], 1);
+            mbar_init(&full_bar[st], TC_PWARPS);
+            mbar_init(&empty_bar[st], 1);
         }
-        mbar_init(&done_bar, 1);
+        for (int b = 0; b < 2; ++b)
+        {
+            mbar_init(&seg_bar[b], 1);
+            mbar_init(&drained_bar[b], TC_PWARPS);
+        }
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == TC_PWARPS)
     {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(sm_addr(&tmem_base))
+        // Two 256-column accumulator buffers (the whole tensor memory).
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(sm_addr(&tmem_base))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
     __syncthreads();
     const int k = J.k;
-    const int d = 1 << k;
     const int nenv = n - k;
     const int r0 = tr * TCM, c0 = tc * TCM;
     if (tid < TCM)
@@ -929,12 +938,47 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const std::uint32_t tmem = tmem_base;
     const Cx<float> *psi = states + (static_cast<std::size_t>(J.traj) << n);
     const int nchunks = 1 << (nenv - 4); // 16 complex environment columns per stage
+    const int nseg = (nchunks + TC_SEG - 1) / TC_SEG;
 
     if (warp < TC_PWARPS)
     {
-        const int ptid = tid;
+        // Warp w drains TMEM lanes 32*(w%4).. and buffer columns 128*(w/4)..;
+        // the running sums stay in registers for the whole K loop.
+        float acc[128];
+#pragma unroll
+        for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+        const std::uint32_t lane_base = static_cast<std::uint32_t>((warp & 3) * 32) << 16;
+        const std::uint32_t col_half = (warp >> 2) * 128;
+        int next_drain = 0;
+        auto drain = [&](int seg) {
+            if (!mbar_wait(&seg_bar[seg & 1], (seg >> 1) & 1, &abort_flag, err)) return;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int cb = 0; cb < 4; ++cb)
+            {
+                std::uint32_t v[32];
+                const std::uint32_t taddr = tmem + lane_base + (seg & 1) * 256 + col_half + cb * 32;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[cb * 32 + i] += __uint_as_float(v[i]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&drained_bar[seg & 1]);
+        };
         for (int chunk = 0; chunk < nchunks; ++chunk)
         {
+            // Drain segment s once one chunk of segment s+1 is queued.
+            if (chunk >= (next_drain + 1) * TC_SEG + 1 && next_drain < nseg) drain(next_drain++);
             const int st = chunk & 1;
             if (chunk >= TC_STAGES && !mbar_wait(&empty_bar[st], ((chunk >> 1) - 1) & 1, &abort_flag, err)) break;
             unsigned char *stage = smem + st * TC_STAGE;
@@ -944,7 +988,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             std::uint64_t ehi = 0;
             for (int b = 4; b < nenv; ++b)
                 if ((e0 >> b) & 1ull) ehi |= 1ull << J.env[b];
-            for (int item = ptid; item < 2 * TCM * 8; item += TC_PWARPS * 32)
+            for (int item = tid; item < 2 * TCM * 8; item += TC_PWARPS * 32)
             {
                 const int which = item >= TCM * 8;
                 const int rem = item & (TCM * 8 - 1);
@@ -966,7 +1010,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     gather(psi, ehi | elo[2 * q] | ro, cl, has_col, (__popcll(ea & cx) & 1) != 0);
                 const Cx<float> v1 =
                     gather(psi, ehi | elo[2 * q + 1] | ro, cl, has_col, (__popcll(eb & cx) & 1) != 0);
-                const float4 X = make_float4(v0.re, v0.im, v1.re, v1.im);
                 auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 v) {
                     const int off = (rr >> 3) * 1024 + (rr & 7) * 128 + ((q ^ (rr & 7)) << 4);
                     float4 h, l;
@@ -983,11 +1026,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 };
                 if (!which)
                 {
-                    put(Ahi, Alo, row, X);
+                    put(Ahi, Alo, row, make_float4(v0.re, v0.im, v1.re, v1.im));
                 }
                 else
                 {
-                    put(Bhi, Blo, row, X);
+                    put(Bhi, Blo, row, make_float4(v0.re, v0.im, v1.re, v1.im));
                     put(Bhi, Blo, TCM + row, make_float4(-v0.im, v0.re, -v1.im, v1.re));
                 }
             }
@@ -996,14 +1039,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             __syncwarp();
             if (lane == 0) mbar_arrive(&full_bar[st]);
         }
+        while (next_drain < nseg) drain(next_drain++);
+
+        // Weighted squares of this thread's row: warps 0-3 hold Re rho, 4-7 Im rho.
+        const int r = r0 + (warp & 3) * 32 + lane;
+        double sum = 0.0;
+        if (!abort_flag)
+        {
+#pragma unroll
+            for (int i = 0; i < 128; ++i)
+            {
+                const int c = c0 + i;
+                const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
+                const double x = static_cast<double>(acc[i]);
+                sum += w * x * x;
+            }
+        }
+        for (int off = 16; off > 0; off /= 2) sum += __shfl_down_sync(0xffffffffu, sum, off);
+        if (lane == 0) red[warp] = sum;
     }
     else if (lane == 0)
     {
         for (int chunk = 0; chunk < nchunks; ++chunk)
         {
             const int st = chunk & 1;
+            const int seg = chunk / TC_SEG;
+            const int buf = seg & 1;
+            if (chunk % TC_SEG == 0 && seg >= 2 &&
+                !mbar_wait(&drained_bar[buf], ((seg >> 1) - 1) & 1, &abort_flag, err))
+                break;
             if (!mbar_wait(&full_bar[st], (chunk >> 1) & 1, &abort_flag, err)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const std::uint32_t dt = tmem + buf * 256;
             const std::uint32_t base = sm_addr(smem + st * TC_STAGE);
             const std::uint32_t Ahi = base, Alo = base + TC_A_BYTES;
             const std::uint32_t Bhi = base + 2 * TC_A_BYTES, Blo = Bhi + TC_B_BYTES;
@@ -1013,75 +1080,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const std::uint32_t koff = ks * 32;
                 const std::uint64_t ah = sw128_desc(Ahi + koff), al = sw128_desc(Alo + koff);
                 const std::uint64_t bh = sw128_desc(Bhi + koff), bl = sw128_desc(Blo + koff);
-                const std::uint32_t acc0 = (chunk | ks) ? 1u : 0u;
+                const std::uint32_t acc0 = ((chunk % TC_SEG) | ks) ? 1u : 0u;
                 asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
                              "l"(ah), "l"(bh), "r"(kTcIdesc), "r"(acc0)
                              : "memory");
                 asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
                              "l"(ah), "l"(bl), "r"(kTcIdesc), "r"(1u)
                              : "memory");
                 asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                             " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(dt),
                              "l"(al), "l"(bh), "r"(kTcIdesc), "r"(1u)
                              : "memory");
             }
-            // Stage st may be overwritten once these MMAs have read it.
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              sm_addr(&empty_bar[st]))
                          : "memory");
+            if (chunk % TC_SEG == TC_SEG - 1 || chunk == nchunks - 1)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 sm_addr(&seg_bar[buf]))
+                             : "memory");
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                         sm_addr(&done_bar))
-                     : "memory");
-    }
-
-    if (warp < 4)
-    {
-        const bool ok = mbar_wait(&done_bar, 0, &abort_flag, err);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int row = warp * 32 + lane;
-        const int r = r0 + row;
-        double acc = 0.0;
-        if (ok)
-        {
-            for (int cb = 0; cb < 8; ++cb)
-            {
-                std::uint32_t v[32];
-                const std::uint32_t taddr = tmem + (static_cast<std::uint32_t>(warp * 32) << 16) + cb * 32;
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
-                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
-                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
-                    : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                const int cbase = c0 + (cb & 3) * 32;
-#pragma unroll
-                for (int i = 0; i < 32; ++i)
-                {
-                    const int c = cbase + i;
-                    const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
-                    const double x = static_cast<double>(__uint_as_float(v[i]));
-                    acc += w * x * x;
-                }
-            }
-        }
-        for (int off = 16; off > 0; off /= 2) acc += __shfl_down_sync(0xffffffffu, acc, off);
-        if (lane == 0) red[warp] = acc;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (tid == 0)
-        pur_out[static_cast<std::size_t>(job) * gridDim.x + blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    {
+        double t = 0.0;
+        for (int w = 0; w < TC_PWARPS; ++w) t += red[w];
+        pur_out[static_cast<std::size_t>(job) * gridDim.x + blockIdx.x] = t;
+    }
     if (warp == TC_PWARPS)
     {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
     }
 }
 } // namespace
