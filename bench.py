@@ -177,7 +177,8 @@ def run_gb300(args):
 
     B = args.batch
     T = 2 * PERIODS
-    batch = mg.Batch(N_QUBITS, PERIODS, capacity=B, fp64=False, observables=mg.OBS_S2_HALF)
+    batch = mg.Batch(N_QUBITS, PERIODS, capacity=B, fp64=False, observables=mg.OBS_S2_HALF,
+                     tile_qubits=args.tile)
     seeds = seeds_for(rank, B)
     ps = p_for(B)
 
@@ -283,6 +284,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--tile", type=int, default=0, help="local qubits per pass tile (0 = library default)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

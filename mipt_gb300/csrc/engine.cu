@@ -953,13 +953,13 @@ __global__ void k_collapse(Cx<Real> *states, std::uint64_t dim, std::uint64_t to
     }
 }
 
-// MIPT_GB300_CLUSTER_PASS=0 selects the single-CTA register-round kernel for
-// FP32 passes instead of the two-CTA cluster kernel.
+// MIPT_GB300_CLUSTER_PASS=1 selects the two-CTA cluster kernel for FP32
+// passes (default: the single-CTA register-round kernel, measured faster).
 bool use_cluster_kernel()
 {
     static const bool on = [] {
         const char *v = std::getenv("MIPT_GB300_CLUSTER_PASS");
-        return !(v && v[0] == '0');
+        return v && v[0] == '1';
     }();
     return on;
 }
