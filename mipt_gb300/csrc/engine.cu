@@ -393,7 +393,7 @@ __device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
 template <typename Real, int RB>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
@@ -1027,6 +1027,15 @@ __host__ __device__ void histogram_geometry(int n, int kmax, int cmin, std::uint
     g.n_nl = n - k;
 }
 
+int fp32_register_bits()
+{
+    static const int rb = [] {
+        const char *v = std::getenv("MIPT_GB300_RB");
+        return (v && v[0] == '5') ? 5 : 6;
+    }();
+    return rb;
+}
+
 const PassGeom &fused_hist_geometry(const PassPlan &p, bool fp32)
 {
     return (fp32 && p.cluster_rounds > 0 && use_cluster_kernel()) ? p.hgeom : p.geom;
@@ -1447,7 +1456,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
         p.geom = make_geom(n, (1ull << kmax) - 1ull);
         p.gates.count = 0;
         plan_rounds(p, rb);
-        if (rb == 6) plan_cluster_rounds(p, cluster_register_bits());
+        if (rb >= 5) plan_cluster_rounds(p, cluster_register_bits());
         return {p};
     }
     // Try first tiles made of a low contiguous block, optionally with the top
@@ -1470,7 +1479,7 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
     for (auto &p : best)
     {
         plan_rounds(p, rb);
-        if (rb == 6) plan_cluster_rounds(p, cluster_register_bits());
+        if (rb >= 5) plan_cluster_rounds(p, cluster_register_bits());
     }
     return best;
 }
@@ -1518,12 +1527,23 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
     }
     if (plan.rounds > 0)
     {
-        constexpr int RB = register_bits<Real>();
-        if (plan.rb != RB) return cudaErrorInvalidValue;
         const std::size_t smem = sizeof(Cx<Real>) << plan.geom.k;
-        cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, RB>), smem);
+        if constexpr (sizeof(Real) == 4)
+        {
+            if (plan.rb == 6)
+            {
+                cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, 6>), smem);
+                if (e != cudaSuccess) return e;
+                k_pass_rounds<Real, 6><<<grid, 1u << (plan.geom.k - 6), smem, s>>>(
+                    states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
+                    fuse_hist, use_packed_fma() ? 1 : 0);
+                return cudaGetLastError();
+            }
+        }
+        if (plan.rb != 5) return cudaErrorInvalidValue;
+        cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, 5>), smem);
         if (e != cudaSuccess) return e;
-        k_pass_rounds<Real, RB><<<grid, 1u << (plan.geom.k - RB), smem, s>>>(
+        k_pass_rounds<Real, 5><<<grid, 1u << (plan.geom.k - 5), smem, s>>>(
             states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
             fuse_hist, use_packed_fma() ? 1 : 0);
         return cudaGetLastError();

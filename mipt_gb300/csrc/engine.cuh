@@ -75,8 +75,10 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
 // the layer's Born histogram (a half tile for the cluster kernel).
 const PassGeom &fused_hist_geometry(const PassPlan &p, bool fp32);
 
-// Register bits per thread of the register-round pass kernel.
-template <typename Real> constexpr int register_bits() { return sizeof(Real) == 4 ? 6 : 5; }
+// Register bits per thread of the register-round pass kernel (FP32: 6 by
+// default, MIPT_GB300_RB=5 for 32 amplitudes per thread; FP64: 5).
+int fp32_register_bits();
+template <typename Real> inline int register_bits() { return sizeof(Real) == 4 ? fp32_register_bits() : 5; }
 
 // Tile geometry used for a stand-alone histogram of the sites in `chunk`:
 // low contiguous qubits, then as many unmeasured qubits as fit, so that few
