@@ -183,6 +183,35 @@ long long mipt_gb300_batch_launches(mipt_gb300_batch *batch);
 int mipt_gb300_batch_set_profiling(mipt_gb300_batch *batch, int enable);
 int mipt_gb300_batch_kernel_stats(mipt_gb300_batch *batch, double *ms, long long *launches);
 
+/* ------------------------------------------ free fermions (covariance) */
+
+/* Monitored free-fermion circuit on the Majorana covariance matrix of N
+ * modes (no counterpart in the reference, which simulates fermionic circuits
+ * only as Jordan-Wigner state vectors): layer t applies Haar SO(4) rotations
+ * to the four Majoranas of mode pairs (m, m+1 mod N), m = t%2, t%2+2, ...,
+ * then measures each mode's parity i g_{2j} g_{2j+1} with probability p.
+ * Same seed streams as the Haar path. */
+typedef struct mipt_gb300_ff_config
+{
+    int n_modes;          /* even, 4..128 */
+    int depth;            /* layers */
+    int closed;           /* 1: odd layers close the ring with modes (N-1, 0) */
+    int repurify_every;   /* FP64 re-purification every k layers (0: final only) */
+    int n_blocks;         /* entropies of the mode blocks [0, block_len[i]) */
+    const int *block_len;
+    int host_threads;     /* sampler threads, 0 = all */
+} mipt_gb300_ff_config;
+
+/* Runs `count` trajectories (seeds[i], rate p[i]). forced (nullable,
+ * [count][depth][N], +-1 for the i-th measured mode of a layer) replays
+ * outcomes. Outputs (nullable): outcomes/probs [count][depth][N] (+-1 and the
+ * realised probability per measured mode, 0 padding), gamma_out
+ * [count][2N][2N] final covariance (FP64, re-purified), s_blocks
+ * [count][n_blocks] and tmi [count] (contiguous quarters), in bits. */
+int mipt_gb300_ff_run(const mipt_gb300_ff_config *config, const uint64_t *seeds, const double *p, int count,
+                      const int *forced, int *outcomes, double *probs, double *gamma_out, double *s_blocks,
+                      double *tmi);
+
 /* Host-side seeding helpers (the reference's splitmix64 streams,
  * cpp/include/mipt/types.hpp:262-273). */
 uint64_t mipt_gb300_splitmix64(uint64_t value);

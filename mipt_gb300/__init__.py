@@ -29,6 +29,12 @@ class MiptError(RuntimeError):
         self.status = status
 
 
+class FFConfig(ctypes.Structure):
+    _fields_ = [("n_modes", ctypes.c_int), ("depth", ctypes.c_int), ("closed", ctypes.c_int),
+                ("repurify_every", ctypes.c_int), ("n_blocks", ctypes.c_int),
+                ("block_len", ctypes.POINTER(ctypes.c_int)), ("host_threads", ctypes.c_int)]
+
+
 class BatchConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in (
         "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
@@ -85,6 +91,7 @@ def lib():
     L.mipt_gb300_trajectory_seed.argtypes = [u64, u64]
     L.mipt_gb300_trajectory_seed.restype = u64
     L.mipt_gb300_draw_haar.argtypes = [u64, ci, ci, cd, ci, ci, vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_ff_run.argtypes = [ctypes.POINTER(FFConfig), vp, vp, ci, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -311,3 +318,24 @@ def outcomes_to_mask(sites, outcomes):
         if s >= 0 and o:
             m |= 1 << int(s)
     return m
+
+
+# ----------------------------------------------------------- free fermions
+def ff_run(seeds, p, n_modes, depth, closed=True, repurify_every=64, blocks=(), tmi=True, forced=None,
+           want_gamma=False, host_threads=0):
+    """Monitored free-fermion trajectories on the Majorana covariance matrix."""
+    seeds = np.ascontiguousarray(seeds, np.uint64)
+    c = len(seeds)
+    p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, np.float64), seeds.shape))
+    bl = np.ascontiguousarray(blocks, np.int32)
+    cfg = FFConfig(n_modes, depth, int(closed), repurify_every, len(bl),
+                   bl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if len(bl) else None, host_threads)
+    outcomes = np.zeros((c, depth, n_modes), np.int32)
+    probs = np.zeros((c, depth, n_modes))
+    gamma = np.zeros((c, 2 * n_modes, 2 * n_modes)) if want_gamma else None
+    sb = np.zeros((c, max(1, len(bl))))
+    t = np.zeros(c) if tmi else None
+    f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+    _check(lib().mipt_gb300_ff_run(ctypes.byref(cfg), _p(seeds), _p(p), c, _p(f), _p(outcomes), _p(probs),
+                                   _p(gamma), _p(sb), _p(t)))
+    return dict(outcomes=outcomes, probs=probs, gamma=gamma, s_blocks=sb[:, : len(bl)], tmi=t)

@@ -530,6 +530,12 @@ constexpr int kCoalesceQubits = 4;
 
 } // namespace
 
+namespace mg
+{
+int api_fail(int code, const std::string &what) { return fail(code, what); }
+int api_cuda_fail(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+} // namespace mg
+
 // ======================================================================= engine
 struct mipt_gb300_engine
 {

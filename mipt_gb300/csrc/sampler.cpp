@@ -178,3 +178,115 @@ void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int
 }
 
 } // namespace mg
+
+namespace mg
+{
+namespace
+{
+// Haar SO(4): Gram-Schmidt of a real Gaussian 4x4 (columns), then the first
+// column negated when the determinant is negative.
+void so4_draw(std::mt19937 &rng, double *O)
+{
+    std::normal_distribution<double> gauss(0.0, 1.0);
+    double q[16];
+    for (int c = 0; c < 4; ++c)
+    {
+        double v[4];
+        for (double &x : v) x = gauss(rng);
+        for (int k = 0; k < c; ++k)
+        {
+            double proj = 0.0;
+            for (int r = 0; r < 4; ++r) proj += q[4 * r + k] * v[r];
+            for (int r = 0; r < 4; ++r) v[r] -= q[4 * r + k] * proj;
+        }
+        double nn = 0.0;
+        for (double x : v) nn += x * x;
+        const double len = std::sqrt(nn);
+        for (int r = 0; r < 4; ++r) q[4 * r + c] = v[r] / len;
+    }
+    auto m3 = [&](int c0, int c1, int c2) {
+        // minor of rows 1..3 and columns c0, c1, c2
+        return q[4 + c0] * (q[8 + c1] * q[12 + c2] - q[8 + c2] * q[12 + c1]) -
+               q[4 + c1] * (q[8 + c0] * q[12 + c2] - q[8 + c2] * q[12 + c0]) +
+               q[4 + c2] * (q[8 + c0] * q[12 + c1] - q[8 + c1] * q[12 + c0]);
+    };
+    const double det = q[0] * m3(1, 2, 3) - q[1] * m3(0, 2, 3) + q[2] * m3(0, 1, 3) - q[3] * m3(0, 1, 2);
+    if (det < 0)
+        for (int r = 0; r < 4; ++r) q[4 * r] = -q[4 * r];
+    for (int i = 0; i < 16; ++i) O[i] = q[i];
+}
+} // namespace
+
+void draw_fermion_trajectory(std::uint64_t seed, int n, int depth, double p, bool closed, FermionDraw &out)
+{
+    if (n < 2 || n > 128) throw std::invalid_argument("free-fermion chains need 2 <= N <= 128 modes");
+    std::mt19937 g, meas;
+    seed_mt(g, seed);
+    seed_mt(meas, splitmix64(seed ^ 0xa0761d0dull));
+    const int mg_ = n / 2 + 1;
+    out.n = n;
+    out.depth = depth;
+    out.max_gates = mg_;
+    out.gate_count.assign(depth, 0);
+    out.gate_mode.assign(static_cast<std::size_t>(depth) * mg_, 0);
+    out.rot.assign(static_cast<std::size_t>(depth) * mg_ * 16, 0.0);
+    out.meas_count.assign(depth, 0);
+    out.meas_mode.assign(static_cast<std::size_t>(depth) * n, 0);
+    out.uniform.assign(static_cast<std::size_t>(depth) * n, 0.0);
+    std::uniform_real_distribution<double> unif(0.0, 1.0);
+    for (int t = 0; t < depth; ++t)
+    {
+        const int start = t & 1;
+        const int stop = (closed && start == 1 && n > 2) ? n : n - 1;
+        int gi = 0;
+        for (int m = start; m < stop; m += 2, ++gi)
+        {
+            out.gate_mode[static_cast<std::size_t>(t) * mg_ + gi] = m;
+            so4_draw(g, &out.rot[(static_cast<std::size_t>(t) * mg_ + gi) * 16]);
+        }
+        out.gate_count[t] = gi;
+        int mc = 0;
+        if (p >= 1.0)
+        {
+            for (int j = 0; j < n; ++j) out.meas_mode[static_cast<std::size_t>(t) * n + mc++] = j;
+        }
+        else if (p > 0.0)
+        {
+            std::bernoulli_distribution flag(p);
+            for (int j = 0; j < n; ++j)
+                if (flag(g)) out.meas_mode[static_cast<std::size_t>(t) * n + mc++] = j;
+        }
+        out.meas_count[t] = mc;
+        for (int i = 0; i < mc; ++i) out.uniform[static_cast<std::size_t>(t) * n + i] = unif(meas);
+    }
+}
+
+void draw_fermion_batch(const std::uint64_t *seeds, const double *p, int count, int n, int depth, bool closed,
+                        std::vector<FermionDraw> &out, int threads)
+{
+    out.resize(count);
+    if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    threads = std::min(threads, std::max(1, count));
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto work = [&]() {
+        for (;;)
+        {
+            const int i = next.fetch_add(1);
+            if (i >= count) return;
+            try
+            {
+                draw_fermion_trajectory(seeds[i], n, depth, p[i], closed, out[i]);
+            }
+            catch (...)
+            {
+                failed = true;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(work);
+    for (auto &th : pool) th.join();
+    if (failed) throw std::runtime_error("free-fermion trajectory draw failed");
+}
+} // namespace mg

@@ -50,3 +50,26 @@ void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int
                      int chunk_bits, std::vector<TrajectoryDraw> &out, int threads);
 
 } // namespace mg
+
+namespace mg
+{
+// One free-fermion (Majorana covariance) trajectory: N modes, `depth`
+// layers. Layer t applies a Haar SO(4) rotation to the Majoranas of modes
+// (m, m+1 mod N) for each gate start m in gate_mode[t] (rot[16*g], row-major),
+// then measures the parity of every mode in measured[t] (ascending, one
+// uniform each, from the measurement stream). Same streams as the Haar path.
+struct FermionDraw
+{
+    int n = 0, depth = 0, max_gates = 0;
+    std::vector<int> gate_count;
+    std::vector<int> gate_mode;  // [depth][max_gates]
+    std::vector<double> rot;     // [depth][max_gates][16]
+    std::vector<int> meas_count;
+    std::vector<int> meas_mode;  // [depth][n]
+    std::vector<double> uniform; // [depth][n]
+};
+
+void draw_fermion_trajectory(std::uint64_t seed, int n, int depth, double p, bool closed, FermionDraw &out);
+void draw_fermion_batch(const std::uint64_t *seeds, const double *p, int count, int n, int depth, bool closed,
+                        std::vector<FermionDraw> &out, int threads);
+} // namespace mg
