@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libmipt_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu"]
+CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu"]
 CXX_SOURCES = ["sampler.cpp"]
 
 

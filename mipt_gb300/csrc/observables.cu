@@ -718,6 +718,22 @@ cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, in
     return cudaGetLastError();
 }
 
+cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                               double *purity_out, void *scratch, std::size_t scratch_bytes, cudaStream_t s)
+{
+    if (njobs <= 0) return cudaSuccess;
+    const int tiles = gram_tiles(k);
+    if (sizeof(double) * static_cast<std::size_t>(tiles) * njobs > scratch_bytes) return cudaErrorInvalidValue;
+    const std::uint64_t E = 1ull << (n - k);
+    dim3 grid(tiles, 1, njobs);
+    k_gram<float, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
+                                                        static_cast<double *>(scratch));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
+    return cudaGetLastError();
+}
+
 cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, cudaStream_t s)
 {
     if (njobs <= 0) return cudaSuccess;

@@ -53,6 +53,13 @@ cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, in
 
 std::size_t gram_scratch_bytes(int n, int k, int njobs, bool rho);
 
+// Purity of FP32 states with FP64 accumulation and no environment split:
+// one block per lower-triangle tile writes its partial into
+// scratch[job][tile] (gram_tiles(k) doubles per job, each written once),
+// then a fixed-order row sum writes purity_out[job].
+cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
+                               double *purity_out, void *scratch, std::size_t scratch_bytes, cudaStream_t s);
+
 // Purity through the tensor-core (tcgen05, 3xTF32) Gram, FP32 states only;
 // needs 7 <= k <= 16 and n - k >= 4. err receives bit 4 if a pipeline wait
 // timed out (the kernel then returns without a result).

@@ -1,0 +1,109 @@
+"""Allocation-free FP32 Renyi-2 (mipt_gb300_renyi2_f32_noalloc) against the
+allocating entry point (mipt_cuda_renyi2_f32), both through the C ABI.
+
+Tolerance: 1e-5 bits, the FP32 path's entropy bound. Each case calls the
+allocation-free entry point twice in a row; both results must agree with
+the allocating entry point, and with each other exactly (every reduction
+runs in a fixed order). The file name sorts last so that the module also
+runs after every other test in the same process; it needs no state from
+them and passes alone in a fresh process.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.gpu_util import random_state
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+E_INVALID = 9001
+
+
+@pytest.fixture(scope="module")
+def mg():
+    from mipt_gb300 import build
+    build.build()
+    import mipt_gb300
+    fn = mipt_gb300.lib().mipt_gb300_renyi2_f32_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    fn.restype = ctypes.c_int
+    return mipt_gb300
+
+
+def call_noalloc(mg, ptr, n, kept, ferm):
+    kept = np.ascontiguousarray(kept, np.int32)
+    out = np.full(1, np.nan)
+    rc = mg.lib().mipt_gb300_renyi2_f32_noalloc(ptr, n, kept.ctypes.data, len(kept), int(ferm), out.ctypes.data)
+    return rc, float(out[0])
+
+
+def noalloc(mg, ptr, n, kept, ferm):
+    rc, s = call_noalloc(mg, ptr, n, kept, ferm)
+    assert rc == 0, mg.lib().mipt_gb300_last_error().decode(errors="replace")
+    return s
+
+
+def fp32_state(mg, psi):
+    e = mg.Engine(fp64=False)
+    e.set_state(psi)
+    return e
+
+
+CASES = [
+    (10, [0, 1, 2, 3, 4], False),
+    (12, [11, 3, 7], True),
+    (14, [2], False),
+    (16, list(range(8)), False),
+    (18, [17, 3, 9, 0, 12, 5, 8, 1, 14], True),
+    (20, list(range(10, 20)), False),
+    (20, list(range(3, 17)), False),
+    (22, [0, 5, 10, 15, 20, 21, 1, 2, 3, 4, 6, 7], True),
+]
+
+
+@pytest.mark.parametrize("n,kept,ferm", CASES)
+def test_noalloc_matches_allocating_entry_point(mg, n, kept, ferm):
+    e = fp32_state(mg, random_state(n, 1000 + n))
+    want = mg.renyi2(e.data, n, kept, ferm, False)
+    first = noalloc(mg, e.data, n, kept, ferm)
+    second = noalloc(mg, e.data, n, kept, ferm)
+    assert abs(first - want) < TOL, (first, want)
+    assert abs(second - want) < TOL, (second, want)
+    assert first == second
+
+
+def test_noalloc_interleaved_sizes(mg):
+    """Back-to-back calls of different sizes reuse the one static array."""
+    n = 18
+    e = fp32_state(mg, random_state(n, 4242))
+    big, small = list(range(14)), [5, 9, 13]
+    want_big = mg.renyi2(e.data, n, big, False, False)
+    want_small = mg.renyi2(e.data, n, small, True, False)
+    got = [noalloc(mg, e.data, n, big, False), noalloc(mg, e.data, n, small, True),
+           noalloc(mg, e.data, n, big, False), noalloc(mg, e.data, n, small, True)]
+    assert abs(got[0] - want_big) < TOL and abs(got[2] - want_big) < TOL
+    assert abs(got[1] - want_small) < TOL and abs(got[3] - want_small) < TOL
+    assert got[0] == got[2] and got[1] == got[3]
+
+
+def test_noalloc_product_state_and_empty_cut(mg):
+    n = 10
+    psi = np.zeros(1 << n, np.complex128)
+    psi[0b1011001101] = 1.0
+    e = fp32_state(mg, psi)
+    assert noalloc(mg, e.data, n, [0, 1, 2, 3, 4], False) == 0.0
+    assert noalloc(mg, e.data, n, [], False) == 0.0
+
+
+def test_noalloc_rejects_oversize_request(mg):
+    n = 16
+    e = fp32_state(mg, random_state(n, 7))
+    rc, _ = call_noalloc(mg, e.data, n, list(range(15)), False)
+    assert rc == E_INVALID
+    msg = mg.lib().mipt_gb300_last_error().decode(errors="replace")
+    assert "14 kept modes" in msg and "512 KiB" in msg
+    # The rejection leaves the entry point usable.
+    want = mg.renyi2(e.data, n, list(range(14)), False, False)
+    assert abs(noalloc(mg, e.data, n, list(range(14)), False) - want) < TOL
