@@ -782,26 +782,38 @@ cudaError_t rho3_sweep(const Cx<Real> *states, int n, int batch, const int *d_su
 // Tensor-core Gram (tcgen05, FP32 states): purity Tr(rho^2) of
 // rho = M M^H without materialising rho.
 //
-// One real GEMM per 128x128 tile of rho: D[128 x 256] = X_r [128 x K] *
+// One real GEMM per 128x64 block of rho: D[128 x 128] = X_r [128 x K] *
 // [X_c ; Y_c]^T, where row i of X holds the Schmidt row as interleaved
-// (re, im) reals and Y holds (-im, re): D[:, :128] = Re rho, D[:, 128:] = Im rho.
+// (re, im) reals and Y holds (-im, re): D[:, :64] = Re rho, D[:, 64:] = Im rho.
 // Operands are split into TF32 hi/lo parts and D accumulates
 // hi*hi + hi*lo + lo*hi in FP32 tensor memory (3xTF32). Producer warps gather
 // the Schmidt rows straight from the state (pending collapse and fermionic
 // signs applied), split them and write the 128B-swizzled K-major layout the
-// MMA descriptors describe; one thread issues tcgen05.mma; the epilogue
-// reads D with tcgen05.ld and reduces the weighted squares.
+// MMA descriptors describe; one thread issues tcgen05.mma. The producers
+// issue all of a chunk's loads together, one chunk ahead of its stores, and
+// also drain D from tensor memory into FP32 registers between segments.
 namespace
 {
-constexpr int TCM = 128;                 // rows of a rho tile
-constexpr int TCN = 256;                 // X rows + Y rows of the column block
-constexpr int TC_PWARPS = 8;             // producer warps (warps 0-3 also run the epilogue)
+constexpr int TCM = 128;                 // rows of a rho block (A rows)
+constexpr int TCC = 64;                  // columns of a rho block (complex B rows)
+constexpr int TCN = 2 * TCC;             // X rows + Y rows = D columns
+constexpr int TC_PWARPS = 8;             // producer warps (they also drain and reduce D)
 constexpr int TC_THREADS = (TC_PWARPS + 1) * 32;
-constexpr int TC_A_BYTES = TCM * 128;    // one 128-row operand half: 16 KB
-constexpr int TC_B_BYTES = TCN * 128;    // 32 KB
+constexpr int TC_DCOLS = TCN / (TC_PWARPS / 4);                 // D columns drained per producer thread
+constexpr int TC_ITEMS = (TCM + TCC) * 8 / (TC_PWARPS * 32);   // gathered items per thread per chunk
+static_assert(TC_DCOLS % 32 == 0 && TC_ITEMS * TC_PWARPS * 32 == (TCM + TCC) * 8, "producer split");
+constexpr int TC_A_BYTES = TCM * 128;    // one operand half (hi or lo) of A: 16 KB
+constexpr int TC_B_BYTES = TCN * 128;    // one operand half of [X ; Y]: 16 KB
 constexpr int TC_STAGE = 2 * TC_A_BYTES + 2 * TC_B_BYTES;
-constexpr int TC_STAGES = 2;
-constexpr std::size_t TC_SMEM = static_cast<std::size_t>(TC_STAGES) * TC_STAGE + 1024;
+constexpr int TC_STAGES = 2;             // operand stages (split hi/lo, MMA layout)
+constexpr int TC_ELEMS = 2 * TC_ITEMS;   // amplitudes a producer thread gathers per chunk
+constexpr int TC_RAW_BYTES = TC_ELEMS * TC_PWARPS * 32 * 8;     // one chunk of raw amplitudes: 24 KB
+constexpr int TC_RING = 3;               // raw chunks in flight (cp.async ring)
+constexpr int TC_TMEM_BUFS = 4;          // accumulation buffers (segments in flight)
+constexpr int TC_TMEM_COLS = TC_TMEM_BUFS * TCN;
+static_assert(TC_ELEMS * 2 <= 32 && TC_TMEM_COLS <= 512, "chunk codes or tensor memory overflow");
+constexpr std::size_t TC_SMEM =
+    static_cast<std::size_t>(TC_STAGES) * TC_STAGE + static_cast<std::size_t>(TC_RING) * TC_RAW_BYTES + 1024;
 constexpr long long TC_SPIN = 1ll << 24;
 
 __device__ __forceinline__ std::uint32_t sm_addr(const void *p)
@@ -859,7 +871,7 @@ __device__ __forceinline__ std::uint64_t sw128_desc(std::uint32_t saddr)
            (2ull << 61);
 }
 
-// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = 256, M = 128.
+// Instruction descriptor: D = F32, A = B = TF32, both K-major, N = TCN, M = 128.
 constexpr std::uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCN >> 3) << 17) | ((TCM >> 4) << 24);
 
 // Chunks (of 32 real K) accumulated in one tensor-memory buffer before the
@@ -875,9 +887,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 {
     extern __shared__ __align__(1024) unsigned char tc_raw[];
     __shared__ GramJob J;
-    __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], seg_bar[2], drained_bar[2];
+    __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], seg_bar[TC_TMEM_BUFS],
+        drained_bar[TC_TMEM_BUFS];
     __shared__ std::uint32_t tmem_base;
-    __shared__ std::uint64_t roffA[TCM], roffB[TCM], crossA[TCM], crossB[TCM], elo[16];
+    __shared__ std::uint64_t roffA[TCM], roffB[TCC], crossA[TCM], crossB[TCC], elo[16];
     __shared__ double red[TC_PWARPS];
     __shared__ volatile int abort_flag;
 
@@ -896,7 +909,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&full_bar[st], TC_PWARPS);
             mbar_init(&empty_bar[st], 1);
         }
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < TC_TMEM_BUFS; ++b)
         {
             mbar_init(&seg_bar[b], 1);
             mbar_init(&drained_bar[b], TC_PWARPS);
@@ -906,8 +919,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (warp == TC_PWARPS)
     {
-        // Two 256-column accumulator buffers (the whole tensor memory).
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(sm_addr(&tmem_base))
+        // TC_TMEM_BUFS accumulation buffers of TCN columns.
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sm_addr(&tmem_base)),
+                     "n"(TC_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -915,7 +929,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     const int k = J.k;
     const int nenv = n - k;
-    const int r0 = tr * TCM, c0 = tc * TCM;
+    // Block (tr, tc) of the 128-row lower triangle is split into two 64-column halves.
+    const int r0 = tr * TCM, c0 = tc * TCM + static_cast<int>(blockIdx.y) * TCC;
     if (tid < TCM)
     {
         std::uint64_t oa = 0, ob = 0, xa = 0, xb = 0;
@@ -934,9 +949,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
         roffA[tid] = oa;
-        roffB[tid] = ob;
         crossA[tid] = J.fermion ? xa : 0ull;
-        crossB[tid] = J.fermion ? xb : 0ull;
+        if (tid < TCC)
+        {
+            roffB[tid] = ob;
+            crossB[tid] = J.fermion ? xb : 0ull;
+        }
     }
     else if (tid < TCM + 16)
     {
@@ -958,22 +976,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     if (warp < TC_PWARPS)
     {
-        // Warp w drains TMEM lanes 32*(w%4).. and buffer columns 128*(w/4)..;
-        // the running sums stay in registers for the whole K loop.
-        float acc[128];
+        // Warp w drains TMEM lanes 32*(w%4).. and buffer columns
+        // TC_DCOLS*(w/4)..; the running sums stay in registers for the whole
+        // K loop.
+        float acc[TC_DCOLS];
 #pragma unroll
-        for (int i = 0; i < 128; ++i) acc[i] = 0.f;
+        for (int i = 0; i < TC_DCOLS; ++i) acc[i] = 0.f;
         const std::uint32_t lane_base = static_cast<std::uint32_t>((warp & 3) * 32) << 16;
-        const std::uint32_t col_half = (warp >> 2) * 128;
+        const int col_base = (warp >> 2) * TC_DCOLS;
         int next_drain = 0;
         auto drain = [&](int seg) {
-            if (!mbar_wait(&seg_bar[seg & 1], (seg >> 1) & 1, &abort_flag, err)) return;
+            const int buf = seg % TC_TMEM_BUFS;
+            if (!mbar_wait(&seg_bar[buf], (seg / TC_TMEM_BUFS) & 1, &abort_flag, err)) return;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int cb = 0; cb < 4; ++cb)
+            for (int cb = 0; cb < TC_DCOLS / 32; ++cb)
             {
                 std::uint32_t v[32];
-                const std::uint32_t taddr = tmem + lane_base + (seg & 1) * 256 + col_half + cb * 32;
+                const std::uint32_t taddr = tmem + lane_base + buf * TCN + col_base + cb * 32;
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -989,83 +1009,147 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(&drained_bar[seg & 1]);
+            if (lane == 0) mbar_arrive(&drained_bar[buf]);
         };
+        // Item j of this thread: operand row `row` of A (which = 0) or of the
+        // column block (which = 1), environment columns 2q, 2q+1 of the chunk.
+        auto item_coords = [&](int j, int &which, int &row, int &q) {
+            const int item = tid + j * TC_PWARPS * 32;
+            which = item >= TCM * 8;
+            const int rem = which ? item - TCM * 8 : item;
+            const int rows = which ? TCC : TCM;
+            if (J.rows_fastest)
+            {
+                row = rem & (rows - 1);
+                q = which ? (rem >> 6) : (rem >> 7);
+            }
+            else
+            {
+                q = rem & 7;
+                row = rem >> 3;
+            }
+        };
+        // Raw amplitudes travel global -> shared with cp.async into a ring of
+        // TC_RING chunk slots; amplitude e of thread t sits at
+        // slot[(e * threads + t) * 8], and each thread converts only what it
+        // copied itself. The returned code holds 2 bits per amplitude:
+        // bit 0 = kept by the pending collapse, bit 1 = fermionic sign.
+        unsigned char *raw = smem + TC_STAGES * TC_STAGE;
+        const std::uint32_t raw_s0 = sm_addr(raw);
+        auto issue_chunk = [&](int chunk) -> std::uint32_t {
+            std::uint32_t code = 0;
+            if (chunk < nchunks)
+            {
+                const std::uint64_t e0 = static_cast<std::uint64_t>(chunk) << 4;
+                std::uint64_t ehi = 0;
+                for (int b = 4; b < nenv; ++b)
+                    if ((e0 >> b) & 1ull) ehi |= 1ull << J.env[b];
+                const std::uint32_t slot = raw_s0 + (chunk % TC_RING) * TC_RAW_BYTES;
+#pragma unroll
+                for (int j = 0; j < TC_ITEMS; ++j)
+                {
+                    int which, row, q;
+                    item_coords(j, which, row, q);
+                    const std::uint64_t ro = which ? roffB[row] : roffA[row];
+                    const std::uint64_t cx = which ? crossB[row] : crossA[row];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                    {
+                        const int el = 2 * j + h;
+                        const std::uint64_t addr = ehi | elo[2 * q + h] | ro;
+                        const bool keep = !has_col || (addr & cl.mask) == cl.value;
+                        const bool neg = (__popcll((e0 + 2 * q + h) & cx) & 1) != 0;
+                        if (keep)
+                            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(
+                                             slot + static_cast<std::uint32_t>((el * TC_PWARPS * 32 + tid) * 8)),
+                                         "l"(psi + addr)
+                                         : "memory");
+                        code |= (keep ? 1u : 0u) << (2 * el);
+                        code |= (neg ? 2u : 0u) << (2 * el);
+                    }
+                }
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            return code;
+        };
+        const float scale = has_col ? static_cast<float>(cl.scale) : 1.0f;
+        std::uint32_t code0 = issue_chunk(0);
+        std::uint32_t code1 = issue_chunk(1);
         for (int chunk = 0; chunk < nchunks; ++chunk)
         {
-            // Drain segment s once one chunk of segment s+1 is queued.
-            if (chunk >= (next_drain + 1) * TC_SEG + 1 && next_drain < nseg) drain(next_drain++);
-            const int st = chunk & 1;
-            if (chunk >= TC_STAGES && !mbar_wait(&empty_bar[st], ((chunk >> 1) - 1) & 1, &abort_flag, err)) break;
+            const std::uint32_t code2 = issue_chunk(chunk + 2);
+            asm volatile("cp.async.wait_group %0;" ::"n"(TC_RING - 1) : "memory");
+            const int st = chunk % TC_STAGES;
+            if (chunk >= TC_STAGES &&
+                !mbar_wait(&empty_bar[st], ((chunk / TC_STAGES) - 1) & 1, &abort_flag, err))
+                break;
             unsigned char *stage = smem + st * TC_STAGE;
             unsigned char *Ahi = stage, *Alo = stage + TC_A_BYTES;
             unsigned char *Bhi = stage + 2 * TC_A_BYTES, *Blo = Bhi + TC_B_BYTES;
-            const std::uint64_t e0 = static_cast<std::uint64_t>(chunk) << 4;
-            std::uint64_t ehi = 0;
-            for (int b = 4; b < nenv; ++b)
-                if ((e0 >> b) & 1ull) ehi |= 1ull << J.env[b];
-            for (int item = tid; item < 2 * TCM * 8; item += TC_PWARPS * 32)
+            const unsigned char *slot = raw + (chunk % TC_RING) * TC_RAW_BYTES;
+#pragma unroll
+            for (int j = 0; j < TC_ITEMS; ++j)
             {
-                const int which = item >= TCM * 8;
-                const int rem = item & (TCM * 8 - 1);
-                int row, q;
-                if (J.rows_fastest)
+                int which, row, q;
+                item_coords(j, which, row, q);
+                Cx<float> v[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
                 {
-                    row = rem & (TCM - 1);
-                    q = rem >> 7;
+                    const int el = 2 * j + h;
+                    const std::uint32_t cd = (code0 >> (2 * el)) & 3u;
+                    const float2 x = *reinterpret_cast<const float2 *>(slot + (el * TC_PWARPS * 32 + tid) * 8);
+                    const float f = (cd & 2u) ? -scale : scale;
+                    v[h].re = (cd & 1u) ? x.x * f : 0.0f;
+                    v[h].im = (cd & 1u) ? x.y * f : 0.0f;
                 }
-                else
-                {
-                    q = rem & 7;
-                    row = rem >> 3;
-                }
-                const std::uint64_t ro = which ? roffB[row] : roffA[row];
-                const std::uint64_t cx = which ? crossB[row] : crossA[row];
-                const std::uint64_t ea = e0 + 2 * q, eb = ea + 1;
-                const Cx<float> v0 =
-                    gather(psi, ehi | elo[2 * q] | ro, cl, has_col, (__popcll(ea & cx) & 1) != 0);
-                const Cx<float> v1 =
-                    gather(psi, ehi | elo[2 * q + 1] | ro, cl, has_col, (__popcll(eb & cx) & 1) != 0);
-                auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 v) {
+                auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 w) {
                     const int off = (rr >> 3) * 1024 + (rr & 7) * 128 + ((q ^ (rr & 7)) << 4);
                     float4 h, l;
-                    h.x = tf32_round(v.x);
-                    h.y = tf32_round(v.y);
-                    h.z = tf32_round(v.z);
-                    h.w = tf32_round(v.w);
-                    l.x = tf32_round(v.x - h.x);
-                    l.y = tf32_round(v.y - h.y);
-                    l.z = tf32_round(v.z - h.z);
-                    l.w = tf32_round(v.w - h.w);
+                    h.x = tf32_round(w.x);
+                    h.y = tf32_round(w.y);
+                    h.z = tf32_round(w.z);
+                    h.w = tf32_round(w.w);
+                    l.x = tf32_round(w.x - h.x);
+                    l.y = tf32_round(w.y - h.y);
+                    l.z = tf32_round(w.z - h.z);
+                    l.w = tf32_round(w.w - h.w);
                     *reinterpret_cast<float4 *>(hi_buf + off) = h;
                     *reinterpret_cast<float4 *>(lo_buf + off) = l;
                 };
                 if (!which)
                 {
-                    put(Ahi, Alo, row, make_float4(v0.re, v0.im, v1.re, v1.im));
+                    put(Ahi, Alo, row, make_float4(v[0].re, v[0].im, v[1].re, v[1].im));
                 }
                 else
                 {
-                    put(Bhi, Blo, row, make_float4(v0.re, v0.im, v1.re, v1.im));
-                    put(Bhi, Blo, TCM + row, make_float4(-v0.im, v0.re, -v1.im, v1.re));
+                    put(Bhi, Blo, row, make_float4(v[0].re, v[0].im, v[1].re, v[1].im));
+                    put(Bhi, Blo, TCC + row, make_float4(-v[0].im, v[0].re, -v[1].im, v[1].re));
                 }
             }
             // Make the generic-proxy stores visible to the tensor core.
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(&full_bar[st]);
+            // Drain segment s once the first chunk of segment s+TC_TMEM_BUFS-1
+            // is queued: by then its MMAs finished long ago.
+            if (chunk >= (next_drain + TC_TMEM_BUFS - 1) * TC_SEG && next_drain < nseg) drain(next_drain++);
+            code0 = code1;
+            code1 = code2;
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
         while (next_drain < nseg) drain(next_drain++);
 
-        // Weighted squares of this thread's row: warps 0-3 hold Re rho, 4-7 Im rho.
+        // Weighted squares of this thread's row: buffer columns below TCC
+        // hold Re rho, the rest Im rho, both for rho columns c0 + (col % TCC).
         const int r = r0 + (warp & 3) * 32 + lane;
         double sum = 0.0;
         if (!abort_flag)
         {
 #pragma unroll
-            for (int i = 0; i < 128; ++i)
+            for (int i = 0; i < TC_DCOLS; ++i)
             {
-                const int c = c0 + i;
+                const int c = c0 + ((col_base + i) & (TCC - 1));
                 const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
                 const double x = static_cast<double>(acc[i]);
                 sum += w * x * x;
@@ -1078,15 +1162,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     {
         for (int chunk = 0; chunk < nchunks; ++chunk)
         {
-            const int st = chunk & 1;
+            const int st = chunk % TC_STAGES;
             const int seg = chunk / TC_SEG;
-            const int buf = seg & 1;
-            if (chunk % TC_SEG == 0 && seg >= 2 &&
-                !mbar_wait(&drained_bar[buf], ((seg >> 1) - 1) & 1, &abort_flag, err))
+            const int buf = seg % TC_TMEM_BUFS;
+            if (chunk % TC_SEG == 0 && seg >= TC_TMEM_BUFS &&
+                !mbar_wait(&drained_bar[buf], ((seg / TC_TMEM_BUFS) - 1) & 1, &abort_flag, err))
                 break;
-            if (!mbar_wait(&full_bar[st], (chunk >> 1) & 1, &abort_flag, err)) break;
+            if (!mbar_wait(&full_bar[st], (chunk / TC_STAGES) & 1, &abort_flag, err)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const std::uint32_t dt = tmem + buf * 256;
+            const std::uint32_t dt = tmem + buf * TCN;
             const std::uint32_t base = sm_addr(smem + st * TC_STAGE);
             const std::uint32_t Ahi = base, Alo = base + TC_A_BYTES;
             const std::uint32_t Bhi = base + 2 * TC_A_BYTES, Blo = Bhi + TC_B_BYTES;
@@ -1125,12 +1209,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     {
         double t = 0.0;
         for (int w = 0; w < TC_PWARPS; ++w) t += red[w];
-        pur_out[static_cast<std::size_t>(job) * gridDim.x + blockIdx.x] = t;
+        pur_out[(static_cast<std::size_t>(job) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
     }
     if (warp == TC_PWARPS)
     {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TC_TMEM_COLS)
+                     : "memory");
     }
 }
 } // namespace
@@ -1144,11 +1229,16 @@ bool gram_tc_supported(int n, int k)
     return on && k >= 7 && k <= 16 && (n - k) >= 4;
 }
 
-int gram_tc_tiles(int k)
+// Lower-triangle 128-row blocks of rho.
+int gram_tc_blocks(int k)
 {
     const int t = 1 << (k - 7);
     return t * (t + 1) / 2;
 }
+
+// CTAs (and purity partials) per job: every block is split into two
+// 64-column halves.
+int gram_tc_tiles(int k) { return 2 * gram_tc_blocks(k); }
 
 std::size_t gram_tc_scratch_bytes(int k, int njobs)
 {
@@ -1166,7 +1256,7 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
     cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(TC_SMEM));
     if (e != cudaSuccess) return e;
-    dim3 grid(tiles, 1, njobs);
+    dim3 grid(gram_tc_blocks(k), 2, njobs);
     k_gram_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(states, n, d_jobs, collapse, collapse_stride,
                                                 static_cast<double *>(scratch), err);
     e = cudaGetLastError();
