@@ -218,10 +218,15 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 const int nb = static_cast<int>(list.size());
                 std::vector<GramJob> jobs(nb);
                 std::vector<int> idx(nb);
+                // Operands by TMA when every job keeps modes 0..k-1 in order.
+                bool low_cut = true;
+                int traj_count = 0;
                 for (int i = 0; i < nb; ++i)
                 {
                     jobs[i] = make_gram_job(list[i]->traj, n, list[i]->kept.data(), k, list[i]->fermion != 0);
                     idx[i] = list[i]->out;
+                    for (int b = 0; b < k; ++b) low_cut = low_cut && list[i]->kept[b] == b;
+                    traj_count = std::max(traj_count, list[i]->traj + 1);
                 }
                 MG_CUDA(ws.jobs.ensure(sizeof(GramJob) * nb));
                 MG_CUDA(ws.idx.ensure(sizeof(int) * nb));
@@ -235,7 +240,7 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
                 MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
                 MG_CUDA(gram_purity_tc(states, n, ws.jobs.as<GramJob>(), nb, k, col, col_stride, ws.vals.as<double>(),
-                                       ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s));
+                                       ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s, low_cut ? traj_count : 0));
                 launches += 2;
                 k_scatter<<<(nb + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nb, d_out, 1);
                 ++launches;

@@ -15,9 +15,13 @@
 //   three-site sweep signs              cpp/src/cuda/rho_reduce.cu:36-110
 #include "observables.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <stdexcept>
 
 namespace mg
@@ -856,11 +860,22 @@ __device__ __forceinline__ bool mbar_wait(std::uint64_t *bar, std::uint32_t pari
     return false;
 }
 
-__device__ __forceinline__ float tf32_round(float x)
+// Bounded wait that ignores the abort flag: used on the way out to let this
+// block's own bulk copies land before it exits.
+__device__ __forceinline__ void mbar_settle(std::uint64_t *bar, std::uint32_t parity)
 {
-    std::uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    for (long long i = 0; i < TC_SPIN; ++i)
+        if (mbar_try(bar, parity)) return;
+}
+
+// 3xTF32 split with integer ops: hi = x rounded to the nearest TF32 value
+// (ties away from zero: half a TF32 ulp added to the magnitude bits, the low
+// 13 mantissa bits cleared), lo = x - hi, exact in FP32 (|lo| <= 2^-11 |x|).
+// The tensor core reads lo with TF32 precision, an error <= 2^-22 |x|.
+__device__ __forceinline__ void tf32_split(float x, float &hi, float &lo)
+{
+    hi = __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xffffe000u);
+    lo = x - hi;
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
@@ -880,15 +895,20 @@ constexpr std::uint32_t kTcIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCN >>
 // in-TMEM sums drift (measured: linear in K); short segments bound it.
 constexpr int TC_SEG = 2;
 
+// kTma: every job keeps modes 0..k-1 in order, so the Schmidt matrix of
+// trajectory t is the plain [E][d] block of the state buffer; `tmap` views
+// the buffer as a 2-D array (d amplitudes per row, E * trajectories rows) and
+// the raw chunks arrive by TMA instead of per-amplitude cp.async gathers.
+template <bool kTma>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_gram_tc(const Cx<float> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
               const Collapse *__restrict__ col, std::size_t col_stride, double *__restrict__ pur_out,
-              int *__restrict__ err)
+              int *__restrict__ err, const __grid_constant__ CUtensorMap tmap)
 {
     extern __shared__ __align__(1024) unsigned char tc_raw[];
     __shared__ GramJob J;
     __shared__ __align__(8) std::uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], seg_bar[TC_TMEM_BUFS],
-        drained_bar[TC_TMEM_BUFS];
+        drained_bar[TC_TMEM_BUFS], raw_bar[TC_RING];
     __shared__ std::uint32_t tmem_base;
     __shared__ std::uint64_t roffA[TCM], roffB[TCC], crossA[TCM], crossB[TCC], elo[16];
     __shared__ double red[TC_PWARPS];
@@ -914,6 +934,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             mbar_init(&seg_bar[b], 1);
             mbar_init(&drained_bar[b], TC_PWARPS);
         }
+        for (int b = 0; b < TC_RING; ++b) mbar_init(&raw_bar[b], 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -1038,7 +1059,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const std::uint32_t raw_s0 = sm_addr(raw);
         auto issue_chunk = [&](int chunk) -> std::uint32_t {
             std::uint32_t code = 0;
-            if (chunk < nchunks)
+            if (!kTma && chunk < nchunks)
             {
                 const std::uint64_t e0 = static_cast<std::uint64_t>(chunk) << 4;
                 std::uint64_t ehi = 0;
@@ -1069,16 +1090,81 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                     }
                 }
             }
-            asm volatile("cp.async.commit_group;" ::: "memory");
+            if (!kTma) asm volatile("cp.async.commit_group;" ::: "memory");
             return code;
         };
+        // TMA mode: thread 0 loads chunk `chunk` into its ring slot as three
+        // 64-row boxes (A rows r0.., r0+64.., column-block rows c0..), each
+        // laid out [16 environment columns][64 rows]. The slot last held
+        // chunk - TC_RING, which every warp has converted once the full
+        // barrier of that chunk completed.
+        const int traj_row0 = J.traj << nenv;
+        int tma_issued = 0; // chunks thread 0 has issued (TMA mode)
+        auto issue_tma = [&](int chunk) {
+            if (!kTma || tid != 0 || chunk >= nchunks) return;
+            if (chunk >= TC_RING && !mbar_wait(&full_bar[(chunk - TC_RING) % TC_STAGES],
+                                               ((chunk - TC_RING) / TC_STAGES) & 1, &abort_flag, err))
+                return;
+            const int slot = chunk % TC_RING;
+            const std::uint32_t bar = sm_addr(&raw_bar[slot]);
+            const std::uint32_t dst = raw_s0 + slot * TC_RAW_BYTES;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TC_RAW_BYTES)
+                         : "memory");
+            const int y = traj_row0 + (chunk << 4);
+            const int xs[3] = {r0, r0 + 64, c0};
+#pragma unroll
+            for (int b = 0; b < 3; ++b)
+                asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                             "%3}], [%4];" ::"r"(dst + b * 8192),
+                             "l"(reinterpret_cast<std::uint64_t>(&tmap)), "r"(xs[b]), "r"(y), "r"(bar)
+                             : "memory");
+            tma_issued = chunk + 1;
+        };
+        // TMA mode keep flags of the pending collapse: per row (fixed per
+        // thread) and per environment column (one ballot per chunk).
+        std::uint32_t row_keep = 0;
+        const std::uint64_t low_mask = (1ull << k) - 1ull;
+        if (kTma)
+            for (int j = 0; j < TC_ITEMS; ++j)
+            {
+                int which, row, q;
+                item_coords(j, which, row, q);
+                const std::uint64_t r = static_cast<std::uint64_t>(which ? c0 + row : r0 + row);
+                if (!has_col || (r & cl.mask) == (cl.value & low_mask)) row_keep |= 1u << j;
+            }
         const float scale = has_col ? static_cast<float>(cl.scale) : 1.0f;
         std::uint32_t code0 = issue_chunk(0);
         std::uint32_t code1 = issue_chunk(1);
+        issue_tma(0);
+        issue_tma(1);
+        int converted = 0;
         for (int chunk = 0; chunk < nchunks; ++chunk)
         {
             const std::uint32_t code2 = issue_chunk(chunk + 2);
-            asm volatile("cp.async.wait_group %0;" ::"n"(TC_RING - 1) : "memory");
+            if constexpr (kTma)
+            {
+                if (!mbar_wait(&raw_bar[chunk % TC_RING], (chunk / TC_RING) & 1, &abort_flag, err)) break;
+                std::uint32_t env_keep = 0xffffu;
+                if (has_col)
+                {
+                    const std::uint64_t e = (static_cast<std::uint64_t>(chunk) << 4) + (lane & 15);
+                    env_keep = __ballot_sync(0xffffffffu, ((e << k) & cl.mask) == (cl.value & ~low_mask)) & 0xffffu;
+                }
+                code0 = 0;
+#pragma unroll
+                for (int j = 0; j < TC_ITEMS; ++j)
+                {
+                    int which, row, q;
+                    item_coords(j, which, row, q);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if (((row_keep >> j) & 1u) && ((env_keep >> (2 * q + h)) & 1u)) code0 |= 1u << (2 * (2 * j + h));
+                }
+            }
+            else
+            {
+                asm volatile("cp.async.wait_group %0;" ::"n"(TC_RING - 1) : "memory");
+            }
             const int st = chunk % TC_STAGES;
             if (chunk >= TC_STAGES &&
                 !mbar_wait(&empty_bar[st], ((chunk / TC_STAGES) - 1) & 1, &abort_flag, err))
@@ -1098,33 +1184,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 {
                     const int el = 2 * j + h;
                     const std::uint32_t cd = (code0 >> (2 * el)) & 3u;
-                    const float2 x = *reinterpret_cast<const float2 *>(slot + (el * TC_PWARPS * 32 + tid) * 8);
+                    const int raw_off = !kTma ? (el * TC_PWARPS * 32 + tid) * 8
+                                        : which ? 2 * 8192 + ((2 * q + h) * 64 + row) * 8
+                                                : (row >> 6) * 8192 + ((2 * q + h) * 64 + (row & 63)) * 8;
+                    const float2 x = *reinterpret_cast<const float2 *>(slot + raw_off);
                     const float f = (cd & 2u) ? -scale : scale;
                     v[h].re = (cd & 1u) ? x.x * f : 0.0f;
                     v[h].im = (cd & 1u) ? x.y * f : 0.0f;
                 }
-                auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 w) {
+                // X row (re, im, re, im) and, for the column block, the Y row
+                // (-im, re, -im, re): the split commutes with negation and
+                // permutation, so Y reuses X's hi/lo.
+                float4 h, l;
+                tf32_split(v[0].re, h.x, l.x);
+                tf32_split(v[0].im, h.y, l.y);
+                tf32_split(v[1].re, h.z, l.z);
+                tf32_split(v[1].im, h.w, l.w);
+                auto put = [&](unsigned char *hi_buf, unsigned char *lo_buf, int rr, float4 hv, float4 lv) {
                     const int off = (rr >> 3) * 1024 + (rr & 7) * 128 + ((q ^ (rr & 7)) << 4);
-                    float4 h, l;
-                    h.x = tf32_round(w.x);
-                    h.y = tf32_round(w.y);
-                    h.z = tf32_round(w.z);
-                    h.w = tf32_round(w.w);
-                    l.x = tf32_round(w.x - h.x);
-                    l.y = tf32_round(w.y - h.y);
-                    l.z = tf32_round(w.z - h.z);
-                    l.w = tf32_round(w.w - h.w);
-                    *reinterpret_cast<float4 *>(hi_buf + off) = h;
-                    *reinterpret_cast<float4 *>(lo_buf + off) = l;
+                    *reinterpret_cast<float4 *>(hi_buf + off) = hv;
+                    *reinterpret_cast<float4 *>(lo_buf + off) = lv;
                 };
                 if (!which)
                 {
-                    put(Ahi, Alo, row, make_float4(v[0].re, v[0].im, v[1].re, v[1].im));
+                    put(Ahi, Alo, row, h, l);
                 }
                 else
                 {
-                    put(Bhi, Blo, row, make_float4(v[0].re, v[0].im, v[1].re, v[1].im));
-                    put(Bhi, Blo, TCC + row, make_float4(-v[0].im, v[0].re, -v[1].im, v[1].re));
+                    put(Bhi, Blo, row, h, l);
+                    put(Bhi, Blo, TCC + row, make_float4(-h.y, h.x, -h.w, h.z), make_float4(-l.y, l.x, -l.w, l.z));
                 }
             }
             // Make the generic-proxy stores visible to the tensor core.
@@ -1134,10 +1222,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // Drain segment s once the first chunk of segment s+TC_TMEM_BUFS-1
             // is queued: by then its MMAs finished long ago.
             if (chunk >= (next_drain + TC_TMEM_BUFS - 1) * TC_SEG && next_drain < nseg) drain(next_drain++);
+            issue_tma(chunk + 2);
+            converted = chunk + 1;
             code0 = code1;
             code1 = code2;
         }
-        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (!kTma) asm volatile("cp.async.wait_all;" ::: "memory");
+        // After an abort, let the chunks thread 0 issued but nobody consumed land.
+        for (int c = converted; c < tma_issued; ++c) mbar_settle(&raw_bar[c % TC_RING], (c / TC_RING) & 1);
         while (next_drain < nseg) drain(next_drain++);
 
         // Weighted squares of this thread's row: buffer columns below TCC
@@ -1245,20 +1337,54 @@ std::size_t gram_tc_scratch_bytes(int k, int njobs)
     return sizeof(double) * static_cast<std::size_t>(gram_tc_tiles(k)) * njobs;
 }
 
+namespace
+{
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+} // namespace
+
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
-                           std::size_t scratch_bytes, int *err, cudaStream_t s)
+                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count)
 {
     if (njobs <= 0) return cudaSuccess;
     if (!gram_tc_supported(n, k)) return cudaErrorInvalidValue;
     const int tiles = gram_tc_tiles(k);
     if (gram_tc_scratch_bytes(k, njobs) > scratch_bytes) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CUtensorMap map;
+    std::memset(&map, 0, sizeof(map));
+    const std::uint64_t rows = static_cast<std::uint64_t>(tma_traj_count) << (n - k);
+    bool tma = tma_traj_count > 0 && rows < (1ull << 31) && tensor_map_encoder() != nullptr &&
+               (reinterpret_cast<std::uintptr_t>(states) & 15u) == 0;
+    if (tma)
+    {
+        const cuuint64_t dims[2] = {1ull << k, rows};
+        const cuuint64_t strides[1] = {(1ull << k) * sizeof(Cx<float>)};
+        const cuuint32_t box[2] = {64, 16};
+        const cuuint32_t estr[2] = {1, 1};
+        tma = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<Cx<float> *>(states), dims,
+                                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    }
+    auto kernel = tma ? k_gram_tc<true> : k_gram_tc<false>;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(TC_SMEM));
     if (e != cudaSuccess) return e;
     dim3 grid(gram_tc_blocks(k), 2, njobs);
-    k_gram_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(states, n, d_jobs, collapse, collapse_stride,
-                                                static_cast<double *>(scratch), err);
+    kernel<<<grid, TC_THREADS, TC_SMEM, s>>>(states, n, d_jobs, collapse, collapse_stride,
+                                             static_cast<double *>(scratch), err, map);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);

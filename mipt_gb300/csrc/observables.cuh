@@ -62,12 +62,14 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
 
 // Purity through the tensor-core (tcgen05, 3xTF32) Gram, FP32 states only;
 // needs 7 <= k <= 16 and n - k >= 4. err receives bit 4 if a pipeline wait
-// timed out (the kernel then returns without a result).
+// timed out (the kernel then returns without a result). tma_traj_count > 0
+// asserts that every job keeps modes 0..k-1 in order and that `states` holds
+// tma_traj_count state vectors; the operands then arrive by TMA.
 bool gram_tc_supported(int n, int k);
 std::size_t gram_tc_scratch_bytes(int k, int njobs);
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
-                           std::size_t scratch_bytes, int *err, cudaStream_t s);
+                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count = 0);
 
 // Purity of full matrices rho[job][d][d].
 cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, cudaStream_t s);

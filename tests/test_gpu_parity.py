@@ -251,10 +251,13 @@ def test_full_size_chain_L24(mg, orc):
 
 @pytest.mark.parametrize("n,kept,ferm", [(14, list(range(7)), False), (16, list(range(8)), False),
                                          (18, [17, 3, 9, 0, 12, 5, 8, 1, 14], True), (20, list(range(10, 20)), False),
-                                         (16, [15, 14, 13, 12, 11, 10, 9, 8], True)])
+                                         (16, [15, 14, 13, 12, 11, 10, 9, 8], True), (18, list(range(9)), True),
+                                         (12, list(range(8)), False), (20, list(range(12)), False),
+                                         (17, [1, 0, 2, 3, 4, 5, 6, 7], False)])
 def test_tensor_core_renyi2(mg, orc, n, kept, ferm):
     """FP32 Renyi-2 through the tcgen05 3xTF32 Gram (cuts with >= 128 rows)
-    against the FP64 oracle's RDM purity."""
+    against the FP64 oracle's RDM purity. Cuts keeping modes 0..k-1 in order
+    take the TMA operand path, the others the gathered one."""
     psi = random_state(n, 77 + n)
     e = device_state(mg, psi, False)
     got = mg.renyi2(e.data, n, kept, ferm, False)
