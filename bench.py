@@ -31,6 +31,7 @@ METRIC = "trajectory-layers/s at L=24 (batched FP32 vs plain FP64) at |dS|<=1e-5
 UNIT = "trajectory-layers/s"
 N_QUBITS = 24
 PERIODS = 24
+PASS_TRAFFIC_PER_TRAJ = 237.9e6  # DRAM bytes per trajectory per pass launch (ncu)
 P_GRID = np.linspace(0.05, 0.35, 16)
 
 
@@ -238,12 +239,24 @@ def run_gb300(args):
         passes_per_layer = pass_n / T
         achieved = alg_bytes_step / (pass_ms / 1000.0) / 1e9
         peak, peak_kind = measured_peak_hbm()
+        # DRAM traffic per pass launch: ncu measured 237.9 MB per trajectory
+        # (read 134.3 MB + write 103.7 MB, the rest of the writes still in L2)
+        # on 2 trajectories; each launch streams every state once, so it
+        # scales with the batch (profiles/k_pass_rounds_L24_batch2.md).
+        traffic = PASS_TRAFFIC_PER_TRAJ * B
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": None, "peak_source": peak_kind,
+                    "traffic": traffic, "traffic_source": "ncu dram bytes, 2-trajectory capture scaled to B",
+                    "peak_source": peak_kind,
                     "kernel": "k_pass (tiled brickwork layer pass)",
                     "alg_bytes_per_launch": alg_bytes_step / pass_n, "launch_ms": pass_ms / pass_n,
                     "passes_per_layer": passes_per_layer,
                     "kernel_ms_per_step": {k: v[0] for k, v in stats.items()}}
+        # Final half-chain S_2: tensor-core Gram, 4 d_A^2 d_B real flops per
+        # trajectory for the Hermitian half (d_A = d_B = 2^12).
+        obs_ms = stats["observables"][0]
+        gram_flops = B * 4.0 * float(1 << (N_QUBITS // 2)) ** 3
+        gram = {"kernel": "k_gram_tc (tcgen05 3xTF32)", "ms_per_step": obs_ms,
+                "alg_tflops": gram_flops / (obs_ms / 1000.0) / 1e12 if obs_ms > 0 else None}
 
         # Plain FP64 per-trajectory path on the same GPU, one trajectory.
         plain = mg.Batch(N_QUBITS, PERIODS, capacity=1, fp64=True, observables=mg.OBS_S2_HALF)
@@ -262,7 +275,7 @@ def run_gb300(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(B), "roofline": roofline, "cpu_baseline": cpu,
+            "config": workload_config(B), "roofline": roofline, "gram": gram, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clocks.summary(),
             "plain_fp64": {"value": plain_value, "unit": UNIT, "path": "FP64 state, one trajectory per launch sequence",
