@@ -151,6 +151,8 @@ typedef struct mipt_gb300_batch_config
     int fermion_trace; /* trace convention for RDMs / rho3 */
     int host_threads;  /* host sampler threads, 0 = all */
     int tile_qubits;   /* local qubits per pass tile, 0 = default */
+    int tmi_cycles;    /* TMI quarters at cyclic offsets 0..tmi_cycles-1 (0 or 1: offset 0 only;
+                          at most n/4) -- cpp/include/mipt/tmi/compute.hpp:89-113 */
 } mipt_gb300_batch_config;
 
 typedef struct mipt_gb300_batch mipt_gb300_batch;
@@ -177,6 +179,11 @@ int mipt_gb300_batch_execute(mipt_gb300_batch *batch, void *stream);
 int mipt_gb300_batch_fetch(mipt_gb300_batch *batch, uint64_t *measured, uint64_t *outcomes, double *surprisal,
                            double *obs, double *rho3);
 /* prepare + execute + fetch in one synchronous call. */
+/* TMI at every cyclic offset, after mipt_gb300_batch_execute:
+ * tmi[count][points][tmi_cycles] (order 1: von Neumann, 2: Renyi-2; the
+ * batch must have been created with the matching MIPT_GB300_OBS_TMI_* flag).
+ * Offset c uses A = [c, c+n/4), B, C, D the following quarters (mod n). */
+int mipt_gb300_batch_fetch_tmi(mipt_gb300_batch *batch, int order, double *tmi);
 int mipt_gb300_batch_run_haar(mipt_gb300_batch *batch, const uint64_t *seeds, const double *p, int count,
                               const uint64_t *forced_outcomes, uint64_t *measured, uint64_t *outcomes,
                               double *surprisal, double *obs, double *rho3);

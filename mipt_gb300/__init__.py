@@ -38,7 +38,7 @@ class FFConfig(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in (
         "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
-        "fermion_trace", "host_threads", "tile_qubits")]
+        "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles")]
 
 
 def lib():
@@ -79,6 +79,7 @@ def lib():
     L.mipt_gb300_batch_prepare_haar.argtypes = [vp, vp, vp, ci, vp]
     L.mipt_gb300_batch_execute.argtypes = [vp, vp]
     L.mipt_gb300_batch_fetch.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_batch_fetch_tmi.argtypes = [vp, ci, vp]
     L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
     L.mipt_gb300_batch_state.restype = vp
@@ -244,9 +245,10 @@ class Batch:
     """Many Haar trajectories of one chain length, run as one device schedule."""
 
     def __init__(self, n, periods, capacity, closed=True, fp64=False, chunk_bits=16, observables=0,
-                 observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0):
+                 observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0, tmi_cycles=0):
         cfg = BatchConfig(n, periods, int(closed), int(fp64), chunk_bits, observables, observe_every, int(rho3),
-                          int(fermion_trace), host_threads, tile_qubits)
+                          int(fermion_trace), host_threads, tile_qubits, tmi_cycles)
+        self.tmi_cycles = max(1, tmi_cycles)
         h = ctypes.c_void_p()
         _check(lib().mipt_gb300_batch_create(ctypes.byref(cfg), capacity, ctypes.byref(h)))
         self._h = h
@@ -286,6 +288,12 @@ class Batch:
         rho3 = np.zeros((c, self.n, 128)) if self.rho3 else None
         _check(lib().mipt_gb300_batch_fetch(self._h, _p(measured), _p(outcomes), _p(surprisal), _p(obs), _p(rho3)))
         return dict(measured=measured, outcomes=outcomes, surprisal=surprisal, obs=obs, rho3=rho3)
+
+    def fetch_tmi(self, order=1):
+        """TMI at every cyclic offset: [count][points][tmi_cycles]."""
+        out = np.zeros((self.count, self.points, self.tmi_cycles))
+        _check(lib().mipt_gb300_batch_fetch_tmi(self._h, int(order), _p(out)))
+        return out
 
     def run(self, seeds, p, forced=None):
         self.prepare(seeds, p, forced)

@@ -17,6 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libmipt_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
+APPS = os.path.join(HERE, "apps")
+APP_TARGETS = [("mipt.cpp", "mipt.exe"), ("sim_tmi.cpp", "sim_tmi.exe")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu"]
@@ -81,7 +83,26 @@ def build(force=False, verbose=False, ptxas_info=False):
         cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcusolver", "-lpthread"]
         _compile(cmd)
         os.replace(tmp, LIB)
+    build_apps(force)
     return LIB
+
+
+def build_apps(force=False):
+    """The drop-in executables (mipt.exe, sim_tmi.exe): host C++ over the C ABI,
+    linked against the library next to them."""
+    headers = [os.path.join(APPS, f) for f in os.listdir(APPS) if f.endswith(".hpp")]
+    headers.append(os.path.join(INCLUDE, "mipt_gb300.h"))
+    jobs = []
+    for src_name, exe_name in APP_TARGETS:
+        src = os.path.join(APPS, src_name)
+        exe = os.path.join(OUT, exe_name)
+        if force or _stale(src, exe, headers + [LIB]):
+            jobs.append(["g++", "-std=c++17", "-O2", "-I", INCLUDE, src, "-o", exe, "-L", OUT, "-lmipt_gb300",
+                         "-Wl,-rpath,$ORIGIN"])
+    if jobs:
+        with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+            list(ex.map(_compile, jobs))
+    return [os.path.join(OUT, e) for _, e in APP_TARGETS]
 
 
 if __name__ == "__main__":

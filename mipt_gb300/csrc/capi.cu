@@ -577,7 +577,8 @@ struct mipt_gb300_batch
     int reqs_per_point = 0;
     std::vector<EntReq> reqs; // for one point, trajectory index filled per launch
     int col_half_vn = -1, col_half_s2 = -1;
-    std::vector<int> tmi_vn, tmi_s2; // 7 request slots each (A,B,C,D,AB,AC,BC)
+    std::vector<int> tmi_vn, tmi_s2; // 7 request slots (A,B,C,D,AB,AC,BC) per cyclic offset
+    int tmi_cycles = 0;
     Workspace ws;
     long long launches = 0;
     bool executed = false;
@@ -1002,18 +1003,27 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
         b->col_half_s2 = static_cast<int>(b->reqs.size());
         b->reqs.push_back(EntReq{0, 2, ft, range(0, n / 2), 0});
     }
+    if (cfg->observables & (MIPT_GB300_OBS_TMI_VN | MIPT_GB300_OBS_TMI_S2))
+    {
+        if (cfg->tmi_cycles < 0 || cfg->tmi_cycles > n / 4)
+            return fail(MIPT_GB300_E_INVALID, "tmi_cycles must be 0..n/4");
+        b->tmi_cycles = std::max(1, cfg->tmi_cycles);
+    }
     for (int order = 1; order <= 2; ++order)
     {
         const int flag = order == 1 ? MIPT_GB300_OBS_TMI_VN : MIPT_GB300_OBS_TMI_S2;
         if (!(cfg->observables & flag)) continue;
         const int q = n / 4;
-        const auto A = range(0, q), B = range(q, q), C = range(2 * q, q), D = range(3 * q, q);
-        const std::vector<std::vector<int>> sets = {A, B, C, D, cat(A, B), cat(A, C), cat(B, C)};
         auto &slots = order == 1 ? b->tmi_vn : b->tmi_s2;
-        for (const auto &s : sets)
+        for (int c = 0; c < b->tmi_cycles; ++c)
         {
-            slots.push_back(static_cast<int>(b->reqs.size()));
-            b->reqs.push_back(EntReq{0, order, ft, s, 0});
+            const auto A = range(c, q), B = range(c + q, q), C = range(c + 2 * q, q), D = range(c + 3 * q, q);
+            const std::vector<std::vector<int>> sets = {A, B, C, D, cat(A, B), cat(A, C), cat(B, C)};
+            for (const auto &s : sets)
+            {
+                slots.push_back(static_cast<int>(b->reqs.size()));
+                b->reqs.push_back(EntReq{0, order, ft, s, 0});
+            }
         }
     }
     b->reqs_per_point = static_cast<int>(b->reqs.size());
@@ -1346,6 +1356,30 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
         if (!b->cfg.rho3) return fail(MIPT_GB300_E_INVALID, "batch was created without rho3");
         MG_CUDA(cudaMemcpy(rho3, b->rho3.p, sizeof(double) * 128 * n * count, cudaMemcpyDeviceToHost));
     }
+    return 0;
+}
+
+int mipt_gb300_batch_fetch_tmi(mipt_gb300_batch *b, int order, double *tmi)
+{
+    if (!b || !b->executed || !tmi) return fail(MIPT_GB300_E_INVALID, "batch not executed or null output");
+    if (order != 1 && order != 2) return fail(MIPT_GB300_E_INVALID, "order must be 1 or 2");
+    const std::vector<int> &slots = order == 1 ? b->tmi_vn : b->tmi_s2;
+    if (slots.empty()) return fail(MIPT_GB300_E_INVALID, "batch was created without this TMI order");
+    MG_CUDA(cudaDeviceSynchronize());
+    const std::size_t P = b->points, R = b->reqs_per_point, Cy = b->tmi_cycles;
+    std::vector<double> ent(static_cast<std::size_t>(b->count) * P * R);
+    MG_CUDA(cudaMemcpy(ent.data(), b->ent.p, sizeof(double) * ent.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < b->count; ++i)
+        for (std::size_t pt = 0; pt < P; ++pt)
+        {
+            const double *e = ent.data() + (static_cast<std::size_t>(i) * P + pt) * R;
+            for (std::size_t c = 0; c < Cy; ++c)
+            {
+                const int *s = slots.data() + 7 * c;
+                tmi[(static_cast<std::size_t>(i) * P + pt) * Cy + c] =
+                    e[s[0]] + e[s[1]] + e[s[2]] + e[s[3]] - e[s[4]] - e[s[5]] - e[s[6]];
+            }
+        }
     return 0;
 }
 

@@ -1,0 +1,127 @@
+"""The drop-in executables (mipt.exe, sim_tmi.exe) on the host: argument
+handling, exit codes and messages of the reference apps
+(cpp/apps/mipt.cpp:312-414, cpp/apps/sim_tmi.cpp), the rho3.bin / info.csv
+formats (cpp/include/mipt/density.hpp, cpp/apps/mipt.cpp:91-97) and the
+sim_tmi resume contract (cpp/include/mipt/tmi/resume.hpp). Nothing here
+needs a GPU: every case ends before device work (or runs none)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from mipt_gb300 import build, rho3file
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def exes():
+    build.build()
+    out = os.path.join(ROOT, "mipt_gb300", "_build")
+    return os.path.join(out, "mipt.exe"), os.path.join(out, "sim_tmi.exe")
+
+
+def run(args, cwd, env=None):
+    e = dict(os.environ)
+    e.pop("CUDA_VISIBLE_DEVICES", None)
+    e.update(env or {})
+    return subprocess.run(args, cwd=cwd, capture_output=True, text=True, env=e, timeout=120)
+
+
+def test_mipt_usage_and_argument_errors(exes, tmp_path):
+    mipt, _ = exes
+    r = run([mipt, "--help"], tmp_path)
+    assert r.returncode == 0 and "Usage:" in r.stdout and "circ_type" in r.stdout
+    r = run([mipt] + ["1"] * 9, tmp_path)
+    assert r.returncode == 2 and "Too many arguments" in r.stderr
+    r = run([mipt, "3"], tmp_path)
+    assert r.returncode == 1 and "mipt.exe error: d must be 1 or 2." in r.stderr
+    r = run([mipt, "1", "10", "2", "1", "1", "0.5", "0.2", "1"], tmp_path)
+    assert r.returncode == 1 and "Require 0 <= p_min <= p_max <= 1." in r.stderr
+    r = run([mipt, "1", "9", "2", "1", "1", "0.1", "0.2", "1"], tmp_path)
+    assert r.returncode == 1 and "Random Haar Unitary requires an even n" in r.stderr
+    r = run([mipt, "1", "10", "2", "1", "1", "0.1", "0.2", "7"], tmp_path)
+    assert r.returncode == 1 and "circ_type must be one of" in r.stderr
+    r = run([mipt, "1", "10", "2", "1", "1", "0.1", "0.2", "0"], tmp_path)
+    assert r.returncode == 1 and "not on the GB300 trajectory path" in r.stderr
+
+
+def test_rho3_bin_and_info_csv_round_trip(exes, tmp_path):
+    """periods = 0 needs no device: every record is |000><000| per triple."""
+    mipt, _ = exes
+    n, R, res = 6, 3, 2
+    r = run([mipt, "1", str(n), "0", str(R), str(res), "0.1", "0.3", "1"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    info = (tmp_path / "info.csv").read_text().splitlines()
+    assert info[0] == "n,periods,realizations,resolution,p_min,p_max,circ_type,circuit_name,fermion_trace,cudaq_backend"
+    assert info[1].startswith("6,0,3,2,0.1,0.3,1,Random Haar Unitary,0,gb300-")
+    meta, rec = rho3file.read(tmp_path / "rho3.bin")
+    assert (meta["spatial_dimension"], meta["total_qubits"], meta["kept_qubits"], meta["matrix_dimension"]) == (1, 6, 3, 8)
+    assert (meta["periods"], meta["realizations"], meta["resolution"], meta["grid_x"], meta["grid_y"]) == (0, 3, 2, 6, 1)
+    assert meta["subsystem_count"] == n and meta["record_count"] == R * res
+    assert (meta["p_min"], meta["p_max"]) == (0.1, 0.3)
+    np.testing.assert_array_equal(meta["subsystem_qubits"], [[s, (s + 1) % n, (s + 2) % n] for s in range(n)])
+    np.testing.assert_array_equal(rec["p_index"], np.repeat(np.arange(res), R))
+    np.testing.assert_array_equal(rec["realization"], np.tile(np.arange(R), res))
+    np.testing.assert_array_equal(rec["p"], np.repeat([0.1, 0.3], R))
+    want = np.zeros((8, 8), complex)
+    want[0, 0] = 1
+    assert np.all(rec["rho"] == want)
+
+
+def test_sim_tmi_usage_and_argument_errors(exes, tmp_path):
+    _, tmi = exes
+    r = run([tmi, "--help"], tmp_path)
+    assert r.returncode == 0 and "p,tmi" in r.stderr
+    r = run([tmi] + ["1"] * 10, tmp_path)
+    assert r.returncode == 2
+    r = run([tmi, "10", "2", "2", "2", "0.1", "0.3", "1"], tmp_path)
+    assert r.returncode == 1 and "n >= 4 and n divisible by 4" in r.stderr
+    r = run([tmi, "12", "2", "2", "2", "0.1", "0.3", "1", "out.csv", "2"], tmp_path)
+    assert r.returncode == 1 and "all_cycles must be 0 or 1" in r.stderr
+    r = run([tmi, "12", "2", "2", "2", "0.1", "0.3", "1"], tmp_path, {"SIM_TMI_ENTROPY_ORDER": "3"})
+    assert r.returncode == 1 and "SIM_TMI_ENTROPY_ORDER must be 1" in r.stderr
+
+
+def default_path(tmp_path, tag, n, R, pmin, pmax, res):
+    return tmp_path / "csv" / "tmi" / tag / f"tmi_{tag}_n_{n}_real_{R}_{pmin}_{pmax}_res_{res}.csv"
+
+
+def test_sim_tmi_complete_file_is_left_alone(exes, tmp_path):
+    _, tmi = exes
+    path = default_path(tmp_path, "haarc", 8, 2, "0.1", "0.3", 2)
+    path.parent.mkdir(parents=True)
+    rows = ["p,tmi"] + [f"{p},-0.5" for p in ("0.10000000000000001", "0.29999999999999999") for _ in range(2 * 2)]
+    path.write_text("\n".join(rows) + "\n")
+    r = run([tmi, "8", "2", "2", "2", "0.1", "0.3", "1", "1"], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "already holds all 8 TMI row(s)" in r.stderr
+
+
+def test_sim_tmi_resume_trims_partial_circuit(exes, tmp_path):
+    """A partially written circuit (1 of 2 cycle rows) is cut off before the
+    run continues (without a GPU the run then stops at device creation; with
+    one it appends the remaining circuits after the kept rows)."""
+    _, tmi = exes
+    path = default_path(tmp_path, "haarc", 8, 2, "0.1", "0.3", 2)
+    path.parent.mkdir(parents=True)
+    keep = "p,tmi\n" + "0.10000000000000001,-0.25\n" * 2
+    path.write_text(keep + "0.10000000000000001,-0.125\n0.1000")
+    r = run([tmi, "8", "2", "2", "2", "0.1", "0.3", "1", "1"], tmp_path)
+    assert "RESUMED from" in r.stderr and "dropped 1 row(s)" in r.stderr, r.stderr
+    text = path.read_text()
+    assert text.startswith(keep) and "-0.125" not in text
+
+
+def test_sim_tmi_refuses_foreign_checkpoint(exes, tmp_path):
+    _, tmi = exes
+    path = default_path(tmp_path, "haar", 8, 2, "0.1", "0.3", 2)
+    path.parent.mkdir(parents=True)
+    path.write_text("p,tmi\n0.2,-1\n")
+    r = run([tmi, "8", "2", "2", "2", "0.1", "0.3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "switches away from p=0.10000000000000001 after 0 rows" in r.stderr
+    other = tmp_path / "csv" / "tmi" / "haar" / "tmi_haar_n_12_real_2_0.1_0.3_res_2.csv"
+    other.write_text("p,tmi\n")
+    r = run([tmi, "8", "2", "2", "2", "0.1", "0.3", "1", "0", str(other)], tmp_path)
+    assert r.returncode == 1 and "n=12 (this run uses 8)" in r.stderr
