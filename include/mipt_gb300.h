@@ -90,6 +90,62 @@ int mipt_cuda_rho3_subsystems_complex_both_f32(const void *device_state_vector, 
                                                const int *host_subsystems, int subsystem_count,
                                                double *host_rho_ri_row_major, double *host_fermion_rho_ri_row_major);
 
+/* Host-resident state vectors: copied to a reusable device buffer of the
+ * calling thread, then the same reduction.
+ * Replaces cpp/include/mipt/cuda/rho_reduce.hpp:78-126. */
+int mipt_cuda_rho3_subsystems_complex_host_f64(const void *host_state_vector, int n_qubits,
+                                               const int *host_subsystems, int subsystem_count,
+                                               double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_host_f32(const void *host_state_vector, int n_qubits,
+                                               const int *host_subsystems, int subsystem_count,
+                                               double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_host_fermion_f64(const void *host_state_vector, int n_qubits,
+                                                       const int *host_subsystems, int subsystem_count,
+                                                       double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_host_fermion_f32(const void *host_state_vector, int n_qubits,
+                                                       const int *host_subsystems, int subsystem_count,
+                                                       double *host_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_host_both_f64(const void *host_state_vector, int n_qubits,
+                                                    const int *host_subsystems, int subsystem_count,
+                                                    double *host_rho_ri_row_major,
+                                                    double *host_fermion_rho_ri_row_major);
+int mipt_cuda_rho3_subsystems_complex_host_both_f32(const void *host_state_vector, int n_qubits,
+                                                    const int *host_subsystems, int subsystem_count,
+                                                    double *host_rho_ri_row_major,
+                                                    double *host_fermion_rho_ri_row_major);
+
+/* --------------------------------------------- diagonal and parity passes */
+
+/* Periodic-boundary Jordan-Wigner chain as one diagonal pass: amplitude *= -1
+ * where bit control_qubit is set and popcount(index & string_mask) is odd.
+ * Invalid arguments return -1. Asynchronous on the default stream.
+ * Replaces cpp/include/mipt/cuda/cusv_diag.hpp:10-20. */
+int mipt_cuda_jw_string_f32(void *device_state_vector, int n_qubits, int control_qubit, uint64_t string_mask);
+int mipt_cuda_jw_string_f64(void *device_state_vector, int n_qubits, int control_qubit, uint64_t string_mask);
+const char *mipt_cuda_cusv_diag_last_error(void);
+
+/* Parity-sector encoding: an encoded index e (encoded_qubits = n-1 bits)
+ * stands for the even-parity basis state whose bit n-1 is parity(e).
+ * gate: 2x2 on bit `target` of every pair, `even_ri` where parity(e with the
+ * target bit cleared) is 0, `odd_ri` where it is 1 (8 doubles each: row-major
+ * (re, im) M00 M01 M10 M11). abs2: {even, odd} weights, fixed-order sums
+ * (synchronous). collapse: keep parity(e) == outcome, scale 1/sqrt(weight).
+ * expand: the encoded state in the low half of a 2^full_qubits buffer becomes
+ * the full state in place. Invalid arguments return -1; other calls are
+ * asynchronous on the default stream.
+ * Replaces cpp/include/mipt/cuda/cusv_parity.hpp:23-60. */
+int mipt_cuda_parity_gate_f32(void *device_state_vector, int encoded_qubits, int target, const double *even_ri,
+                              const double *odd_ri);
+int mipt_cuda_parity_gate_f64(void *device_state_vector, int encoded_qubits, int target, const double *even_ri,
+                              const double *odd_ri);
+int mipt_cuda_parity_abs2_f32(const void *device_state_vector, int encoded_qubits, double *host_weights);
+int mipt_cuda_parity_abs2_f64(const void *device_state_vector, int encoded_qubits, double *host_weights);
+int mipt_cuda_parity_collapse_f32(void *device_state_vector, int encoded_qubits, int outcome, double weight);
+int mipt_cuda_parity_collapse_f64(void *device_state_vector, int encoded_qubits, int outcome, double weight);
+int mipt_cuda_parity_expand_f32(void *device_state_vector, int full_qubits);
+int mipt_cuda_parity_expand_f64(void *device_state_vector, int full_qubits);
+const char *mipt_cuda_cusv_parity_last_error(void);
+
 /* ----------------------------------------------------------- measurement */
 
 /* Sequential single-site Born measurement with collapse; the collapse is
@@ -153,6 +209,8 @@ typedef struct mipt_gb300_batch_config
     int tile_qubits;   /* local qubits per pass tile, 0 = default */
     int tmi_cycles;    /* TMI quarters at cyclic offsets 0..tmi_cycles-1 (0 or 1: offset 0 only;
                           at most n/4) -- cpp/include/mipt/tmi/compute.hpp:89-113 */
+    int lattice_x;     /* lattice_y > 1: 2-D four-colour brickwork on a lattice_x x lattice_y torus */
+    int lattice_y;     /* (n_qubits = x * y, qubit = row * x + column; closed is ignored) */
 } mipt_gb300_batch_config;
 
 typedef struct mipt_gb300_batch mipt_gb300_batch;
@@ -179,6 +237,29 @@ int mipt_gb300_batch_execute(mipt_gb300_batch *batch, void *stream);
 int mipt_gb300_batch_fetch(mipt_gb300_batch *batch, uint64_t *measured, uint64_t *outcomes, double *surprisal,
                            double *obs, double *rho3);
 /* prepare + execute + fetch in one synchronous call. */
+/* Extra observable regions, evaluated at every observation point: the
+ * entropy of order 1 (von Neumann) or 2 (Renyi-2) of the kept modes
+ * modes[0..k). Add before mipt_gb300_batch_prepare_haar; *region_id gets the
+ * region's column in mipt_gb300_batch_fetch_regions's out[count][points][regions]. */
+int mipt_gb300_batch_add_region(mipt_gb300_batch *batch, const int *modes, int k, int order, int *region_id);
+int mipt_gb300_batch_fetch_regions(mipt_gb300_batch *batch, double *out);
+/* Three-site subsystems of the rho3 output (default: the n ring triples in
+ * 1-D, the horizontal then vertical lattice triples in 2-D,
+ * cpp/include/mipt/rdm.hpp:92-127). With observe_every > 0 the blocks are also
+ * evaluated at every observation point: mipt_gb300_batch_fetch_rho3_points
+ * writes out[count][points][subsystems][128]. */
+int mipt_gb300_batch_set_rho3_subsystems(mipt_gb300_batch *batch, const int *triples, int subsystem_count);
+int mipt_gb300_batch_rho3_subsystem_count(mipt_gb300_batch *batch);
+int mipt_gb300_batch_fetch_rho3_points(mipt_gb300_batch *batch, double *out);
+
+/* The bond list of colour 0..3 of the x by y lattice brickwork (pairs[2*count]) */
+int mipt_gb300_lattice_bonds(int x, int y, int colour, int *pairs, int *count);
+/* One 2-D Haar trajectory as the batch draws it (layer t uses colour t % 4):
+ * outputs as mipt_gb300_draw_haar with `layers` layers. */
+int mipt_gb300_draw_haar_lattice(uint64_t seed, int x, int y, int layers, double p, int chunk_bits,
+                                 int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured,
+                                 double *uniforms, int *n_uniforms);
+
 /* TMI at every cyclic offset, after mipt_gb300_batch_execute:
  * tmi[count][points][tmi_cycles] (order 1: von Neumann, 2: Renyi-2; the
  * batch must have been created with the matching MIPT_GB300_OBS_TMI_* flag).

@@ -425,6 +425,23 @@ int compat_rho3(const void *state, int n, const int *subs, int count, int fermio
     return 0;
 }
 
+// Host-resident state vectors: one reusable device copy per calling thread.
+template <typename Real>
+int host_rho3(const void *host_state, int n, const int *subs, int count, int fermion, double *out, double *fout)
+{
+    if (!host_state || n < 3 || n > 32) return fail(MIPT_GB300_E_INVALID, "invalid host state vector");
+    static thread_local DevBuf dev;
+    const std::size_t bytes = sizeof(Real) * 2 * (std::size_t{1} << n);
+    MG_CUDA(dev.ensure(bytes));
+    MG_CUDA(cudaMemcpy(dev.p, host_state, bytes, cudaMemcpyHostToDevice));
+    if (fermion == 2)
+    {
+        const int rc = compat_rho3<Real>(dev.p, n, subs, count, 0, out);
+        return rc ? rc : compat_rho3<Real>(dev.p, n, subs, count, 1, fout);
+    }
+    return compat_rho3<Real>(dev.p, n, subs, count, fermion, out);
+}
+
 // --------------------------------------------- single-site measurement
 constexpr int kNormBlocks = 256;
 
@@ -566,7 +583,12 @@ struct mipt_gb300_batch
     int T = 0, G = 0, kmax = 0, cmin = 0;
     std::uint64_t dim = 0;
     std::size_t elem = 0;
-    std::vector<PassPlan> plan[2];
+    std::vector<PassPlan> plan[4]; // per colour: 2 (1-D even/odd) or 4 (2-D)
+    int ncolour = 2;
+    bool lattice = false;
+    std::vector<int> region_slots; // request index of each added region
+    int rho3_count = 0;            // three-site subsystems
+    DevBuf rho3_pts;               // [points][count][rho3_count][128]
     DevBuf states, gates, meas, forced, col, res, part, bins, err, ent, subs, rho3, r3scratch;
     PinnedBuf h_gates, h_meas, h_forced, h_res;
     std::vector<std::uint64_t> measured;
@@ -645,6 +667,34 @@ enum
 extern "C" {
 
 const char *mipt_gb300_last_error(void) { return g_error.c_str(); }
+
+
+int mipt_cuda_rho3_subsystems_complex_host_f64(const void *s, int n, const int *subs, int c, double *o)
+{
+    return host_rho3<double>(s, n, subs, c, 0, o, nullptr);
+}
+int mipt_cuda_rho3_subsystems_complex_host_f32(const void *s, int n, const int *subs, int c, double *o)
+{
+    return host_rho3<float>(s, n, subs, c, 0, o, nullptr);
+}
+int mipt_cuda_rho3_subsystems_complex_host_fermion_f64(const void *s, int n, const int *subs, int c, double *o)
+{
+    return host_rho3<double>(s, n, subs, c, 1, o, nullptr);
+}
+int mipt_cuda_rho3_subsystems_complex_host_fermion_f32(const void *s, int n, const int *subs, int c, double *o)
+{
+    return host_rho3<float>(s, n, subs, c, 1, o, nullptr);
+}
+int mipt_cuda_rho3_subsystems_complex_host_both_f64(const void *s, int n, const int *subs, int c, double *o,
+                                                    double *fo)
+{
+    return host_rho3<double>(s, n, subs, c, 2, o, fo);
+}
+int mipt_cuda_rho3_subsystems_complex_host_both_f32(const void *s, int n, const int *subs, int c, double *o,
+                                                    double *fo)
+{
+    return host_rho3<float>(s, n, subs, c, 2, o, fo);
+}
 const char *mipt_gb300_version(void) { return "mipt_gb300 0.1 (sm_103a)"; }
 std::uint64_t mipt_gb300_splitmix64(std::uint64_t v) { return mg::splitmix64(v); }
 std::uint64_t mipt_gb300_trajectory_seed(std::uint64_t m, std::uint64_t i) { return mg::trajectory_seed(m, i); }
@@ -944,11 +994,51 @@ int mipt_gb300_engine_measure_layer(mipt_gb300_engine *e, const int *sites, int 
 }
 
 // ----------------------------------------------------------------- batch
+} // extern "C"
+
+namespace
+{
+// Uploads the rho3 triples and sizes the rho3 outputs and scratch.
+int set_rho3_subs(mipt_gb300_batch *b, const std::vector<int> &subs)
+{
+    const int n = b->cfg.n_qubits, S = static_cast<int>(subs.size() / 3);
+    if (S <= 0) return fail(MIPT_GB300_E_INVALID, "no rho3 subsystems");
+    for (int i = 0; i < S; ++i)
+    {
+        const int a = subs[3 * i], c = subs[3 * i + 1], d = subs[3 * i + 2];
+        if (a < 0 || a >= n || c < 0 || c >= n || d < 0 || d >= n || a == c || a == d || c == d)
+            return fail(MIPT_GB300_E_INVALID, "three-site subsystem out of range or repeated");
+    }
+    const std::size_t C = static_cast<std::size_t>(b->capacity);
+    cudaError_t e;
+    if ((e = b->subs.ensure(sizeof(int) * subs.size())) != cudaSuccess) return cuda_fail(e, "subs");
+    if ((e = cudaMemcpy(b->subs.p, subs.data(), sizeof(int) * subs.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "subs upload");
+    if ((e = b->rho3.ensure(C * S * 128 * sizeof(double))) != cudaSuccess) return cuda_fail(e, "rho3");
+    if ((e = b->r3scratch.ensure(rho3_scratch_bytes(n, b->capacity, S))) != cudaSuccess)
+        return cuda_fail(e, "rho3 scratch");
+    if (b->cfg.observe_every > 0)
+        if ((e = b->rho3_pts.ensure(static_cast<std::size_t>(b->points) * C * S * 128 * sizeof(double))) !=
+            cudaSuccess)
+            return cuda_fail(e, "rho3 per point");
+    b->rho3_count = S;
+    return 0;
+}
+} // namespace
+
+extern "C" {
 int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mipt_gb300_batch **out)
 {
     if (!cfg || !out || capacity <= 0) return fail(MIPT_GB300_E_INVALID, "null config or capacity <= 0");
     const int n = cfg->n_qubits;
-    if (n < 4 || n > 30 || (n % 2) != 0) return fail(MIPT_GB300_E_INVALID, "n_qubits must be even, 4..30");
+    const bool lattice = cfg->lattice_y > 1;
+    if (lattice)
+    {
+        if (cfg->lattice_x < 2 || cfg->lattice_x * cfg->lattice_y != n || n < 4 || n > 30)
+            return fail(MIPT_GB300_E_INVALID, "lattice needs x >= 2, y >= 2 and x * y = n_qubits <= 30");
+    }
+    else if (n < 4 || n > 30 || (n % 2) != 0)
+        return fail(MIPT_GB300_E_INVALID, "n_qubits must be even, 4..30");
     if (cfg->periods < 1) return fail(MIPT_GB300_E_INVALID, "periods must be >= 1");
     if (cfg->chunk_bits < 1 || cfg->chunk_bits > 20) return fail(MIPT_GB300_E_INVALID, "chunk_bits must be 1..20");
     if ((cfg->observables & (MIPT_GB300_OBS_TMI_VN | MIPT_GB300_OBS_TMI_S2)) && (n % 4) != 0)
@@ -967,14 +1057,24 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     if (n - std::min(b->kmax, n) + b->cmin > 20) return fail(MIPT_GB300_E_INVALID, "tile too small for this n");
     b->dim = 1ull << n;
     b->elem = cfg->fp64 ? 16 : 8;
-    for (int parity = 0; parity < 2; ++parity)
+    b->lattice = lattice;
+    b->ncolour = lattice ? 4 : 2;
+    for (int colour = 0; colour < b->ncolour; ++colour)
     {
         std::vector<Bond> bonds;
-        const int stop = (cfg->closed && parity == 1 && n > 2) ? n : n - 1;
-        for (int i = parity; i < stop; i += 2) bonds.push_back(Bond{i, (i + 1) % n});
         try
         {
-            b->plan[parity] = plan_layer(n, bonds, b->kmax, b->cmin,
+            if (lattice)
+            {
+                for (const auto &pr : lattice_bonds(cfg->lattice_x, cfg->lattice_y, colour))
+                    bonds.push_back(Bond{pr.first, pr.second});
+            }
+            else
+            {
+                const int stop = (cfg->closed && colour == 1 && n > 2) ? n : n - 1;
+                for (int i = colour; i < stop; i += 2) bonds.push_back(Bond{i, (i + 1) % n});
+            }
+            b->plan[colour] = plan_layer(n, bonds, b->kmax, b->cmin,
                                          cfg->fp64 ? register_bits<double>() : register_bits<float>());
         }
         catch (const std::exception &e)
@@ -1046,19 +1146,26 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
             return cuda_fail(e, "entropy outputs");
     if (cfg->rho3)
     {
+        // Default triples: the ring {s, s+1, s+2} in 1-D; in 2-D the horizontal
+        // then the vertical lattice triples (cpp/include/mipt/rdm.hpp:92-127).
         std::vector<int> subs;
-        for (int s = 0; s < n; ++s)
+        if (lattice)
         {
-            subs.push_back(s);
-            subs.push_back((s + 1) % n);
-            subs.push_back((s + 2) % n);
+            const int X = cfg->lattice_x, Y = cfg->lattice_y;
+            for (int r = 0; r < Y; ++r)
+                for (int c = 0; c < X; ++c)
+                    for (int k = 0; k < 3; ++k) subs.push_back(r * X + (c + k) % X);
+            for (int c = 0; c < X; ++c)
+                for (int r = 0; r < Y; ++r)
+                    for (int k = 0; k < 3; ++k) subs.push_back(((r + k) % Y) * X + c);
         }
-        if ((e = b->subs.ensure(sizeof(int) * subs.size())) != cudaSuccess) return cuda_fail(e, "subs");
-        if ((e = cudaMemcpy(b->subs.p, subs.data(), sizeof(int) * subs.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return cuda_fail(e, "subs upload");
-        if ((e = b->rho3.ensure(C * n * 128 * sizeof(double))) != cudaSuccess) return cuda_fail(e, "rho3");
-        if ((e = b->r3scratch.ensure(rho3_scratch_bytes(n, capacity, n))) != cudaSuccess)
-            return cuda_fail(e, "rho3 scratch");
+        else
+        {
+            for (int s = 0; s < n; ++s)
+                for (int k = 0; k < 3; ++k) subs.push_back((s + k) % n);
+        }
+        const int rc = set_rho3_subs(b.get(), subs);
+        if (rc) return rc;
     }
     if ((e = b->h_gates.ensure(C * T * b->G * 16 * b->elem)) != cudaSuccess) return cuda_fail(e, "pinned gates");
     if ((e = b->h_meas.ensure(C * T * sizeof(LayerMeas))) != cudaSuccess) return cuda_fail(e, "pinned meas");
@@ -1079,7 +1186,11 @@ int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seed
     std::vector<TrajectoryDraw> draws;
     try
     {
-        draw_haar_batch(seeds, p, count, n, b->cfg.periods, b->cfg.closed != 0, cb, draws, b->cfg.host_threads);
+        if (b->lattice)
+            draw_haar_lattice_batch(seeds, p, count, b->cfg.lattice_x, b->cfg.lattice_y, T, cb, draws,
+                                    b->cfg.host_threads);
+        else
+            draw_haar_batch(seeds, p, count, n, b->cfg.periods, b->cfg.closed != 0, cb, draws, b->cfg.host_threads);
     }
     catch (const std::exception &e)
     {
@@ -1145,7 +1256,7 @@ int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seed
             {
                 b->any_meas[t] = 1;
                 b->max_chunks[t] = std::max(b->max_chunks[t], M.nchunks);
-                const PassGeom &hg = fused_hist_geometry(b->plan[t & 1].back(), b->cfg.fp64 == 0);
+                const PassGeom &hg = fused_hist_geometry(b->plan[t % b->ncolour].back(), b->cfg.fp64 == 0);
                 const int ml = local_measured_count(hg, M.chunk[0]);
                 if ((std::size_t{1} << (hg.n_nl + ml)) > kHistScratch) b->fusable[t] = 0;
             }
@@ -1194,7 +1305,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     const std::size_t gstride = static_cast<std::size_t>(T) * G * 16;
     for (int t = 0; t < T; ++t)
     {
-        const auto &plan = b->plan[t & 1];
+        const auto &plan = b->plan[t % b->ncolour];
         const bool fuse = b->any_meas[t] && b->fusable[t];
         for (std::size_t pi = 0; pi < plan.size(); ++pi)
         {
@@ -1243,6 +1354,17 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             const int rc = run_entropies<Real>(states, n, reqs, col + t, T, b->ws, s, b->ent.as<double>(), L);
             if (rc) return rc;
         }
+        if (due && b->cfg.rho3 && b->cfg.observe_every > 0)
+        {
+            const int point = (t + 1) / b->cfg.observe_every - 1;
+            Mark m(b, K_OBS, s);
+            MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count, b->cfg.fermion_trace ? 1 : 0,
+                                     col + t, T,
+                                     b->rho3_pts.as<double>() +
+                                         static_cast<std::size_t>(point) * b->capacity * b->rho3_count * 128,
+                                     b->r3scratch.p, b->r3scratch.bytes, s));
+            L += 2;
+        }
     }
     // Leave every trajectory in its collapsed, normalised final state.
     {
@@ -1268,8 +1390,8 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     if (b->cfg.rho3)
     {
         Mark m(b, K_OBS, s);
-        MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), n, b->cfg.fermion_trace ? 1 : 0, nullptr, 0,
-                                 b->rho3.as<double>(), b->r3scratch.p, b->r3scratch.bytes, s));
+        MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count, b->cfg.fermion_trace ? 1 : 0,
+                                 nullptr, 0, b->rho3.as<double>(), b->r3scratch.p, b->r3scratch.bytes, s));
         L += 2;
     }
     b->launches = L;
@@ -1354,9 +1476,121 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
     if (rho3)
     {
         if (!b->cfg.rho3) return fail(MIPT_GB300_E_INVALID, "batch was created without rho3");
-        MG_CUDA(cudaMemcpy(rho3, b->rho3.p, sizeof(double) * 128 * n * count, cudaMemcpyDeviceToHost));
+        MG_CUDA(cudaMemcpy(rho3, b->rho3.p, sizeof(double) * 128 * b->rho3_count * count, cudaMemcpyDeviceToHost));
     }
     return 0;
+}
+
+int mipt_gb300_batch_add_region(mipt_gb300_batch *b, const int *modes, int k, int order, int *region_id)
+{
+    if (!b || !modes || !region_id || k < 0 || k > 16 || (order != 1 && order != 2))
+        return fail(MIPT_GB300_E_INVALID, "bad region (k <= 16, order 1 or 2)");
+    const int n = b->cfg.n_qubits;
+    std::uint64_t used = 0;
+    for (int i = 0; i < k; ++i)
+    {
+        if (modes[i] < 0 || modes[i] >= n || ((used >> modes[i]) & 1ull))
+            return fail(MIPT_GB300_E_INVALID, "region modes must be distinct and in range");
+        used |= 1ull << modes[i];
+    }
+    b->region_slots.push_back(static_cast<int>(b->reqs.size()));
+    b->reqs.push_back(EntReq{0, order, b->cfg.fermion_trace ? 1 : 0, std::vector<int>(modes, modes + k), 0});
+    b->reqs_per_point = static_cast<int>(b->reqs.size());
+    MG_CUDA(b->ent.ensure(static_cast<std::size_t>(b->capacity) * b->points * b->reqs_per_point * sizeof(double)));
+    *region_id = static_cast<int>(b->region_slots.size()) - 1;
+    b->executed = false;
+    return 0;
+}
+
+int mipt_gb300_batch_fetch_regions(mipt_gb300_batch *b, double *out)
+{
+    if (!b || !b->executed || !out) return fail(MIPT_GB300_E_INVALID, "batch not executed or null output");
+    if (b->region_slots.empty()) return fail(MIPT_GB300_E_INVALID, "batch has no regions");
+    MG_CUDA(cudaDeviceSynchronize());
+    const std::size_t P = b->points, R = b->reqs_per_point, G = b->region_slots.size();
+    std::vector<double> ent(static_cast<std::size_t>(b->count) * P * R);
+    MG_CUDA(cudaMemcpy(ent.data(), b->ent.p, sizeof(double) * ent.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < b->count; ++i)
+        for (std::size_t pt = 0; pt < P; ++pt)
+            for (std::size_t g = 0; g < G; ++g)
+                out[(static_cast<std::size_t>(i) * P + pt) * G + g] =
+                    ent[(static_cast<std::size_t>(i) * P + pt) * R + b->region_slots[g]];
+    return 0;
+}
+
+int mipt_gb300_batch_set_rho3_subsystems(mipt_gb300_batch *b, const int *triples, int count)
+{
+    if (!b || !triples || count <= 0) return fail(MIPT_GB300_E_INVALID, "bad rho3 subsystems");
+    if (!b->cfg.rho3) return fail(MIPT_GB300_E_INVALID, "batch was created without rho3");
+    b->executed = false;
+    return set_rho3_subs(b, std::vector<int>(triples, triples + 3 * static_cast<std::size_t>(count)));
+}
+
+int mipt_gb300_batch_rho3_subsystem_count(mipt_gb300_batch *b) { return b ? b->rho3_count : -1; }
+
+int mipt_gb300_batch_fetch_rho3_points(mipt_gb300_batch *b, double *out)
+{
+    if (!b || !b->executed || !out) return fail(MIPT_GB300_E_INVALID, "batch not executed or null output");
+    if (!b->cfg.rho3 || b->cfg.observe_every <= 0)
+        return fail(MIPT_GB300_E_INVALID, "rho3 per point needs rho3 and observe_every > 0");
+    MG_CUDA(cudaDeviceSynchronize());
+    const std::size_t P = b->points, S = b->rho3_count, C = b->capacity, per = S * 128;
+    for (std::size_t pt = 0; pt < P; ++pt)
+        for (int i = 0; i < b->count; ++i)
+            MG_CUDA(cudaMemcpy(out + (static_cast<std::size_t>(i) * P + pt) * per,
+                               b->rho3_pts.as<double>() + (pt * C + i) * per, sizeof(double) * per,
+                               cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int mipt_gb300_lattice_bonds(int x, int y, int colour, int *pairs, int *count)
+{
+    try
+    {
+        const auto bonds = lattice_bonds(x, y, colour);
+        if (count) *count = static_cast<int>(bonds.size());
+        if (pairs)
+            for (std::size_t i = 0; i < bonds.size(); ++i)
+            {
+                pairs[2 * i] = bonds[i].first;
+                pairs[2 * i + 1] = bonds[i].second;
+            }
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+}
+
+int mipt_gb300_draw_haar_lattice(std::uint64_t seed, int x, int y, int layers, double p, int chunk_bits,
+                                 int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured,
+                                 double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        TrajectoryDraw d;
+        draw_haar_lattice_trajectory(seed, x, y, layers, p, chunk_bits, d);
+        for (int t = 0; t < d.layers; ++t)
+        {
+            if (gates_per_layer) gates_per_layer[t] = d.bond_count[t];
+            if (measured) measured[t] = d.measured[t];
+        }
+        if (bond_q) std::copy(d.bond_q.begin(), d.bond_q.end(), bond_q);
+        if (bond_u)
+            for (std::size_t i = 0; i < d.bond_u.size(); ++i)
+            {
+                bond_u[2 * i] = d.bond_u[i].real();
+                bond_u[2 * i + 1] = d.bond_u[i].imag();
+            }
+        if (uniforms) std::copy(d.uniforms.begin(), d.uniforms.end(), uniforms);
+        if (n_uniforms) *n_uniforms = static_cast<int>(d.uniforms.size());
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
 }
 
 int mipt_gb300_batch_fetch_tmi(mipt_gb300_batch *b, int order, double *tmi)

@@ -141,6 +141,115 @@ void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool
     out.uniform_offset[T] = static_cast<int>(out.uniforms.size());
 }
 
+std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour)
+{
+    if (X < 2 || Y < 1 || colour < 0 || colour > 3) throw std::invalid_argument("bad lattice or colour");
+    std::vector<std::pair<int, int>> out;
+    // One line of `len` sites (site i at base + i*step): pairs from 0 when the
+    // line's parity matches the colour, else the wrap bond (even lengths > 2)
+    // and pairs from 1.
+    auto line = [&](int base, int step, int len, bool from_zero) {
+        if (len < 2) return;
+        if (from_zero)
+        {
+            for (int i = 0; i + 1 < len; i += 2) out.emplace_back(base + i * step, base + (i + 1) * step);
+            return;
+        }
+        if (len % 2 == 0 && len > 2) out.emplace_back(base, base + (len - 1) * step);
+        for (int i = 1; i + 1 < len; i += 2) out.emplace_back(base + i * step, base + (i + 1) * step);
+    };
+    if (colour < 2)
+        for (int r = 0; r < Y; ++r) line(r * X, 1, X, (r % 2) == colour);
+    else
+        for (int c = 0; c < X; ++c) line(c, X, Y, (c % 2) == colour - 2);
+    return out;
+}
+
+void draw_haar_lattice_trajectory(std::uint64_t seed, int X, int Y, int layers, double p, int chunk_bits,
+                                  TrajectoryDraw &out)
+{
+    const int n = X * Y;
+    if (X < 2 || Y < 2 || n > 62) throw std::invalid_argument("lattice needs X, Y >= 2 and X*Y <= 62");
+    if (chunk_bits < 1) throw std::invalid_argument("chunk_bits must be positive");
+    std::mt19937 gates_rng, meas_rng;
+    seed_mt(gates_rng, seed);
+    seed_mt(meas_rng, splitmix64(seed ^ 0xa0761d0dull));
+    std::vector<std::pair<int, int>> colours[4];
+    for (int c = 0; c < 4; ++c) colours[c] = lattice_bonds(X, Y, c);
+    const int mb = n / 2;
+    out.n = n;
+    out.layers = layers;
+    out.max_bonds = mb;
+    out.bond_count.assign(layers, 0);
+    out.bond_q.assign(static_cast<std::size_t>(layers) * mb * 2, 0);
+    out.bond_u.assign(static_cast<std::size_t>(layers) * mb * 16, C(0.0, 0.0));
+    out.measured.assign(layers, 0);
+    out.uniforms.clear();
+    out.uniform_offset.assign(layers + 1, 0);
+    std::uniform_real_distribution<double> unif(0.0, 1.0);
+    for (int t = 0; t < layers; ++t)
+    {
+        const auto &bonds = colours[t % 4];
+        for (std::size_t j = 0; j < bonds.size(); ++j)
+        {
+            C *u = &out.bond_u[(static_cast<std::size_t>(t) * mb + j) * 16];
+            do
+            {
+                std::normal_distribution<double> gauss(0.0, 1.0);
+                gram_schmidt_u4(gates_rng, gauss, u);
+            } while (csd_is_singular(u));
+            out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2] = bonds[j].first;
+            out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2 + 1] = bonds[j].second;
+        }
+        out.bond_count[t] = static_cast<int>(bonds.size());
+        std::uint64_t mask = 0;
+        if (p >= 1.0)
+        {
+            mask = (1ull << n) - 1ull;
+        }
+        else if (p > 0.0)
+        {
+            std::bernoulli_distribution flag(p);
+            for (int s = 0; s < n; ++s)
+                if (flag(gates_rng)) mask |= 1ull << s;
+        }
+        out.measured[t] = mask;
+        out.uniform_offset[t] = static_cast<int>(out.uniforms.size());
+        const int m = __builtin_popcountll(mask);
+        for (int c = 0; c < m; c += chunk_bits) out.uniforms.push_back(unif(meas_rng));
+    }
+    out.uniform_offset[layers] = static_cast<int>(out.uniforms.size());
+}
+
+void draw_haar_lattice_batch(const std::uint64_t *seeds, const double *p, int count, int X, int Y, int layers,
+                             int chunk_bits, std::vector<TrajectoryDraw> &out, int threads)
+{
+    out.resize(count);
+    if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    threads = std::min(threads, std::max(1, count));
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto work = [&]() {
+        for (;;)
+        {
+            const int i = next.fetch_add(1);
+            if (i >= count) return;
+            try
+            {
+                draw_haar_lattice_trajectory(seeds[i], X, Y, layers, p[i], chunk_bits, out[i]);
+            }
+            catch (...)
+            {
+                failed = true;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(work);
+    for (auto &th : pool) th.join();
+    if (failed) throw std::runtime_error("lattice trajectory draw failed");
+}
+
 void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, bool closed,
                      int chunk_bits, std::vector<TrajectoryDraw> &out, int threads)
 {

@@ -73,3 +73,23 @@ void draw_fermion_trajectory(std::uint64_t seed, int n, int depth, double p, boo
 void draw_fermion_batch(const std::uint64_t *seeds, const double *p, int count, int n, int depth, bool closed,
                         std::vector<FermionDraw> &out, int threads);
 } // namespace mg
+
+namespace mg
+{
+// Four-colour brickwork on an X x Y torus, qubit q = r * X + c. Colour 0/1:
+// horizontal bonds, rows of parity 0/1 pair (c, c+1) from c = 0, the other
+// rows take the wrap bond (0, X-1) first and pair from c = 1; colour 2/3: the
+// same for columns and vertical bonds. Bond order and first qubits follow the
+// reference's 2-D loops (python/mipt.py:244-311); a direction of odd length has
+// no wrap bond (one idle site per line), which the reference's square-lattice
+// indexing does not define.
+std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour);
+
+// A 2-D Haar trajectory of `layers` layers (colour t % 4 at layer t), drawn
+// with the streams and per-layer order of the 1-D path: the layer's unitaries,
+// then Bernoulli(p) flags site by site, then one measurement uniform per chunk.
+void draw_haar_lattice_trajectory(std::uint64_t seed, int X, int Y, int layers, double p, int chunk_bits,
+                                  TrajectoryDraw &out);
+void draw_haar_lattice_batch(const std::uint64_t *seeds, const double *p, int count, int X, int Y, int layers,
+                             int chunk_bits, std::vector<TrajectoryDraw> &out, int threads);
+} // namespace mg
