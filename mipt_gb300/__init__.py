@@ -38,7 +38,7 @@ class FFConfig(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in (
         "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
-        "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles")]
+        "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles", "lattice_x", "lattice_y")]
 
 
 def lib():
@@ -80,6 +80,13 @@ def lib():
     L.mipt_gb300_batch_execute.argtypes = [vp, vp]
     L.mipt_gb300_batch_fetch.argtypes = [vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_fetch_tmi.argtypes = [vp, ci, vp]
+    L.mipt_gb300_batch_add_region.argtypes = [vp, vp, ci, ci, vp]
+    L.mipt_gb300_batch_fetch_regions.argtypes = [vp, vp]
+    L.mipt_gb300_batch_set_rho3_subsystems.argtypes = [vp, vp, ci]
+    L.mipt_gb300_batch_rho3_subsystem_count.argtypes = [vp]
+    L.mipt_gb300_batch_fetch_rho3_points.argtypes = [vp, vp]
+    L.mipt_gb300_lattice_bonds.argtypes = [ci, ci, ci, vp, vp]
+    L.mipt_gb300_draw_haar_lattice.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
     L.mipt_gb300_batch_state.restype = vp
@@ -245,9 +252,12 @@ class Batch:
     """Many Haar trajectories of one chain length, run as one device schedule."""
 
     def __init__(self, n, periods, capacity, closed=True, fp64=False, chunk_bits=16, observables=0,
-                 observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0, tmi_cycles=0):
+                 observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0, tmi_cycles=0,
+                 lattice=None):
+        lx, ly = lattice if lattice is not None else (0, 0)
         cfg = BatchConfig(n, periods, int(closed), int(fp64), chunk_bits, observables, observe_every, int(rho3),
-                          int(fermion_trace), host_threads, tile_qubits, tmi_cycles)
+                          int(fermion_trace), host_threads, tile_qubits, tmi_cycles, lx, ly)
+        self.regions = 0
         self.tmi_cycles = max(1, tmi_cycles)
         h = ctypes.c_void_p()
         _check(lib().mipt_gb300_batch_create(ctypes.byref(cfg), capacity, ctypes.byref(h)))
@@ -285,9 +295,35 @@ class Batch:
         outcomes = np.zeros((c, T), np.uint64)
         surprisal = np.zeros((c, T))
         obs = np.zeros((c, self.points, 4))
-        rho3 = np.zeros((c, self.n, 128)) if self.rho3 else None
+        rho3 = np.zeros((c, self.rho3_count, 128)) if self.rho3 else None
         _check(lib().mipt_gb300_batch_fetch(self._h, _p(measured), _p(outcomes), _p(surprisal), _p(obs), _p(rho3)))
         return dict(measured=measured, outcomes=outcomes, surprisal=surprisal, obs=obs, rho3=rho3)
+
+    @property
+    def rho3_count(self):
+        return lib().mipt_gb300_batch_rho3_subsystem_count(self._h)
+
+    def add_region(self, modes, order=1):
+        """Entropy (order 1: von Neumann, 2: Renyi-2) of `modes` at every observation point."""
+        modes = np.ascontiguousarray(modes, np.int32)
+        rid = ctypes.c_int()
+        _check(lib().mipt_gb300_batch_add_region(self._h, _p(modes), len(modes), int(order), ctypes.byref(rid)))
+        self.regions += 1
+        return rid.value
+
+    def fetch_regions(self):
+        out = np.zeros((self.count, self.points, self.regions))
+        _check(lib().mipt_gb300_batch_fetch_regions(self._h, _p(out)))
+        return out
+
+    def set_rho3_subsystems(self, triples):
+        t = np.ascontiguousarray(triples, np.int32).reshape(-1, 3)
+        _check(lib().mipt_gb300_batch_set_rho3_subsystems(self._h, _p(t), len(t)))
+
+    def fetch_rho3_points(self):
+        out = np.zeros((self.count, self.points, self.rho3_count, 128))
+        _check(lib().mipt_gb300_batch_fetch_rho3_points(self._h, _p(out)))
+        return out
 
     def fetch_tmi(self, order=1):
         """TMI at every cyclic offset: [count][points][tmi_cycles]."""
@@ -317,6 +353,28 @@ class Batch:
         n = np.zeros(5, np.int64)
         _check(lib().mipt_gb300_batch_kernel_stats(self._h, _p(ms), _p(n)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+
+def lattice_bonds(x, y, colour):
+    """Bond list (pairs) of colour 0..3 of the x by y lattice brickwork."""
+    pairs = np.zeros(x * y + 2, np.int32)
+    cnt = ctypes.c_int()
+    _check(lib().mipt_gb300_lattice_bonds(x, y, colour, _p(pairs), ctypes.byref(cnt)))
+    return pairs[: 2 * cnt.value].reshape(-1, 2)
+
+
+def draw_haar_lattice(seed, x, y, layers, p, chunk_bits=16):
+    """One 2-D Haar trajectory as the batch draws it."""
+    n, mb = x * y, (x * y) // 2
+    gpl = np.zeros(layers, np.int32)
+    bq = np.zeros((layers, mb, 2), np.int32)
+    bu = np.zeros((layers, mb, 32))
+    meas = np.zeros(layers, np.uint64)
+    uni = np.zeros(layers * n)
+    nu = ctypes.c_int()
+    _check(lib().mipt_gb300_draw_haar_lattice(seed, x, y, layers, p, chunk_bits, _p(gpl), _p(bq), _p(bu), _p(meas),
+                                               _p(uni), ctypes.byref(nu)))
+    return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu.value])
 
 
 def outcomes_to_mask(sites, outcomes):

@@ -146,8 +146,8 @@ std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour)
     if (X < 2 || Y < 1 || colour < 0 || colour > 3) throw std::invalid_argument("bad lattice or colour");
     std::vector<std::pair<int, int>> out;
     // One line of `len` sites (site i at base + i*step): pairs from 0 when the
-    // line's parity matches the colour, else the wrap bond (even lengths > 2)
-    // and pairs from 1.
+    // line's parity matches the colour, else the wrap bond (even lengths) and
+    // pairs from 1.
     auto line = [&](int base, int step, int len, bool from_zero) {
         if (len < 2) return;
         if (from_zero)
@@ -155,7 +155,7 @@ std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour)
             for (int i = 0; i + 1 < len; i += 2) out.emplace_back(base + i * step, base + (i + 1) * step);
             return;
         }
-        if (len % 2 == 0 && len > 2) out.emplace_back(base, base + (len - 1) * step);
+        if (len % 2 == 0) out.emplace_back(base, base + (len - 1) * step);
         for (int i = 1; i + 1 < len; i += 2) out.emplace_back(base + i * step, base + (i + 1) * step);
     };
     if (colour < 2)

@@ -162,6 +162,65 @@ void draw_trajectory(std::vector<Layer> &layers, std::uint64_t seed, int n, int 
     for (int t = 0; t < 2 * periods; ++t) draw_layer(layers[t], n, t & 1, p, closed, gates);
 }
 
+// Four-colour 2-D brickwork on an X x Y torus, qubit q = r * X + c: the loops
+// of the reference's python/mipt.py:244-311 (colour 0/1 horizontal, 2/3
+// vertical; lines of the colour's parity pair from site 0, the other lines
+// take the wrap bond first and pair from site 1). Lines of odd length get no
+// wrap bond (the reference's square-lattice indexing leaves them undefined).
+std::vector<std::pair<int, int>> lattice_colour(int X, int Y, int colour)
+{
+    std::vector<std::pair<int, int>> b;
+    const bool horizontal = colour < 2;
+    const int lines = horizontal ? Y : X, len = horizontal ? X : Y;
+    for (int i = 0; i < lines; ++i)
+    {
+        auto site = [&](int j) { return horizontal ? i * X + j : j * X + i; };
+        if (i % 2 == colour % 2)
+        {
+            for (int j = 0; j + 1 < len; j += 2) b.emplace_back(site(j), site(j + 1));
+        }
+        else
+        {
+            if (len % 2 == 0) b.emplace_back(site(0), site(len - 1));
+            for (int j = 1; j + 1 < len - (len % 2 == 0 ? 1 : 0); j += 2) b.emplace_back(site(j), site(j + 1));
+        }
+    }
+    return b;
+}
+
+void draw_lattice_trajectory(std::vector<Layer> &layers, std::uint64_t seed, int X, int Y, int T, double p,
+                             std::mt19937 &meas)
+{
+    std::mt19937 gates;
+    seed_pair(seed, gates, meas);
+    const int n = X * Y;
+    layers.resize(T);
+    for (int t = 0; t < T; ++t)
+    {
+        Layer &L = layers[t];
+        L.q.clear();
+        L.m.clear();
+        L.sites.clear();
+        for (const auto &pr : lattice_colour(X, Y, t % 4))
+        {
+            const auto u = draw_u4(gates);
+            L.q.push_back(pr.first);
+            L.q.push_back(pr.second);
+            L.m.insert(L.m.end(), u.begin(), u.end());
+        }
+        if (p >= 1.0)
+        {
+            for (int s = 0; s < n; ++s) L.sites.push_back(s);
+        }
+        else if (p > 0.0)
+        {
+            std::bernoulli_distribution flag(p);
+            for (int s = 0; s < n; ++s)
+                if (flag(gates)) L.sites.push_back(s);
+        }
+    }
+}
+
 // psi <- U psi on (q0, q1); U row-major with index bit 0 = q0, bit 1 = q1.
 void apply_bond(cd *psi, int n, int q0, int q1, const cd *U)
 {
@@ -675,6 +734,104 @@ int orc_haar_draw(std::uint64_t seed, int n, int periods, double p, int closed, 
             for (std::size_t s = 0; s < layers[t].sites.size(); s += chunk_bits) uniforms[u++] = unif(meas);
         }
         *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+int orc_lattice_bonds(int X, int Y, int colour, int *pairs)
+{
+    const auto b = lattice_colour(X, Y, colour);
+    for (std::size_t i = 0; i < b.size(); ++i)
+    {
+        pairs[2 * i] = b[i].first;
+        pairs[2 * i + 1] = b[i].second;
+    }
+    return static_cast<int>(b.size());
+}
+
+// The 2-D draw in orc_haar_draw's output layout (layers = T).
+int orc_haar_lattice_draw(std::uint64_t seed, int X, int Y, int T, double p, int chunk_bits, int *gates_per_layer,
+                          int *gate_q, double *gate_m, int *sites_per_layer, int *sites, double *uniforms,
+                          int *n_uniforms)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<Layer> layers;
+        draw_lattice_trajectory(layers, seed, X, Y, T, p, meas);
+        const int n = X * Y, mg = n / 2;
+        int u = 0;
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        for (std::size_t t = 0; t < layers.size(); ++t)
+        {
+            const int g = static_cast<int>(layers[t].q.size() / 2);
+            gates_per_layer[t] = g;
+            for (int i = 0; i < g; ++i)
+            {
+                gate_q[(t * mg + i) * 2] = layers[t].q[2 * i];
+                gate_q[(t * mg + i) * 2 + 1] = layers[t].q[2 * i + 1];
+                for (int e = 0; e < 16; ++e)
+                {
+                    gate_m[(t * mg + i) * 32 + 2 * e] = layers[t].m[16 * i + e].real();
+                    gate_m[(t * mg + i) * 32 + 2 * e + 1] = layers[t].m[16 * i + e].imag();
+                }
+            }
+            sites_per_layer[t] = static_cast<int>(layers[t].sites.size());
+            for (std::size_t s = 0; s < layers[t].sites.size(); ++s) sites[t * n + s] = layers[t].sites[s];
+            for (std::size_t s = 0; s < layers[t].sites.size(); s += chunk_bits) uniforms[u++] = unif(meas);
+        }
+        *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// A 2-D trajectory in FP64: outcomes[layer][n] (ascending measured sites, -1
+// padding), surprisal[layer], the state after every layer whose index+1 is a
+// multiple of observe_every into states_ri[point] (nullable), final state.
+int orc_run_lattice_trajectory(std::uint64_t seed, int X, int Y, int T, double p, int chunk_bits,
+                               const int *forced, int *outcomes, double *surprisal, int observe_every,
+                               double *states_ri, double *final_psi_ri)
+{
+    try
+    {
+        std::mt19937 meas;
+        std::vector<Layer> layers;
+        draw_lattice_trajectory(layers, seed, X, Y, T, p, meas);
+        const int n = X * Y;
+        const std::uint64_t dim = 1ull << n;
+        std::vector<cd> psi(dim, cd(0.0, 0.0));
+        psi[0] = 1.0;
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        for (int t = 0; t < T; ++t)
+        {
+            const Layer &L = layers[t];
+            for (std::size_t g = 0; g < L.q.size() / 2; ++g)
+                apply_bond(psi.data(), n, L.q[2 * g], L.q[2 * g + 1], &L.m[16 * g]);
+            std::vector<double> us;
+            for (std::size_t s = 0; s < L.sites.size(); s += chunk_bits) us.push_back(unif(meas));
+            std::vector<int> oc(L.sites.size(), 0);
+            int used = 0;
+            const double sp = measure_layer(psi.data(), n, L.sites, chunk_bits, us.data(), used,
+                                            forced ? forced + static_cast<std::size_t>(t) * n : nullptr, oc.data());
+            if (surprisal) surprisal[t] = sp;
+            if (outcomes)
+            {
+                for (int s = 0; s < n; ++s) outcomes[static_cast<std::size_t>(t) * n + s] = -1;
+                for (std::size_t s = 0; s < oc.size(); ++s) outcomes[static_cast<std::size_t>(t) * n + s] = oc[s];
+            }
+            if (states_ri && observe_every > 0 && (t + 1) % observe_every == 0)
+                std::memcpy(states_ri + static_cast<std::size_t>((t + 1) / observe_every - 1) * 2 * dim, psi.data(),
+                            dim * sizeof(cd));
+        }
+        if (final_psi_ri) std::memcpy(final_psi_ri, psi.data(), dim * sizeof(cd));
         return 0;
     }
     catch (...)

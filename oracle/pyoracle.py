@@ -223,3 +223,58 @@ def ff_block_entropy(gamma, modes):
     g = np.ascontiguousarray(gamma, np.float64)
     m = np.ascontiguousarray(modes, np.int32)
     return L.orc_ff_block_entropy(_p(g), g.shape[0] // 2, _p(m), len(m))
+
+
+# ------------------------------------------------------------ 2-D lattices
+def _lattice_bind():
+    L = lib()
+    if getattr(L, "_lattice_bound", False):
+        return L
+    vp, ci, cd, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
+    L.orc_lattice_bonds.argtypes = [ci, ci, ci, vp]
+    L.orc_lattice_bonds.restype = ci
+    L.orc_haar_lattice_draw.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp, vp]
+    L.orc_haar_lattice_draw.restype = ci
+    L.orc_run_lattice_trajectory.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, ci, vp, vp]
+    L.orc_run_lattice_trajectory.restype = ci
+    L._lattice_bound = True
+    return L
+
+
+def lattice_bonds(X, Y, colour):
+    L = _lattice_bind()
+    pairs = np.zeros(X * Y, np.int32)
+    c = L.orc_lattice_bonds(X, Y, colour, _p(pairs))
+    return pairs[: 2 * c].reshape(-1, 2)
+
+
+def haar_lattice_draw(seed, X, Y, layers, p, chunk_bits=16):
+    L = _lattice_bind()
+    n, mg = X * Y, (X * Y) // 2
+    gpl = np.zeros(layers, np.int32)
+    gq = np.zeros((layers, mg, 2), np.int32)
+    gm = np.zeros((layers, mg, 32))
+    spl = np.zeros(layers, np.int32)
+    sites = np.full((layers, n), -1, np.int32)
+    uni = np.zeros(layers * n)
+    nu = np.zeros(1, np.int32)
+    if L.orc_haar_lattice_draw(seed, X, Y, layers, p, chunk_bits, _p(gpl), _p(gq), _p(gm), _p(spl), _p(sites),
+                               _p(uni), _p(nu)):
+        raise RuntimeError("orc_haar_lattice_draw failed")
+    return dict(gates_per_layer=gpl, gate_q=gq, gate_m=gm, sites_per_layer=spl, sites=sites,
+                uniforms=uni[: int(nu[0])])
+
+
+def run_lattice_trajectory(seed, X, Y, layers, p, chunk_bits=16, forced=None, observe_every=0):
+    L = _lattice_bind()
+    n = X * Y
+    outcomes = np.full((layers, n), -1, np.int32)
+    surprisal = np.zeros(layers)
+    points = layers // observe_every if observe_every > 0 else 0
+    states = np.zeros((max(points, 1), 1 << n), np.complex128)
+    psi = np.zeros(1 << n, np.complex128)
+    f = None if forced is None else np.ascontiguousarray(forced, np.int32)
+    if L.orc_run_lattice_trajectory(seed, X, Y, layers, p, chunk_bits, _p(f), _p(outcomes), _p(surprisal),
+                                    observe_every, _p(states) if points else None, _p(psi)):
+        raise RuntimeError("orc_run_lattice_trajectory failed")
+    return dict(outcomes=outcomes, surprisal=surprisal, states=states[:points], psi=psi)
