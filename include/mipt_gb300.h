@@ -281,6 +281,34 @@ long long mipt_gb300_batch_launches(mipt_gb300_batch *batch);
 int mipt_gb300_batch_set_profiling(mipt_gb300_batch *batch, int enable);
 int mipt_gb300_batch_kernel_stats(mipt_gb300_batch *batch, double *ms, long long *launches);
 
+/* ------------------------------------------------- GMN of three-qubit states */
+
+/* Genuine multipartite negativity of rho3 blocks: the reference's monotone
+ * witness SDP (cpp/src/analysis/gmn_mosek.c:14-40, python/gmn.py:236-358),
+ *     min Re Tr(rho W)  s.t.  0 <= Q_m <= I, 0 <= W - PT_m(Q_m) <= I, m = 1..3,
+ * GMN = -min (0 at or below 1e-8), solved for all `count` states at once by
+ * ADMM on the GPU (FP32, or FP64 with fp64 = 1) with FP64 certificates: a
+ * state is done when the primal value and a dual bound differ by at most
+ * gap_tol and the box constraints are violated by at most feas_tol. */
+typedef struct mipt_gb300_gmn_config
+{
+    int max_iter;    /* ADMM iterations per state at most */
+    int check_every; /* iterations between FP64 certificates */
+    double gap_tol;  /* duality gap, e.g. 1e-6 */
+    double feas_tol; /* eigenvalue violation of the box constraints */
+    double sigma;    /* ADMM penalty (0: 1.0) */
+    int fp64;        /* 1: FP64 iterations */
+} mipt_gb300_gmn_config;
+
+/* rho: [count][128] row-major (re, im) 8x8 blocks (the rho3.bin payload
+ * layout). warm_start (nullable): [count][7][128] floats, row-major (re, im)
+ * W, Q_1..3, Z_1..3 (Z_m the duals of the W - PT_m(Q_m) constraints).
+ * Outputs (nullable): gmn[count], gap[count] (at the last certificate),
+ * iterations[count] (negative: max_iter reached without a certificate),
+ * solution[count][7][128] (W, Q_1..3, Z_1..3, same layout). */
+int mipt_gb300_gmn_solve(const mipt_gb300_gmn_config *config, const double *rho, int count,
+                         const float *warm_start, double *gmn, double *gap, int *iterations, double *solution);
+
 /* ------------------------------------------ free fermions (covariance) */
 
 /* Monitored free-fermion circuit on the Majorana covariance matrix of N

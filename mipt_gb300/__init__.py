@@ -86,6 +86,7 @@ def lib():
     L.mipt_gb300_batch_rho3_subsystem_count.argtypes = [vp]
     L.mipt_gb300_batch_fetch_rho3_points.argtypes = [vp, vp]
     L.mipt_gb300_lattice_bonds.argtypes = [ci, ci, ci, vp, vp]
+    L.mipt_gb300_gmn_solve.argtypes = [vp, vp, ci, vp, vp, vp, vp, vp]
     L.mipt_gb300_draw_haar_lattice.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
@@ -353,6 +354,43 @@ class Batch:
         n = np.zeros(5, np.int64)
         _check(lib().mipt_gb300_batch_kernel_stats(self._h, _p(ms), _p(n)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+
+class GmnConfig(ctypes.Structure):
+    _fields_ = [("max_iter", ctypes.c_int), ("check_every", ctypes.c_int), ("gap_tol", ctypes.c_double),
+                ("feas_tol", ctypes.c_double), ("sigma", ctypes.c_double), ("fp64", ctypes.c_int)]
+
+
+def rho_to_ri(rho):
+    """[..., 8, 8] complex -> [..., 128] row-major (re, im) doubles."""
+    rho = np.asarray(rho, np.complex128)
+    return np.ascontiguousarray(np.stack([rho.real, rho.imag], -1).reshape(rho.shape[:-2] + (128,)))
+
+
+def ri_to_rho(ri):
+    ri = np.asarray(ri, np.float64)
+    return (ri[..., 0::2] + 1j * ri[..., 1::2]).reshape(ri.shape[:-1] + (8, 8))
+
+
+def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6, feas_tol=1e-6, sigma=1.0,
+              fp64=False, want_solution=False):
+    """GMN of three-qubit states rho[N, 8, 8] by the batched GPU ADMM.
+    warm_start: [N, 7, 8, 8] (W, Q_1..3, Z_1..3) or None."""
+    r = rho_to_ri(np.asarray(rho).reshape(-1, 8, 8))
+    n = len(r)
+    cfg = GmnConfig(max_iter, check_every, gap_tol, feas_tol, sigma, int(fp64))
+    ws = None
+    if warm_start is not None:
+        ws = np.ascontiguousarray(rho_to_ri(np.asarray(warm_start).reshape(n, 7, 8, 8)), np.float32)
+    g = np.zeros(n)
+    gap = np.zeros(n)
+    it = np.zeros(n, np.int32)
+    sol = np.zeros((n, 7, 128)) if want_solution else None
+    _check(lib().mipt_gb300_gmn_solve(ctypes.byref(cfg), _p(r), n, _p(ws), _p(g), _p(gap), _p(it), _p(sol)))
+    out = dict(gmn=g, gap=gap, iters=it)
+    if want_solution:
+        out["solution"] = ri_to_rho(sol)
+    return out
 
 
 def lattice_bonds(x, y, colour):
