@@ -309,6 +309,28 @@ typedef struct mipt_gb300_gmn_config
 int mipt_gb300_gmn_solve(const mipt_gb300_gmn_config *config, const double *rho, int count,
                          const float *warm_start, double *gmn, double *gap, int *iterations, double *solution);
 
+/* Learned warm start: a multilayer perceptron (dims[0] inputs, ReLU between
+ * layers, linear output) trained and evaluated on the GPU by the library's
+ * own kernels. Weights are FP32 master copies (Adam) and BF16 copies that
+ * every product reads with FP32 accumulation. Parameters are laid out layer
+ * by layer: W_l (dims[l+1] x dims[l], row-major), then b_l. No reference
+ * counterpart (the reference has no learned component). */
+typedef struct mipt_gb300_mlp mipt_gb300_mlp;
+int mipt_gb300_mlp_create(const int *dims, int n_dims, uint64_t seed, mipt_gb300_mlp **out);
+void mipt_gb300_mlp_destroy(mipt_gb300_mlp *mlp);
+long long mipt_gb300_mlp_param_count(const mipt_gb300_mlp *mlp);
+int mipt_gb300_mlp_get_params(mipt_gb300_mlp *mlp, float *params);
+int mipt_gb300_mlp_set_params(mipt_gb300_mlp *mlp, const float *params);
+/* y[n][dims.back()] from x[n][dims[0]] (host arrays). */
+int mipt_gb300_mlp_forward(mipt_gb300_mlp *mlp, const float *x, int n, float *y);
+/* Mean squared error of the n rows and its gradient w.r.t. every parameter. */
+int mipt_gb300_mlp_loss_grad(mipt_gb300_mlp *mlp, const float *x, const float *target, int n, double *loss,
+                             float *grad);
+/* Adam epochs over the n rows in shuffled batches; final_loss = the MSE of
+ * the last batch of the last epoch. */
+int mipt_gb300_mlp_train(mipt_gb300_mlp *mlp, const float *x, const float *target, int n, int epochs, int batch,
+                         float learning_rate, uint64_t shuffle_seed, double *final_loss);
+
 /* ------------------------------------------ free fermions (covariance) */
 
 /* Monitored free-fermion circuit on the Majorana covariance matrix of N

@@ -21,7 +21,7 @@ APPS = os.path.join(HERE, "apps")
 APP_TARGETS = [("mipt.cpp", "mipt.exe"), ("sim_tmi.cpp", "sim_tmi.exe")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu", "parity.cu", "gmn.cu"]
+CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu", "parity.cu", "gmn.cu", "mlp.cu"]
 CXX_SOURCES = ["sampler.cpp"]
 
 
