@@ -290,6 +290,179 @@ def run_gb300(args):
     return 0
 
 
+# ------------------------------------------------- the other BASELINE configs
+# `--config N` measures configuration N of the workload list (0: plain FP64
+# chain, 1: free fermions, 2: mixed-length batch, 3: 2-D lattice, 4: GMN) and
+# prints one JSON line for it; the default run (no --config) is the headline
+# L = 24 metric above.
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def _oracle_pool(fn, items, threads):
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(fn, items))
+    return res, time.perf_counter() - t0
+
+
+def config0():
+    """L = 12 open chain, FP64, p = 0.2, 24 layers, 200 trajectories from seed 0;
+    per-layer half-chain S_vN, S_2 and TMI (A..D = 3 qubits)."""
+    import mipt_gb300 as mg
+    from oracle import pyoracle as orc
+    n, periods, count = 12, 12, 200
+    seeds = np.array([mg.trajectory_seed(0, i) for i in range(count)], np.uint64)
+    b = mg.Batch(n, periods, capacity=count, closed=False, fp64=True, observables=15, observe_every=1)
+    b.run(seeds, 0.2)
+    out, dt = _timed(lambda: b.run(seeds, 0.2))
+    units = count * 2 * periods
+    ref = orc.run_trajectory(int(seeds[0]), n, periods, 0.2, False, 16, 15, 1)
+    ds = float(np.nanmax(np.abs(out["obs"][0] - ref["obs"])))
+    threads = orc.max_threads()
+    sample = list(seeds[:threads])
+    _, cdt = _oracle_pool(lambda sd: orc.run_trajectory(int(sd), n, periods, 0.2, False, 16, 15, 1), sample, threads)
+    return {"config": "0: L=12 open chain, FP64, p=0.2, 24 layers, 200 trajectories, per-layer S_vN/S_2/TMI",
+            "value": units / dt, "unit": UNIT, "e2e_includes": "host sampling, upload, all layers, fetch",
+            "max_abs_dS_vs_oracle": ds,
+            "cpu_baseline": {"value": len(sample) * 2 * periods / cdt, "unit": UNIT, "cores": threads,
+                             "kind": "port", "sample": f"{len(sample)} trajectories, same observables"}}
+
+
+def config1():
+    """Free-fermion covariance, N = 128, depth 256, 500 trajectories per p in
+    {0.1, 0.2, 0.3}; entropies of every block [0, l) and TMI of the quarters."""
+    import mipt_gb300 as mg
+    from oracle import pyoracle as orc
+    N, depth, per_p = 128, 256, 500
+    ps = np.repeat([0.1, 0.2, 0.3], per_p)
+    seeds = np.array([mg.trajectory_seed(1, i) for i in range(len(ps))], np.uint64)
+    blocks = list(range(1, N + 1))
+    mg.ff_run(seeds[:8], ps[:8], N, depth, blocks=blocks)
+    out, dt = _timed(lambda: mg.ff_run(seeds, ps, N, depth, blocks=blocks))
+    ref = orc.ff_trajectory(int(seeds[0]), N, depth, float(ps[0]), True, 64, blocks=blocks, want_gamma=False)
+    ds = float(np.max(np.abs(out["s_blocks"][0] - ref["s_blocks"])))
+    threads = orc.max_threads()
+    sample = list(range(threads))
+    _, cdt = _oracle_pool(lambda i: orc.ff_trajectory(int(seeds[i]), N, depth, float(ps[i]), True, 64,
+                                                       blocks=blocks, want_gamma=False), sample, threads)
+    return {"config": "1: free fermions N=128 (256 Majoranas), depth 256, 1500 trajectories, all prefix blocks + TMI",
+            "value": len(ps) * depth / dt, "unit": UNIT, "max_abs_dS_vs_oracle_traj0": ds,
+            "cpu_baseline": {"value": len(sample) * depth / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{len(sample)} trajectories, FP64 oracle"}}
+
+
+def config2():
+    """4096 trajectories, L uniform on {16, 18, 20, 22}, p from 16 values in
+    [0.05, 0.35], periodic, depth 2L, FP32; per-layer half-chain S_2 and (L a
+    multiple of 4) TMI of the quarters from S_2. Each length runs as one batch."""
+    import mipt_gb300 as mg
+    rng = np.random.default_rng(2)
+    total = 4096
+    Ls = rng.choice([16, 18, 20, 22], size=total)
+    ps = P_GRID[rng.integers(0, 16, size=total)]
+    seeds = np.array([mg.trajectory_seed(2, i) for i in range(total)], np.uint64)
+    groups = []
+    for L in (16, 18, 20, 22):
+        idx = np.nonzero(Ls == L)[0]
+        obs = mg.OBS_S2_HALF | (mg.OBS_TMI_S2 if L % 4 == 0 else 0)
+        groups.append((L, idx, mg.Batch(L, L, capacity=len(idx), fp64=False, observables=obs, observe_every=1)))
+    for L, idx, b in groups:
+        b.run(seeds[idx[:8]], ps[idx[:8]])
+    _, dt = _timed(lambda: [b.run(seeds[idx], ps[idx]) for L, idx, b in groups])
+    units = int(sum(2 * L * len(idx) for L, idx, b in groups))
+    # plain FP64 per-trajectory arm on a sample
+    plain_units, plain_t = 0, 0.0
+    for L in (16, 22):
+        pb = mg.Batch(L, L, capacity=1, fp64=True, observables=mg.OBS_S2_HALF | (mg.OBS_TMI_S2 if L % 4 == 0 else 0),
+                      observe_every=1)
+        i = int(np.nonzero(Ls == L)[0][0])
+        pb.run(seeds[i:i + 1], ps[i:i + 1])
+        _, t = _timed(lambda: pb.run(seeds[i:i + 1], ps[i:i + 1]))
+        plain_units += 2 * L
+        plain_t += t
+        pb.close()
+    return {"config": "2: 4096 trajectories, L uniform on {16,18,20,22}, depth 2L, FP32, per-layer S_2 (+TMI_S2 for L%4==0)",
+            "value": units / dt, "unit": UNIT, "trajectory_layers": units,
+            "plain_fp64_per_trajectory": {"value": plain_units / plain_t, "unit": UNIT,
+                                          "sample": "one L=16 and one L=22 trajectory"},
+            "speedup_vs_plain_fp64": (units / dt) / (plain_units / plain_t)}
+
+
+def config3():
+    """4 x 7 lattice (L = 28, FP32, 2 GiB), p = 0.15, depth 56; per layer
+    half-system S_2 (16384 x 16384 Gram on the tensor cores), S_vN of the first
+    two rows (8 qubits) and three rho3 blocks."""
+    import mipt_gb300 as mg
+    X, Y, periods = 4, 7, 28
+    b = mg.Batch(X * Y, periods, capacity=1, fp64=False, observables=mg.OBS_S2_HALF, observe_every=1, rho3=True,
+                 lattice=(X, Y))
+    b.add_region(list(range(8)), 1)
+    b.set_rho3_subsystems([[0, 1, 2], [0, 4, 8], [5, 6, 9]])
+    seed = np.array([mg.trajectory_seed(3, 0)], np.uint64)
+    b.set_profiling(True)
+    out, dt = _timed(lambda: b.run(seed, 0.15))
+    stats = b.kernel_stats()
+    return {"config": "3: 4x7 lattice L=28 FP32, p=0.15, depth 56, per-layer S_2(half)+S_vN(8 qubits)+3 rho3",
+            "value": 2 * periods / dt, "unit": UNIT, "seconds_per_trajectory": dt,
+            "kernel_ms": {k: v[0] for k, v in stats.items()}, "final_half_S2": float(out["obs"][0, -1, 1])}
+
+
+def config4():
+    """65,536 rho3 blocks: half from L = 16 trajectories (final ring triples,
+    p in [0.05, 0.35]), half GHZ/W/product mixtures with white noise; batched
+    GMN to a certified gap of 1e-6 (FP32 ADMM, FP64 certificates), cold and
+    with the learned warm start."""
+    import mipt_gb300 as mg
+    from mipt_gb300 import gmn_warm
+    from oracle import gmn as ogmn
+    b = mg.Batch(16, 16, capacity=2048, fp64=False, rho3=True)
+    rng = np.random.default_rng(4)
+    seeds = np.array([mg.trajectory_seed(4, i) for i in range(2048)], np.uint64)
+    r = b.run(seeds, rng.uniform(0.05, 0.35, size=2048))
+    traj = (r["rho3"].reshape(-1, 128)[:, 0::2] + 1j * r["rho3"].reshape(-1, 128)[:, 1::2]).reshape(-1, 8, 8)
+    rho = np.concatenate([traj, gmn_warm.mixtures(len(traj), 5)])
+    cold, dt = _timed(lambda: mg.gmn_solve(rho, gap_tol=1e-6, max_iter=3000, check_every=10))
+    ok = cold["iters"] > 0
+    train = gmn_warm.mixtures(24000, 6)
+    x, t, _ = gmn_warm.solve_pairs(train, gap_tol=1e-6, max_iter=3000)
+    model = gmn_warm.WarmStartModel(seed=0)
+    (_, tdt) = _timed(lambda: model.fit(x, t))
+    guess = model.predict(rho)
+    warm, wdt = _timed(lambda: mg.gmn_solve(rho, warm_start=guess, gap_tol=1e-6, max_iter=3000, check_every=10))
+    both = ok & (warm["iters"] > 0)
+    sample = list(range(0, len(rho), len(rho) // 16))
+    _, cdt = _oracle_pool(lambda i: ogmn.solve(rho[i], gap_tol=1e-6, max_iter=3000), sample, 16)
+    return {"config": "4: 65536 rho3 (half L=16 trajectories, half GHZ/W/product mixtures), GMN to gap 1e-6",
+            "value": len(rho) / dt, "unit": "SDPs/s (cold start, incl. uncertified at 3000 iterations)",
+            "certified_fraction": float(ok.mean()),
+            "certified_fraction_trajectory_states": float(ok[:len(traj)].mean()),
+            "certified_fraction_mixtures": float(ok[len(traj):].mean()),
+            "mean_iterations_certified": float(cold["iters"][ok].mean()),
+            "warm_start": {"value": len(rho) / wdt, "certified_fraction": float((warm["iters"] > 0).mean()),
+                           "iterations_on_states_both_certify": [float(cold["iters"][both].mean()),
+                                                                 float(warm["iters"][both].mean())],
+                           "train_pairs": int(len(x)), "train_seconds": tdt},
+            "cpu_baseline": {"value": len(sample) / cdt, "unit": "SDPs/s", "cores": 16, "kind": "port",
+                             "sample": f"{len(sample)} states, FP64 ADMM oracle (the reference uses MOSEK, absent)"}}
+
+
+def run_config(k):
+    import torch
+    torch.cuda.set_device(0)
+    fn = [config0, config1, config2, config3, config4][k]
+    line = fn()
+    line["data"] = "synthetic"
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -298,7 +471,10 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tile", type=int, default=0, help="local qubits per pass tile (0 = library default)")
+    ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..4 instead")
     args = ap.parse_args()
+    if args.config >= 0:
+        return run_config(args.config)
     if args.impl == "reference":
         return run_reference(args)
     return run_gb300(args)
