@@ -229,6 +229,7 @@ struct GmnArrays
     void *W, *Q;       // [P][64], [P][3][64] (latest x-step)
     const double *sigma;
     const int *done;
+    float *res; // FP32 residual of each state's last iteration
 };
 
 template <typename Real>
@@ -253,8 +254,12 @@ __global__ void __launch_bounds__(kThreads) k_gmn_iterate(GmnArrays a, int iters
     C2<Real> *Wg = static_cast<C2<Real> *>(a.W) + static_cast<std::size_t>(prob) * 64;
     C2<Real> *Qg = static_cast<C2<Real> *>(a.Q) + static_cast<std::size_t>(prob) * 192;
     const Real two_over_sigma = Real(2) / sigma;
+    // Residual of the launch's last iteration: |dYh|^2 + |dZh|^2 (primal) plus
+    // sigma^2 (|dU|^2 + |dV|^2) (dual), over this lane's column.
+    float resid = 0.f;
     for (int it = 0; it < iters; ++it)
     {
+        const bool last = it + 1 == iters;
         // x-step: W column c.
 #pragma unroll
         for (int r = 0; r < 8; ++r)
@@ -302,6 +307,13 @@ __global__ void __launch_bounds__(kThreads) k_gmn_iterate(GmnArrays a, int iters
 #pragma unroll
             for (int r = 0; r < 8; ++r)
             {
+                if (last)
+                {
+                    const C2<Real> dy = csub(csub(X0[r], X[r]), Yh[o + c * 8 + r]);
+                    const C2<Real> du = csub(X[r], U[o + c * 8 + r]);
+                    resid += float(dy.re * dy.re + dy.im * dy.im) +
+                             float(sigma * sigma * (du.re * du.re + du.im * du.im));
+                }
                 U[o + c * 8 + r] = X[r];
                 Yh[o + c * 8 + r] = csub(X0[r], X[r]);
             }
@@ -316,6 +328,13 @@ __global__ void __launch_bounds__(kThreads) k_gmn_iterate(GmnArrays a, int iters
 #pragma unroll
             for (int r = 0; r < 8; ++r)
             {
+                if (last)
+                {
+                    const C2<Real> dz = csub(csub(X0[r], X[r]), Zh[o + c * 8 + r]);
+                    const C2<Real> dv = csub(X[r], V[o + c * 8 + r]);
+                    resid += float(dz.re * dz.re + dz.im * dz.im) +
+                             float(sigma * sigma * (dv.re * dv.re + dv.im * dv.im));
+                }
                 V[o + c * 8 + r] = X[r];
                 Zh[o + c * 8 + r] = csub(X0[r], X[r]);
             }
@@ -329,6 +348,8 @@ __global__ void __launch_bounds__(kThreads) k_gmn_iterate(GmnArrays a, int iters
 #pragma unroll
         for (int m = 0; m < 3; ++m) Qg[m * 64 + c * 8 + r] = sQ[g][m][c * 8 + r];
     }
+    for (int off = 4; off > 0; off /= 2) resid += __shfl_xor_sync(gmask, resid, off);
+    if (c == 0) a.res[prob] = sqrtf(resid);
 }
 
 // Sum over the 8 lanes of a group.
@@ -356,6 +377,14 @@ struct GmnCheck
     double gap_tol, feas_tol;
     double *primal, *dual, *gap, *infeas, *gmn;
     int *remaining;
+    // FP64 certificates are computed for candidates only: states whose FP32
+    // residual is at most cand_tol and whose back-off has expired (after a
+    // failed candidate check the next one waits 2, then 4 check intervals).
+    const float *res;
+    float cand_tol;
+    int *next_check, *backoff;
+    int check_every;
+    int force; // certify every remaining state (final pass)
 };
 
 // Spectrum of the group's Hermitian matrix (FP64), lane c returns eigenvalue c.
@@ -373,6 +402,11 @@ template <typename Real> __global__ void __launch_bounds__(kThreads) k_gmn_check
     const int lane = threadIdx.x & 31, gbase = lane & ~7;
     const unsigned gmask = 0xFFu << gbase;
     if (prob >= k.count || k.done[prob]) return;
+    if (!k.force && (k.res[prob] > k.cand_tol || k.iter_now < k.next_check[prob]))
+    {
+        if (c == 0) atomicAdd(k.remaining, 1);
+        return;
+    }
     const double sigma = k.sigma[prob];
     const double2 *rho = k.rho64 + static_cast<std::size_t>(prob) * 64;
     const C2<Real> *W = static_cast<const C2<Real> *>(k.W) + static_cast<std::size_t>(prob) * 64;
@@ -429,9 +463,16 @@ template <typename Real> __global__ void __launch_bounds__(kThreads) k_gmn_check
         k.gmn[prob] = v > 1e-8 ? v : 0.0;
         k.iters[prob] = k.iter_now;
         if (fabs(gp) <= k.gap_tol && feas <= k.feas_tol)
+        {
             k.done[prob] = 1;
+        }
         else
+        {
             atomicAdd(k.remaining, 1);
+            const int b = min(2 * max(k.backoff[prob], 1), 4);
+            k.backoff[prob] = b;
+            k.next_check[prob] = k.iter_now + b * k.check_every;
+        }
     }
 }
 
@@ -514,7 +555,7 @@ int gmn_solve(const mipt_gb300_gmn_config &cfg, const double *h_rho, int count, 
               double *h_gap, int *h_iters, double *h_solution)
 {
     const std::size_t P = static_cast<std::size_t>(count), M = sizeof(C2<Real>) * 64;
-    DevMem rho_in, rho, rho64, U, V, Yh, Zh, W, Q, sig, done, iters, outs, rem, guess;
+    DevMem rho_in, rho, rho64, U, V, Yh, Zh, W, Q, sig, done, iters, outs, rem, guess, res, nextc, boff;
     GMN_CUDA(rho_in.ensure(P * 128 * sizeof(double)));
     GMN_CUDA(rho.ensure(P * M));
     GMN_CUDA(rho64.ensure(P * 64 * sizeof(double2)));
@@ -525,6 +566,11 @@ int gmn_solve(const mipt_gb300_gmn_config &cfg, const double *h_rho, int count, 
     GMN_CUDA(iters.ensure(P * sizeof(int)));
     GMN_CUDA(outs.ensure(P * 5 * sizeof(double)));
     GMN_CUDA(rem.ensure(sizeof(int)));
+    GMN_CUDA(res.ensure(P * sizeof(float)));
+    GMN_CUDA(nextc.ensure(P * sizeof(int)));
+    GMN_CUDA(boff.ensure(P * sizeof(int)));
+    GMN_CUDA(cudaMemset(nextc.p, 0, P * sizeof(int)));
+    GMN_CUDA(cudaMemset(boff.p, 0, P * sizeof(int)));
     GMN_CUDA(cudaMemcpy(rho_in.p, h_rho, P * 128 * sizeof(double), cudaMemcpyHostToDevice));
     const int lb = static_cast<int>((P * 64 + 255) / 256);
     k_gmn_load<Real><<<lb, 256>>>(count, static_cast<const double *>(rho_in.p), static_cast<C2<Real> *>(rho.p),
@@ -544,11 +590,13 @@ int gmn_solve(const mipt_gb300_gmn_config &cfg, const double *h_rho, int count, 
     }
     GMN_CUDA(cudaGetLastError());
     GmnArrays a{count, rho.p, U.p, V.p, Yh.p, Zh.p, W.p, Q.p, static_cast<const double *>(sig.p),
-                static_cast<const int *>(done.p)};
+                static_cast<const int *>(done.p), static_cast<float *>(res.p)};
     double *o = static_cast<double *>(outs.p);
     GmnCheck k{count, rho.p, static_cast<const double2 *>(rho64.p), W.p, Q.p, Zh.p,
                static_cast<const double *>(sig.p), static_cast<int *>(done.p), static_cast<int *>(iters.p), 0,
-               cfg.gap_tol, cfg.feas_tol, o, o + P, o + 2 * P, o + 3 * P, o + 4 * P, static_cast<int *>(rem.p)};
+               cfg.gap_tol, cfg.feas_tol, o, o + P, o + 2 * P, o + 3 * P, o + 4 * P, static_cast<int *>(rem.p),
+               static_cast<const float *>(res.p), static_cast<float>(30.0 * std::max(cfg.gap_tol, cfg.feas_tol)),
+               static_cast<int *>(nextc.p), static_cast<int *>(boff.p), std::max(1, cfg.check_every), 0};
     const int blocks = static_cast<int>((P + kProbPerBlock - 1) / kProbPerBlock);
     const int every = std::max(1, cfg.check_every);
     int it = 0;
@@ -567,16 +615,23 @@ int gmn_solve(const mipt_gb300_gmn_config &cfg, const double *h_rho, int count, 
         int remaining = 0;
         GMN_CUDA(cudaMemcpy(&remaining, rem.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (remaining == 0) break;
+        if (it >= cfg.max_iter)
+        {
+            // Last pass: bounds for every state still uncertified.
+            k.force = 1;
+            k_gmn_check<Real><<<blocks, kThreads>>>(k);
+            GMN_CUDA(cudaGetLastError());
+        }
     }
-    std::vector<double> res(P * 5);
-    GMN_CUDA(cudaMemcpy(res.data(), outs.p, res.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double> hres(P * 5);
+    GMN_CUDA(cudaMemcpy(hres.data(), outs.p, hres.size() * sizeof(double), cudaMemcpyDeviceToHost));
     std::vector<int> its(P), dn(P);
     GMN_CUDA(cudaMemcpy(its.data(), iters.p, P * sizeof(int), cudaMemcpyDeviceToHost));
     GMN_CUDA(cudaMemcpy(dn.data(), done.p, P * sizeof(int), cudaMemcpyDeviceToHost));
     for (std::size_t i = 0; i < P; ++i)
     {
-        if (h_gmn) h_gmn[i] = res[4 * P + i];
-        if (h_gap) h_gap[i] = res[2 * P + i];
+        if (h_gmn) h_gmn[i] = hres[4 * P + i];
+        if (h_gap) h_gap[i] = hres[2 * P + i];
         if (h_iters) h_iters[i] = dn[i] ? its[i] : -its[i];
     }
     if (h_solution)
