@@ -293,6 +293,91 @@ __device__ void value_histogram(const T *val, int k, const int *lm, int m_loc, d
     }
 }
 
+// Born histogram of an FP32 tile straight from the registers of the pass's
+// last round, in a fixed order: squared magnitudes are folded over the
+// unmeasured register bits (pairwise FP32 adds), then over the unmeasured lane
+// bits (xor shuffles), then summed over the unmeasured warp bits through
+// shared memory `S` (2^k floats, warp-major, lanes innermost); out[bin] as in value_histogram. `mmask` is
+// the measured set in tile positions, lm[0..m_loc) its positions in ascending
+// order (bin bit i <-> lm[i]). A pairwise tree of depth <= k in FP32 bounds
+// the relative rounding error of a bin by k * 2^-24, below the reference's
+// sequential FP32 runs of 64 (cpp/include/mipt/cuda/reduce_sweep.cuh:59-96);
+// only the per-bin result is widened to FP64.
+template <int RB>
+__device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round &Z, int TB, std::uint32_t mmask,
+                                   const int *lm, int m_loc, float *S, int *hs, double *out)
+{
+    constexpr int NA = 1 << RB;
+    const int tid = threadIdx.x;
+    const int nl = TB < 5 ? TB : 5;
+    const int LW = 1 << nl; // lanes per warp
+    const unsigned lanes = TB >= 5 ? 0xffffffffu : ((1u << LW) - 1u);
+    float p[NA];
+#pragma unroll
+    for (int r = 0; r < NA; ++r) p[r] = norm2(amp[r]);
+    unsigned um_reg = 0;
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+        if (!((mmask >> Z.reg[i]) & 1u)) um_reg |= 1u << i;
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+        if ((um_reg >> i) & 1u)
+        {
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+                if (!((r >> i) & 1)) p[r] += p[r | (1 << i)];
+        }
+#pragma unroll
+    for (int b = 0; b < 5; ++b)
+        if (b < nl && !((mmask >> Z.tid[b]) & 1u))
+        {
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+                if ((r & um_reg) == 0) p[r] += __shfl_xor_sync(lanes, p[r], 1 << b);
+        }
+    __syncthreads(); // the tile buffer is free
+    const int w = tid >> 5, lane = tid & 31;
+#pragma unroll
+    for (int r = 0; r < NA; ++r)
+        if ((r & um_reg) == 0) S[(w * NA + r) * LW + lane] = p[r];
+    if (tid == 0)
+    {
+        // hs[i], i < m_loc: offset in S of bin bit i; hs[16 + t]: offset of
+        // the t-th unmeasured warp bit; hs[31]: their count.
+        int uw = 0;
+        for (int i = 0; i < m_loc; ++i)
+        {
+            const int q = lm[i];
+            int st = 0;
+            for (int j = 0; j < RB; ++j)
+                if (Z.reg[j] == q) st = (1 << j) * LW;
+            for (int j = 0; j < TB; ++j)
+                if (Z.tid[j] == q) st = j < nl ? (1 << j) : (1 << (j - nl)) * NA * LW;
+            hs[i] = st;
+        }
+        for (int j = nl; j < TB; ++j)
+            if (!((mmask >> Z.tid[j]) & 1u)) hs[16 + uw++] = (1 << (j - nl)) * NA * LW;
+        hs[31] = uw;
+    }
+    __syncthreads();
+    const int uw = hs[31];
+    for (int bin = tid; bin < (1 << m_loc); bin += blockDim.x)
+    {
+        int off = 0;
+        for (int i = 0; i < m_loc; ++i)
+            if ((bin >> i) & 1) off += hs[i];
+        float s = 0.f;
+        for (int c = 0; c < (1 << uw); ++c)
+        {
+            int o = off;
+            for (int t = 0; t < uw; ++t)
+                if ((c >> t) & 1) o += hs[16 + t];
+            s += S[o];
+        }
+        out[bin] = static_cast<double>(s);
+    }
+}
+
 // Position of tile bit p once tile bit x is removed (CTA-local offset).
 __device__ __forceinline__ int opos_d(int p, int x) { return p > x ? p - 1 : p; }
 
@@ -389,151 +474,212 @@ __device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real
     apply_slot<S>(a, Us);
 }
 
+// Start offsets of co-resident pass CTAs, one counter per SM (see
+// k_pass_rounds): the parity of the value a CTA draws picks its phase.
+__device__ unsigned g_pass_sm_slot[1024];
+
 // One tiled pass with register rounds: global -> registers (lanes on the
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
+// Work items are (trajectory, tile) pairs, item = trajectory * 2^n_nl + tile;
+// the CTA at flat index c runs items c, c + C, ... with C the number of CTAs,
+// so one launch shape serves both one item per CTA (C = items) and a
+// persistent grid. With `stagger_ns` > 0 every second CTA that starts on an SM
+// first waits that long: two resident CTAs then work out of phase, one
+// streaming its tile while the other is in its gate rounds.
 template <typename Real, int RB>
 __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
-                  int fuse_hist, int packed)
+                  int fuse_hist, int packed, int batch, int stagger_ns)
 {
     constexpr int NA = 1 << RB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
     __shared__ Cx<Real> U[kMaxPassGates][16];
     __shared__ double red[8];
+    __shared__ unsigned phase;
 
     const PassGeom &g = P.geom;
     const int TB = g.k - RB;
     const int tid = threadIdx.x;
-    const int b = blockIdx.y;
-    const std::uint64_t tix = blockIdx.x;
-    Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
-    const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
-    for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
-        U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
-    Collapse cl{0, 0, 1.0, 0.0};
-    const bool has_col = col_in != nullptr;
-    if (has_col) cl = col_in[b * col_stride];
-    const Real scale = static_cast<Real>(cl.scale);
-
-    Cx<Real> amp[NA];
+    if (stagger_ns > 0)
     {
-        const Round &R = P.round[0];
-        std::uint64_t gt = base;
-        for (int i = 0; i < TB; ++i)
-            if ((tid >> i) & 1) gt |= 1ull << g.pos[R.tid[i]];
-        std::uint64_t gr[RB];
-#pragma unroll
-        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[R.reg[i]];
-#pragma unroll
-        for (int r = 0; r < NA; ++r)
+        if (tid == 0)
         {
-            std::uint64_t gi = gt;
-#pragma unroll
-            for (int i = 0; i < RB; ++i)
-                if ((r >> i) & 1) gi |= gr[i];
-            Cx<Real> v = psi[gi];
-            if (has_col) v = collapse_value(v, gi, cl, scale);
-            amp[r] = v;
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            phase = atomicAdd(&g_pass_sm_slot[smid & 1023u], 1u) & 1u;
+        }
+        __syncthreads();
+        if (phase)
+        {
+            std::uint64_t t0, t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+            for (int it = 0; it < 100000; ++it) // at most ~0.1 s whatever the timer does
+            {
+                __nanosleep(256);
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+                if (t - t0 >= static_cast<std::uint64_t>(stagger_ns)) break;
+            }
         }
     }
-    __syncthreads(); // gate matrices visible
-
-    for (int ri = 0; ri < P.rounds; ++ri)
+    const std::uint64_t items = static_cast<std::uint64_t>(batch) << g.n_nl;
+    const std::uint64_t step = static_cast<std::uint64_t>(gridDim.x) * gridDim.y;
+    int cur_b = -1;
+    for (std::uint64_t item = static_cast<std::uint64_t>(blockIdx.y) * gridDim.x + blockIdx.x; item < items;
+         item += step)
     {
-        const Round &R = P.round[ri];
-        if (ri > 0)
+        const int b = static_cast<int>(item >> g.n_nl);
+        const std::uint64_t tix = item & ((1ull << g.n_nl) - 1);
+        __syncthreads(); // the previous item's shared-memory reads are complete
+        Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
+        const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+        if (b != cur_b)
+            for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
+                U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
+        cur_b = b;
+        Collapse cl{0, 0, 1.0, 0.0};
+        const bool has_col = col_in != nullptr;
+        if (has_col) cl = col_in[b * col_stride];
+        const Real scale = static_cast<Real>(cl.scale);
+
+        Cx<Real> amp[NA];
         {
-            const Round &A = P.round[ri - 1];
-            std::uint32_t sa = 0, sb = 0;
+            const Round &R = P.round[0];
+            std::uint64_t gt = base;
             for (int i = 0; i < TB; ++i)
-                if ((tid >> i) & 1)
+                if ((tid >> i) & 1) gt |= 1ull << g.pos[R.tid[i]];
+            std::uint64_t gr[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[R.reg[i]];
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint64_t gi = gt;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) gi |= gr[i];
+                Cx<Real> v = psi[gi];
+                if (has_col) v = collapse_value(v, gi, cl, scale);
+                amp[r] = v;
+            }
+        }
+        __syncthreads(); // gate matrices visible
+
+        for (int ri = 0; ri < P.rounds; ++ri)
+        {
+            const Round &R = P.round[ri];
+            if (ri > 0)
+            {
+                const Round &A = P.round[ri - 1];
+                std::uint32_t sa = 0, sb = 0;
+                for (int i = 0; i < TB; ++i)
+                    if ((tid >> i) & 1)
+                    {
+                        sa ^= swz1(A.tid[i]);
+                        sb ^= swz1(R.tid[i]);
+                    }
+                std::uint32_t ra[RB], rb_[RB];
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
                 {
-                    sa ^= swz1(A.tid[i]);
-                    sb ^= swz1(R.tid[i]);
+                    ra[i] = swz1(A.reg[i]);
+                    rb_[i] = swz1(R.reg[i]);
                 }
-            std::uint32_t ra[RB], rb_[RB];
+                if (ri > 1) __syncthreads(); // previous round's reads are complete
 #pragma unroll
-            for (int i = 0; i < RB; ++i)
-            {
-                ra[i] = swz1(A.reg[i]);
-                rb_[i] = swz1(R.reg[i]);
+                for (int r = 0; r < NA; ++r)
+                {
+                    std::uint32_t p = sa;
+#pragma unroll
+                    for (int i = 0; i < RB; ++i)
+                        if ((r >> i) & 1) p ^= ra[i];
+                    tile[p] = amp[r];
+                }
+                __syncthreads();
+#pragma unroll
+                for (int r = 0; r < NA; ++r)
+                {
+                    std::uint32_t p = sb;
+#pragma unroll
+                    for (int i = 0; i < RB; ++i)
+                        if ((r >> i) & 1) p ^= rb_[i];
+                    amp[r] = tile[p];
+                }
             }
-            if (ri > 1) __syncthreads(); // previous round's reads are complete
-#pragma unroll
-            for (int r = 0; r < NA; ++r)
-            {
-                std::uint32_t p = sa;
-#pragma unroll
-                for (int i = 0; i < RB; ++i)
-                    if ((r >> i) & 1) p ^= ra[i];
-                tile[p] = amp[r];
-            }
-            __syncthreads();
-#pragma unroll
-            for (int r = 0; r < NA; ++r)
-            {
-                std::uint32_t p = sb;
-#pragma unroll
-                for (int i = 0; i < RB; ++i)
-                    if ((r >> i) & 1) p ^= rb_[i];
-                amp[r] = tile[p];
-            }
+            if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+            if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
+            if (RB >= 6 && R.slot[2] >= 0) apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
         }
-        if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
-        if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
-        if (RB >= 6 && R.slot[2] >= 0) apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
-    }
 
-    const Round &Z = P.round[P.rounds - 1];
-    {
-        std::uint64_t gt = base;
-        for (int i = 0; i < TB; ++i)
-            if ((tid >> i) & 1) gt |= 1ull << g.pos[Z.tid[i]];
-        std::uint64_t gr[RB];
-#pragma unroll
-        for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[Z.reg[i]];
-#pragma unroll
-        for (int r = 0; r < NA; ++r)
+        const Round &Z = P.round[P.rounds - 1];
         {
-            std::uint64_t gi = gt;
-#pragma unroll
-            for (int i = 0; i < RB; ++i)
-                if ((r >> i) & 1) gi |= gr[i];
-            psi[gi] = amp[r];
-        }
-    }
-
-    if (fuse_hist)
-    {
-        const LayerMeas &M = meas[b * meas_stride];
-        if (M.nchunks > 0)
-        {
-            __syncthreads(); // the tile buffer is free
-            Real *val = reinterpret_cast<Real *>(smem_raw);
-            std::uint32_t jt = 0;
+            std::uint64_t gt = base;
             for (int i = 0; i < TB; ++i)
-                if ((tid >> i) & 1) jt |= 1u << Z.tid[i];
+                if ((tid >> i) & 1) gt |= 1ull << g.pos[Z.tid[i]];
+            std::uint64_t gr[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i) gr[i] = 1ull << g.pos[Z.reg[i]];
 #pragma unroll
             for (int r = 0; r < NA; ++r)
             {
-                std::uint32_t j = jt;
+                std::uint64_t gi = gt;
 #pragma unroll
                 for (int i = 0; i < RB; ++i)
-                    if ((r >> i) & 1) j |= 1u << Z.reg[i];
-                val[j] = norm2(amp[r]);
+                    if ((r >> i) & 1) gi |= gr[i];
+                psi[gi] = amp[r];
             }
-            __syncthreads();
-            const std::uint64_t chunk = M.chunk[0];
-            int lm[kMaxLocal + 1];
-            int m_loc = 0;
-            for (int i = 0; i < g.k; ++i)
-                if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
-            double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
-            value_histogram(val, g.k, lm, m_loc, part, red);
+        }
+
+        if (fuse_hist)
+        {
+            const LayerMeas &M = meas[b * meas_stride];
+            if constexpr (sizeof(Real) == 4)
+            {
+                if (M.nchunks > 0)
+                {
+                    __shared__ int hs[32];
+                    const std::uint64_t chunk = M.chunk[0];
+                    int lm[kMaxLocal + 1];
+                    int m_loc = 0;
+                    std::uint32_t mmask = 0;
+                    for (int i = 0; i < g.k; ++i)
+                        if ((chunk >> g.pos[i]) & 1ull)
+                        {
+                            lm[m_loc++] = i;
+                            mmask |= 1u << i;
+                        }
+                    double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+                    register_histogram<RB>(amp, Z, TB, mmask, lm, m_loc, reinterpret_cast<float *>(smem_raw), hs, part);
+                }
+            }
+            else if (M.nchunks > 0)
+            {
+                __syncthreads(); // the tile buffer is free
+                Real *val = reinterpret_cast<Real *>(smem_raw);
+                std::uint32_t jt = 0;
+                for (int i = 0; i < TB; ++i)
+                    if ((tid >> i) & 1) jt |= 1u << Z.tid[i];
+#pragma unroll
+                for (int r = 0; r < NA; ++r)
+                {
+                    std::uint32_t j = jt;
+#pragma unroll
+                    for (int i = 0; i < RB; ++i)
+                        if ((r >> i) & 1) j |= 1u << Z.reg[i];
+                    val[j] = norm2(amp[r]);
+                }
+                __syncthreads();
+                const std::uint64_t chunk = M.chunk[0];
+                int lm[kMaxLocal + 1];
+                int m_loc = 0;
+                for (int i = 0; i < g.k; ++i)
+                    if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
+                double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+                value_histogram(val, g.k, lm, m_loc, part, red);
+            }
         }
     }
 }
@@ -972,6 +1118,46 @@ bool use_packed_fma()
         return !(v && v[0] == '0');
     }();
     return on;
+}
+
+// MIPT_GB300_PERSISTENT_PASS=1 runs the register-round pass on a persistent
+// grid (resident CTAs loop over the (trajectory, tile) items);
+// MIPT_GB300_PASS_STAGGER_NS sets the start offset of every second CTA on an
+// SM in that mode.
+bool use_persistent_pass()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_PERSISTENT_PASS");
+        return v && v[0] == '1';
+    }();
+    return on;
+}
+
+int pass_stagger_ns()
+{
+    static const int ns = [] {
+        const char *v = std::getenv("MIPT_GB300_PASS_STAGGER_NS");
+        return v ? std::max(0, std::min(1000000, std::atoi(v))) : 0;
+    }();
+    return ns;
+}
+
+// Launch grid of a register-round pass: one CTA per (tile, trajectory) item,
+// or, in persistent mode, as many CTAs as fit on the device at once.
+dim3 pass_grid(const void *fn, int threads, std::size_t smem, dim3 items)
+{
+    if (!use_persistent_pass()) return items;
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess || per_sm < 1)
+    {
+        cudaGetLastError();
+        return items;
+    }
+    const std::uint64_t total = static_cast<std::uint64_t>(items.x) * items.y;
+    const std::uint64_t resident = static_cast<std::uint64_t>(sms) * per_sm;
+    return dim3(static_cast<unsigned>(std::min(total, resident)), 1, 1);
 }
 
 int grid_for(std::uint64_t total, int threads)
@@ -1532,20 +1718,26 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
         {
             if (plan.rb == 6)
             {
-                cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, 6>), smem);
+                const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, 6>);
+                cudaError_t e = ensure_smem_attr<Real>(fn, smem);
                 if (e != cudaSuccess) return e;
-                k_pass_rounds<Real, 6><<<grid, 1u << (plan.geom.k - 6), smem, s>>>(
+                const int threads = 1 << (plan.geom.k - 6);
+                const dim3 pgrid = pass_grid(fn, threads, smem, grid);
+                k_pass_rounds<Real, 6><<<pgrid, threads, smem, s>>>(
                     states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-                    fuse_hist, use_packed_fma() ? 1 : 0);
+                    fuse_hist, use_packed_fma() ? 1 : 0, batch, use_persistent_pass() ? pass_stagger_ns() : 0);
                 return cudaGetLastError();
             }
         }
         if (plan.rb != 5) return cudaErrorInvalidValue;
-        cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass_rounds<Real, 5>), smem);
+        const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, 5>);
+        cudaError_t e = ensure_smem_attr<Real>(fn, smem);
         if (e != cudaSuccess) return e;
-        k_pass_rounds<Real, 5><<<grid, 1u << (plan.geom.k - 5), smem, s>>>(
+        const int threads = 1 << (plan.geom.k - 5);
+        const dim3 pgrid = pass_grid(fn, threads, smem, grid);
+        k_pass_rounds<Real, 5><<<pgrid, threads, smem, s>>>(
             states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-            fuse_hist, use_packed_fma() ? 1 : 0);
+            fuse_hist, use_packed_fma() ? 1 : 0, batch, use_persistent_pass() ? pass_stagger_ns() : 0);
         return cudaGetLastError();
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
