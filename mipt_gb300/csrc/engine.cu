@@ -296,29 +296,36 @@ __device__ void value_histogram(const T *val, int k, const int *lm, int m_loc, d
 // Born histogram of an FP32 tile straight from the registers of the pass's
 // last round, in a fixed order: squared magnitudes are folded over the
 // unmeasured register bits (pairwise FP32 adds), then over the unmeasured lane
-// bits (xor shuffles), then summed over the unmeasured warp bits through
-// shared memory `S` (2^k floats, warp-major, lanes innermost); out[bin] as in value_histogram. `mmask` is
-// the measured set in tile positions, lm[0..m_loc) its positions in ascending
-// order (bin bit i <-> lm[i]). A pairwise tree of depth <= k in FP32 bounds
-// the relative rounding error of a bin by k * 2^-24, below the reference's
-// sequential FP32 runs of 64 (cpp/include/mipt/cuda/reduce_sweep.cuh:59-96);
-// only the per-bin result is widened to FP64.
+// bits (xor shuffles); each surviving value goes to S[w * 2^m_loc + bin], w
+// the rank of its warp among the warps that differ only in unmeasured bits,
+// and out[bin] = sum over w in order (value_histogram's result). `mmask` is
+// the measured set in tile positions (bin bit i <-> i-th measured position
+// from the bottom); S needs 2^k floats. A pairwise tree of depth <= k in FP32
+// bounds the relative rounding error of a bin by k * 2^-24, below the
+// reference's sequential FP32 runs of 64
+// (cpp/include/mipt/cuda/reduce_sweep.cuh:59-96); only the per-bin result is
+// widened to FP64.
 template <int RB>
 __device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round &Z, int TB, std::uint32_t mmask,
-                                   const int *lm, int m_loc, float *S, int *hs, double *out)
+                                   int m_loc, float *S, double *out)
 {
     constexpr int NA = 1 << RB;
     const int tid = threadIdx.x;
     const int nl = TB < 5 ? TB : 5;
-    const int LW = 1 << nl; // lanes per warp
-    const unsigned lanes = TB >= 5 ? 0xffffffffu : ((1u << LW) - 1u);
+    const unsigned lanes = TB >= 5 ? 0xffffffffu : ((1u << (1u << TB)) - 1u);
     float p[NA];
 #pragma unroll
     for (int r = 0; r < NA; ++r) p[r] = norm2(amp[r]);
+    // Register bits: unmeasured ones are folded; a measured one adds its bin bit.
     unsigned um_reg = 0;
+    std::uint32_t regbin[RB];
 #pragma unroll
     for (int i = 0; i < RB; ++i)
-        if (!((mmask >> Z.reg[i]) & 1u)) um_reg |= 1u << i;
+    {
+        const int q = Z.reg[i];
+        regbin[i] = ((mmask >> q) & 1u) ? 1u << __popc(mmask & ((1u << q) - 1u)) : 0u;
+        if (!((mmask >> q) & 1u)) um_reg |= 1u << i;
+    }
 #pragma unroll
     for (int i = 0; i < RB; ++i)
         if ((um_reg >> i) & 1u)
@@ -327,53 +334,54 @@ __device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round 
             for (int r = 0; r < NA; ++r)
                 if (!((r >> i) & 1)) p[r] += p[r | (1 << i)];
         }
+    // Thread bits: measured ones give the thread's bin bits, unmeasured lane
+    // bits are summed by shuffles, unmeasured warp bits index S's rows.
+    std::uint32_t tbin = 0, um_lane = 0, wrow = 0;
+    int uw = 0;
+    for (int j = 0; j < TB; ++j)
+    {
+        const int q = Z.tid[j];
+        const bool set = (tid >> j) & 1;
+        if ((mmask >> q) & 1u)
+        {
+            if (set) tbin |= 1u << __popc(mmask & ((1u << q) - 1u));
+        }
+        else if (j < nl)
+            um_lane |= 1u << j;
+        else
+        {
+            if (set) wrow |= 1u << uw;
+            ++uw;
+        }
+    }
 #pragma unroll
     for (int b = 0; b < 5; ++b)
-        if (b < nl && !((mmask >> Z.tid[b]) & 1u))
+        if ((um_lane >> b) & 1u)
         {
 #pragma unroll
             for (int r = 0; r < NA; ++r)
                 if ((r & um_reg) == 0) p[r] += __shfl_xor_sync(lanes, p[r], 1 << b);
         }
     __syncthreads(); // the tile buffer is free
-    const int w = tid >> 5, lane = tid & 31;
-#pragma unroll
-    for (int r = 0; r < NA; ++r)
-        if ((r & um_reg) == 0) S[(w * NA + r) * LW + lane] = p[r];
-    if (tid == 0)
+    if ((tid & um_lane) == 0)
     {
-        // hs[i], i < m_loc: offset in S of bin bit i; hs[16 + t]: offset of
-        // the t-th unmeasured warp bit; hs[31]: their count.
-        int uw = 0;
-        for (int i = 0; i < m_loc; ++i)
-        {
-            const int q = lm[i];
-            int st = 0;
-            for (int j = 0; j < RB; ++j)
-                if (Z.reg[j] == q) st = (1 << j) * LW;
-            for (int j = 0; j < TB; ++j)
-                if (Z.tid[j] == q) st = j < nl ? (1 << j) : (1 << (j - nl)) * NA * LW;
-            hs[i] = st;
-        }
-        for (int j = nl; j < TB; ++j)
-            if (!((mmask >> Z.tid[j]) & 1u)) hs[16 + uw++] = (1 << (j - nl)) * NA * LW;
-        hs[31] = uw;
+        float *row = S + (static_cast<std::size_t>(wrow) << m_loc);
+#pragma unroll
+        for (int r = 0; r < NA; ++r)
+            if ((r & um_reg) == 0)
+            {
+                std::uint32_t bin = tbin;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1) bin |= regbin[i];
+                row[bin] = p[r];
+            }
     }
     __syncthreads();
-    const int uw = hs[31];
     for (int bin = tid; bin < (1 << m_loc); bin += blockDim.x)
     {
-        int off = 0;
-        for (int i = 0; i < m_loc; ++i)
-            if ((bin >> i) & 1) off += hs[i];
         float s = 0.f;
-        for (int c = 0; c < (1 << uw); ++c)
-        {
-            int o = off;
-            for (int t = 0; t < uw; ++t)
-                if ((c >> t) & 1) o += hs[16 + t];
-            s += S[o];
-        }
+        for (int w = 0; w < (1 << uw); ++w) s += S[(static_cast<std::size_t>(w) << m_loc) + bin];
         out[bin] = static_cast<double>(s);
     }
 }
@@ -474,57 +482,29 @@ __device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real
     apply_slot<S>(a, Us);
 }
 
-// Start offsets of co-resident pass CTAs, one counter per SM (see
-// k_pass_rounds): the parity of the value a CTA draws picks its phase.
-__device__ unsigned g_pass_sm_slot[1024];
-
 // One tiled pass with register rounds: global -> registers (lanes on the
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
 // Work items are (trajectory, tile) pairs, item = trajectory * 2^n_nl + tile;
 // the CTA at flat index c runs items c, c + C, ... with C the number of CTAs,
 // so one launch shape serves both one item per CTA (C = items) and a
-// persistent grid. With `stagger_ns` > 0 every second CTA that starts on an SM
-// first waits that long: two resident CTAs then work out of phase, one
-// streaming its tile while the other is in its gate rounds.
+// persistent grid.
 template <typename Real, int RB>
 __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
-                  int fuse_hist, int packed, int batch, int stagger_ns)
+                  int fuse_hist, int packed, int batch)
 {
     constexpr int NA = 1 << RB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
     __shared__ Cx<Real> U[kMaxPassGates][16];
     __shared__ double red[8];
-    __shared__ unsigned phase;
 
     const PassGeom &g = P.geom;
     const int TB = g.k - RB;
     const int tid = threadIdx.x;
-    if (stagger_ns > 0)
-    {
-        if (tid == 0)
-        {
-            unsigned smid;
-            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-            phase = atomicAdd(&g_pass_sm_slot[smid & 1023u], 1u) & 1u;
-        }
-        __syncthreads();
-        if (phase)
-        {
-            std::uint64_t t0, t;
-            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-            for (int it = 0; it < 100000; ++it) // at most ~0.1 s whatever the timer does
-            {
-                __nanosleep(256);
-                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-                if (t - t0 >= static_cast<std::uint64_t>(stagger_ns)) break;
-            }
-        }
-    }
     const std::uint64_t items = static_cast<std::uint64_t>(batch) << g.n_nl;
     const std::uint64_t step = static_cast<std::uint64_t>(gridDim.x) * gridDim.y;
     int cur_b = -1;
@@ -640,19 +620,13 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
             {
                 if (M.nchunks > 0)
                 {
-                    __shared__ int hs[32];
                     const std::uint64_t chunk = M.chunk[0];
-                    int lm[kMaxLocal + 1];
-                    int m_loc = 0;
                     std::uint32_t mmask = 0;
                     for (int i = 0; i < g.k; ++i)
-                        if ((chunk >> g.pos[i]) & 1ull)
-                        {
-                            lm[m_loc++] = i;
-                            mmask |= 1u << i;
-                        }
+                        if ((chunk >> g.pos[i]) & 1ull) mmask |= 1u << i;
+                    const int m_loc = __popc(mmask);
                     double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
-                    register_histogram<RB>(amp, Z, TB, mmask, lm, m_loc, reinterpret_cast<float *>(smem_raw), hs, part);
+                    register_histogram<RB>(amp, Z, TB, mmask, m_loc, reinterpret_cast<float *>(smem_raw), part);
                 }
             }
             else if (M.nchunks > 0)
@@ -1120,26 +1094,16 @@ bool use_packed_fma()
     return on;
 }
 
-// MIPT_GB300_PERSISTENT_PASS=1 runs the register-round pass on a persistent
-// grid (resident CTAs loop over the (trajectory, tile) items);
-// MIPT_GB300_PASS_STAGGER_NS sets the start offset of every second CTA on an
-// SM in that mode.
+// The register-round pass runs on a persistent grid (resident CTAs loop over
+// the (trajectory, tile) items; measured 1.5 % faster at L=24 than one CTA per
+// item); MIPT_GB300_PERSISTENT_PASS=0 launches one CTA per item instead.
 bool use_persistent_pass()
 {
     static const bool on = [] {
         const char *v = std::getenv("MIPT_GB300_PERSISTENT_PASS");
-        return v && v[0] == '1';
+        return !(v && v[0] == '0');
     }();
     return on;
-}
-
-int pass_stagger_ns()
-{
-    static const int ns = [] {
-        const char *v = std::getenv("MIPT_GB300_PASS_STAGGER_NS");
-        return v ? std::max(0, std::min(1000000, std::atoi(v))) : 0;
-    }();
-    return ns;
 }
 
 // Launch grid of a register-round pass: one CTA per (tile, trajectory) item,
@@ -1725,7 +1689,7 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
                 const dim3 pgrid = pass_grid(fn, threads, smem, grid);
                 k_pass_rounds<Real, 6><<<pgrid, threads, smem, s>>>(
                     states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-                    fuse_hist, use_packed_fma() ? 1 : 0, batch, use_persistent_pass() ? pass_stagger_ns() : 0);
+                    fuse_hist, use_packed_fma() ? 1 : 0, batch);
                 return cudaGetLastError();
             }
         }
@@ -1737,7 +1701,7 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
         const dim3 pgrid = pass_grid(fn, threads, smem, grid);
         k_pass_rounds<Real, 5><<<pgrid, threads, smem, s>>>(
             states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-            fuse_hist, use_packed_fma() ? 1 : 0, batch, use_persistent_pass() ? pass_stagger_ns() : 0);
+            fuse_hist, use_packed_fma() ? 1 : 0, batch);
         return cudaGetLastError();
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
