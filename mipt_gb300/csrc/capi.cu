@@ -899,13 +899,15 @@ int mipt_gb300_engine_apply_bonds(mipt_gb300_engine *e, const int *pairs, int nb
     {
         return fail(MIPT_GB300_E_INVALID, ex.what());
     }
+    MG_CUDA(e->err.ensure(sizeof(int) + sizeof(std::uint64_t)));
+    MG_CUDA(cudaMemset(e->err.p, 0, sizeof(int)));
     if (e->fp64)
     {
         MG_CUDA(e->gates.ensure(sizeof(double) * 32 * nb));
         MG_CUDA(cudaMemcpy(e->gates.p, m, sizeof(double) * 32 * nb, cudaMemcpyHostToDevice));
         for (const auto &p : plan)
             MG_CUDA(launch_pass<double>(static_cast<Cx<double> *>(e->data()), 1, p, e->gates.as<Cx<double>>(), 0,
-                                        nullptr, 0, nullptr, 0, nullptr, 0, 0));
+                                        nullptr, 0, nullptr, 0, nullptr, 0, e->err.as<int>(), 0));
     }
     else
     {
@@ -915,9 +917,12 @@ int mipt_gb300_engine_apply_bonds(mipt_gb300_engine *e, const int *pairs, int nb
         MG_CUDA(cudaMemcpy(e->gates.p, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
         for (const auto &p : plan)
             MG_CUDA(launch_pass<float>(static_cast<Cx<float> *>(e->data()), 1, p, e->gates.as<Cx<float>>(), 0, nullptr,
-                                       0, nullptr, 0, nullptr, 0, 0));
+                                       0, nullptr, 0, nullptr, 0, e->err.as<int>(), 0));
     }
     MG_CUDA(cudaDeviceSynchronize());
+    int err = 0;
+    MG_CUDA(cudaMemcpy(&err, e->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(MIPT_GB300_E_INTERNAL, "tile load wait timed out");
     return 0;
 }
 
@@ -1313,7 +1318,8 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             const bool last = pi + 1 == plan.size();
             Mark m(b, K_PASS, s);
             MG_CUDA(launch_pass<Real>(states, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
-                                      cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0, s));
+                                      cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0,
+                                      b->err.as<int>(), s));
             ++L;
         }
         if (b->any_meas[t])
@@ -1435,6 +1441,7 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
     b->marks.clear();
     int err = 0;
     MG_CUDA(cudaMemcpy(&err, b->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err & 8) return fail(MIPT_GB300_E_INTERNAL, "tile load wait timed out");
     if (err) return fail(MIPT_GB300_E_NUMERIC, "a measurement found a zero-norm state or no outcome with weight");
     if (b->ws.err.p)
     {

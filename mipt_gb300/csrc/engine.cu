@@ -16,9 +16,12 @@
 #include <array>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <stdexcept>
 
 #include <cooperative_groups.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 
 namespace mg
 {
@@ -294,38 +297,35 @@ __device__ void value_histogram(const T *val, int k, const int *lm, int m_loc, d
 }
 
 // Born histogram of an FP32 tile straight from the registers of the pass's
-// last round, in a fixed order: squared magnitudes are folded over the
-// unmeasured register bits (pairwise FP32 adds), then over the unmeasured lane
-// bits (xor shuffles); each surviving value goes to S[w * 2^m_loc + bin], w
-// the rank of its warp among the warps that differ only in unmeasured bits,
-// and out[bin] = sum over w in order (value_histogram's result). `mmask` is
-// the measured set in tile positions (bin bit i <-> i-th measured position
-// from the bottom); S needs 2^k floats. A pairwise tree of depth <= k in FP32
-// bounds the relative rounding error of a bin by k * 2^-24, below the
-// reference's sequential FP32 runs of 64
-// (cpp/include/mipt/cuda/reduce_sweep.cuh:59-96); only the per-bin result is
+// last round, in a fixed order. Squared magnitudes are folded over the
+// unmeasured register bits in registers (pairwise FP32 adds); every thread
+// then stores its 2^RB values to S[(warp * 2^RB + r) * L + lane] (L lanes per
+// warp; S needs 2^k floats), and the bins are summed from there: bin `bin`
+// collects the entries whose measured bits spell it, over all values of the
+// unmeasured lane and warp bits, G threads per bin each summing a fixed
+// slice and a shuffle tree joining the G partial sums. `mmask` is the measured
+// set in tile positions (bin bit i <-> i-th measured position from the
+// bottom); out[bin] as in value_histogram. Rounding: pairwise register folds
+// and shuffle trees plus sequential runs of at most 2^(TB - log2 G) terms in
+// FP32, within the reference's scheme of FP32 runs of 64
+// (cpp/include/mipt/cuda/reduce_sweep.cuh:59-96); the per-bin result is
 // widened to FP64.
 template <int RB>
 __device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round &Z, int TB, std::uint32_t mmask,
-                                   int m_loc, float *S, double *out)
+                                   int m_loc, float *S, int *tab, double *out)
 {
     constexpr int NA = 1 << RB;
     const int tid = threadIdx.x;
     const int nl = TB < 5 ? TB : 5;
-    const unsigned lanes = TB >= 5 ? 0xffffffffu : ((1u << (1u << TB)) - 1u);
+    const int L = 1 << nl;
+    const unsigned lanes = TB >= 5 ? 0xffffffffu : ((1u << L) - 1u);
     float p[NA];
 #pragma unroll
     for (int r = 0; r < NA; ++r) p[r] = norm2(amp[r]);
-    // Register bits: unmeasured ones are folded; a measured one adds its bin bit.
     unsigned um_reg = 0;
-    std::uint32_t regbin[RB];
 #pragma unroll
     for (int i = 0; i < RB; ++i)
-    {
-        const int q = Z.reg[i];
-        regbin[i] = ((mmask >> q) & 1u) ? 1u << __popc(mmask & ((1u << q) - 1u)) : 0u;
-        if (!((mmask >> q) & 1u)) um_reg |= 1u << i;
-    }
+        if (!((mmask >> Z.reg[i]) & 1u)) um_reg |= 1u << i;
 #pragma unroll
     for (int i = 0; i < RB; ++i)
         if ((um_reg >> i) & 1u)
@@ -334,55 +334,59 @@ __device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round 
             for (int r = 0; r < NA; ++r)
                 if (!((r >> i) & 1)) p[r] += p[r | (1 << i)];
         }
-    // Thread bits: measured ones give the thread's bin bits, unmeasured lane
-    // bits are summed by shuffles, unmeasured warp bits index S's rows.
-    std::uint32_t tbin = 0, um_lane = 0, wrow = 0;
-    int uw = 0;
-    for (int j = 0; j < TB; ++j)
+    // tab[q], q < k: offset in S of tile position q; tab[16 + t]: offset of
+    // the t-th unmeasured thread bit; tab[31]: their count.
+    for (int q = tid; q < 16; q += blockDim.x)
     {
-        const int q = Z.tid[j];
-        const bool set = (tid >> j) & 1;
-        if ((mmask >> q) & 1u)
-        {
-            if (set) tbin |= 1u << __popc(mmask & ((1u << q) - 1u));
-        }
-        else if (j < nl)
-            um_lane |= 1u << j;
-        else
-        {
-            if (set) wrow |= 1u << uw;
-            ++uw;
-        }
+        int st = 0;
+        for (int j = 0; j < RB; ++j)
+            if (Z.reg[j] == q) st = (1 << j) * L;
+        for (int j = 0; j < TB; ++j)
+            if (Z.tid[j] == q) st = j < nl ? (1 << j) : (1 << (j - nl)) * NA * L;
+        tab[q] = st;
     }
-#pragma unroll
-    for (int b = 0; b < 5; ++b)
-        if ((um_lane >> b) & 1u)
-        {
-#pragma unroll
-            for (int r = 0; r < NA; ++r)
-                if ((r & um_reg) == 0) p[r] += __shfl_xor_sync(lanes, p[r], 1 << b);
-        }
-    __syncthreads(); // the tile buffer is free
-    if ((tid & um_lane) == 0)
+    if (tid == 0)
     {
-        float *row = S + (static_cast<std::size_t>(wrow) << m_loc);
+        int uc = 0;
+        for (int j = 0; j < TB; ++j)
+            if (!((mmask >> Z.tid[j]) & 1u)) tab[16 + uc++] = j < nl ? (1 << j) : (1 << (j - nl)) * NA * L;
+        tab[31] = uc;
+    }
+    __syncthreads(); // the tile buffer is free; tab is ready
+    {
+        float *row = S + (static_cast<std::size_t>((tid >> 5) * NA) << nl) + (tid & 31);
 #pragma unroll
-        for (int r = 0; r < NA; ++r)
-            if ((r & um_reg) == 0)
-            {
-                std::uint32_t bin = tbin;
-#pragma unroll
-                for (int i = 0; i < RB; ++i)
-                    if ((r >> i) & 1) bin |= regbin[i];
-                row[bin] = p[r];
-            }
+        for (int r = 0; r < NA; ++r) row[r << nl] = p[r];
     }
     __syncthreads();
-    for (int bin = tid; bin < (1 << m_loc); bin += blockDim.x)
+    const int uc = tab[31];
+    const int nbin = 1 << m_loc;
+    const int T = blockDim.x;
+    const int G = nbin >= T ? 1 : (T / nbin < 32 ? T / nbin : 32);
+    const int per = (1 << uc) / G > 0 ? (1 << uc) / G : 1;
+    for (int w = tid / G; w < nbin; w += T / G)
     {
+        const int sub = tid % G;
+        int off = 0;
+        {
+            std::uint32_t mm = mmask;
+            for (int i = 0; i < m_loc; ++i)
+            {
+                const int q = __ffs(mm) - 1;
+                mm &= mm - 1u;
+                if ((w >> i) & 1) off += tab[q];
+            }
+        }
         float s = 0.f;
-        for (int w = 0; w < (1 << uw); ++w) s += S[(static_cast<std::size_t>(w) << m_loc) + bin];
-        out[bin] = static_cast<double>(s);
+        for (int c = sub * per; c < (sub + 1) * per && c < (1 << uc); ++c)
+        {
+            int o = off;
+            for (int t = 0; t < uc; ++t)
+                if ((c >> t) & 1) o += tab[16 + t];
+            s += S[o];
+        }
+        for (int d = G >> 1; d > 0; d >>= 1) s += __shfl_down_sync(lanes, s, d, G);
+        if (sub == 0) out[w] = static_cast<double>(s);
     }
 }
 
@@ -482,22 +486,109 @@ __device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real
     apply_slot<S>(a, Us);
 }
 
+__device__ __forceinline__ std::uint32_t smem_u32(const void *p)
+{
+    return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool tile_bar_try(std::uint64_t *bar, std::uint32_t parity)
+{
+    std::uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for a tile load (about 0.3 s at most).
+__device__ __forceinline__ bool tile_bar_wait(std::uint64_t *bar, std::uint32_t parity)
+{
+    for (int i = 0; i < (1 << 22); ++i)
+    {
+        if (tile_bar_try(bar, parity)) return true;
+        if (i >= 32) __nanosleep(64);
+    }
+    return false;
+}
+
+// One thread: fetches the tile of work item `item` (trajectory item >> n_nl,
+// tile item mod 2^n_nl) into `tile` in plain tile order with one TMA tensor
+// load. Dimension d of the map covers global index bits [lo[d], lo[d] +
+// bits[d]) (the last one also the trajectory index above bit n); its
+// coordinate is those bits of the item's base index, 0 on local runs.
+__device__ __forceinline__ void tile_tma_load(void *tile, const CUtensorMap *map, const TileTma &t, const PassGeom &g,
+                                              std::uint64_t item, std::uint64_t *bar)
+{
+    const std::uint64_t gb =
+        ((item >> g.n_nl) << g.n) | scatter_bits(item & ((1ull << g.n_nl) - 1), g.nl, g.n_nl);
+    int c[5] = {0, 0, 0, 0, 0};
+    for (int d = 0; d < t.rank; ++d)
+    {
+        const std::uint64_t v = gb >> t.lo[d];
+        c[d] = static_cast<int>(d + 1 == t.rank ? v : (v & ((1ull << t.bits[d]) - 1)));
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(static_cast<std::uint32_t>(sizeof(Cx<float>) << g.k))
+                 : "memory");
+    const std::uint32_t dst = smem_u32(tile), mb = smem_u32(bar);
+    const unsigned long long m = reinterpret_cast<unsigned long long>(map);
+    switch (t.rank)
+    {
+    case 1:
+        asm volatile("cp.async.bulk.tensor.1d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2}], [%3];"
+                     ::"r"(dst), "l"(m), "r"(c[0]), "r"(mb) : "memory");
+        break;
+    case 2:
+        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                     "[%4];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(mb) : "memory");
+        break;
+    case 3:
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4}], [%5];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(mb) : "memory");
+        break;
+    case 4:
+        asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4, %5}], [%6];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(mb)
+                     : "memory");
+        break;
+    default:
+        asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                     "%4, %5, %6}], [%7];" ::"r"(dst), "l"(m), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]),
+                     "r"(mb)
+                     : "memory");
+        break;
+    }
+}
+
 // One tiled pass with register rounds: global -> registers (lanes on the
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
 // Work items are (trajectory, tile) pairs, item = trajectory * 2^n_nl + tile;
 // the CTA at flat index c runs items c, c + C, ... with C the number of CTAs,
 // so one launch shape serves both one item per CTA (C = items) and a
-// persistent grid.
-template <typename Real, int RB>
+// persistent grid. With TMA (FP32, persistent grid) tiles arrive by one TMA
+// tensor load each into the shared tile buffer in plain tile order: the load
+// of the CTA's next item is issued as soon as the current item's last
+// transpose has read the buffer, so it streams under the last gate round, the
+// stores and the histogram, whose values then use their own 2^k floats after
+// the tile buffer. A load wait that runs out sets bit 8 of *err and ends the
+// CTA.
+template <typename Real, int RB, bool TMA>
 __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
-                  int fuse_hist, int packed, int batch)
+                  int fuse_hist, int packed, int batch, const __grid_constant__ CUtensorMap tmap, TileTma tt,
+                  int *err)
 {
     constexpr int NA = 1 << RB;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_dyn[];
+    // TMA tensor loads need a 128-byte aligned destination; the launch adds
+    // 128 bytes of dynamic shared memory for the shift.
+    unsigned char *smem_raw = smem_dyn;
+    if constexpr (TMA) smem_raw += (128u - (smem_u32(smem_dyn) & 127u)) & 127u;
     Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
     __shared__ Cx<Real> U[kMaxPassGates][16];
     __shared__ double red[8];
@@ -507,9 +598,23 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     const int tid = threadIdx.x;
     const std::uint64_t items = static_cast<std::uint64_t>(batch) << g.n_nl;
     const std::uint64_t step = static_cast<std::uint64_t>(gridDim.x) * gridDim.y;
+    const std::uint64_t first = static_cast<std::uint64_t>(blockIdx.y) * gridDim.x + blockIdx.x;
+    __shared__ __align__(8) std::uint64_t tile_bar;
+    __shared__ int tile_fail;
+    std::uint32_t tile_phase = 0;
+    if constexpr (TMA)
+    {
+        if (tid == 0)
+        {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&tile_bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            tile_fail = 0;
+        }
+        __syncthreads();
+        if (tid == 0 && first < items) tile_tma_load(tile, &tmap, tt, g, first, &tile_bar);
+    }
     int cur_b = -1;
-    for (std::uint64_t item = static_cast<std::uint64_t>(blockIdx.y) * gridDim.x + blockIdx.x; item < items;
-         item += step)
+    for (std::uint64_t item = first; item < items; item += step)
     {
         const int b = static_cast<int>(item >> g.n_nl);
         const std::uint64_t tix = item & ((1ull << g.n_nl) - 1);
@@ -525,7 +630,48 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
         if (has_col) cl = col_in[b * col_stride];
         const Real scale = static_cast<Real>(cl.scale);
 
+        const std::uint64_t next = item + step;
         Cx<Real> amp[NA];
+        if constexpr (TMA)
+        {
+            // This item's tile is in the tile buffer in plain tile order.
+            if (!tile_bar_wait(&tile_bar, tile_phase)) tile_fail = 1;
+            tile_phase ^= 1u;
+            const Round &R = P.round[0];
+            std::uint64_t gt = base;
+            std::uint32_t jt = 0;
+            for (int i = 0; i < TB; ++i)
+                if ((tid >> i) & 1)
+                {
+                    gt |= 1ull << g.pos[R.tid[i]];
+                    jt |= 1u << R.tid[i];
+                }
+            std::uint64_t gr[RB];
+            std::uint32_t jr[RB];
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+            {
+                gr[i] = 1ull << g.pos[R.reg[i]];
+                jr[i] = 1u << R.reg[i];
+            }
+#pragma unroll
+            for (int r = 0; r < NA; ++r)
+            {
+                std::uint32_t j = jt;
+                std::uint64_t gi = gt;
+#pragma unroll
+                for (int i = 0; i < RB; ++i)
+                    if ((r >> i) & 1)
+                    {
+                        j |= jr[i];
+                        gi |= gr[i];
+                    }
+                Cx<Real> v = tile[j];
+                if (has_col) v = collapse_value(v, gi, cl, scale);
+                amp[r] = v;
+            }
+        }
+        else
         {
             const Round &R = P.round[0];
             std::uint64_t gt = base;
@@ -546,7 +692,20 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                 amp[r] = v;
             }
         }
-        __syncthreads(); // gate matrices visible
+        __syncthreads(); // gate matrices visible; round-0 reads of the tile buffer are done
+        if constexpr (TMA)
+        {
+            if (tile_fail)
+            {
+                if (tid == 0)
+                {
+                    atomicOr(err, 8);
+                    tile_bar_wait(&tile_bar, tile_phase ^ 1u); // let the load land before leaving
+                }
+                return;
+            }
+            if (P.rounds == 1 && next < items && tid == 0) tile_tma_load(tile, &tmap, tt, g, next, &tile_bar);
+        }
 
         for (int ri = 0; ri < P.rounds; ++ri)
         {
@@ -588,6 +747,14 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                         if ((r >> i) & 1) p ^= rb_[i];
                     amp[r] = tile[p];
                 }
+                if constexpr (TMA)
+                {
+                    if (ri == P.rounds - 1 && next < items)
+                    {
+                        __syncthreads(); // the last reads of the tile buffer for this item are done
+                        if (tid == 0) tile_tma_load(tile, &tmap, tt, g, next, &tile_bar);
+                    }
+                }
             }
             if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
             if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
@@ -626,7 +793,9 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                         if ((chunk >> g.pos[i]) & 1ull) mmask |= 1u << i;
                     const int m_loc = __popc(mmask);
                     double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
-                    register_histogram<RB>(amp, Z, TB, mmask, m_loc, reinterpret_cast<float *>(smem_raw), part);
+                    float *S = reinterpret_cast<float *>(smem_raw + (TMA ? (sizeof(Cx<float>) << g.k) : 0));
+                    __shared__ int tab[32];
+                    register_histogram<RB>(amp, Z, TB, mmask, m_loc, S, tab, part);
                 }
             }
             else if (M.nchunks > 0)
@@ -1642,11 +1811,100 @@ cudaError_t launch_init_zero(Cx<Real> *states, std::uint64_t dim, int batch, cud
     return cudaGetLastError();
 }
 
+// MIPT_GB300_TILE_TMA=0 turns the TMA tile loads of FP32 passes off.
+bool use_tile_tma()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_TILE_TMA");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tile_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Tensor map over `batch` FP32 states of 2^n amplitudes whose box is one tile
+// of geometry g in plain tile order. The global index bits split into runs of
+// local or non-local qubits; local runs longer than 8 bits split into boxes of
+// at most 256; the last run also carries the trajectory index. Needs local
+// positions in ascending qubit order, a local run at bit 0 (the innermost box
+// then spans >= 16 bytes) and at most 5 dimensions; false otherwise.
+bool encode_tile_map(CUtensorMap &map, TileTma &t, const Cx<float> *states, int batch, const PassGeom &g)
+{
+    std::memset(&map, 0, sizeof(map));
+    t = TileTma{};
+    if (tile_map_encoder() == nullptr || (reinterpret_cast<std::uintptr_t>(states) & 15u) != 0) return false;
+    for (int i = 1; i < g.k; ++i)
+        if (g.pos[i] <= g.pos[i - 1]) return false;
+    bool local[kMaxQubits] = {};
+    for (int i = 0; i < g.k; ++i) local[g.pos[i]] = true;
+    if (!local[0]) return false;
+    int q = 0;
+    while (q < g.n)
+    {
+        int len = 1;
+        while (q + len < g.n && local[q + len] == local[q] && (!local[q] || len < 8)) ++len;
+        if (t.rank == 5) return false;
+        t.lo[t.rank] = q;
+        t.bits[t.rank] = len;
+        ++t.rank;
+        q += len;
+    }
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5], es[5];
+    for (int d = 0; d < t.rank; ++d)
+    {
+        const bool loc = local[t.lo[d]];
+        dims[d] = 1ull << t.bits[d];
+        if (d + 1 == t.rank) dims[d] *= static_cast<cuuint64_t>(batch);
+        box[d] = loc ? (1u << t.bits[d]) : 1u;
+        es[d] = 1;
+        if (d > 0) strides[d - 1] = (1ull << t.lo[d]) * sizeof(Cx<float>);
+    }
+    if (dims[t.rank - 1] >= (1ull << 32)) return false;
+    return tile_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, static_cast<cuuint32_t>(t.rank),
+                              const_cast<Cx<float> *>(states), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Launches k_pass_rounds<Real, RB, TMA> on its grid.
+template <typename Real, int RB, bool TMA>
+cudaError_t launch_rounds(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
+                          std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
+                          const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
+                          const CUtensorMap &map, const TileTma &tt, int *err, cudaStream_t s)
+{
+    const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, RB, TMA>);
+    const std::size_t smem = (sizeof(Cx<Real>) << plan.geom.k) + (TMA ? (sizeof(float) << plan.geom.k) + 128 : 0);
+    cudaError_t e = ensure_smem_attr<Real>(fn, smem);
+    if (e != cudaSuccess) return e;
+    const int threads = 1 << (plan.geom.k - RB);
+    const dim3 pgrid = pass_grid(fn, threads, smem, dim3(1u << plan.geom.n_nl, batch));
+    k_pass_rounds<Real, RB, TMA><<<pgrid, threads, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
+                                                               collapse_stride, meas, meas_stride, partials,
+                                                               fuse_hist, use_packed_fma() ? 1 : 0, batch, map, tt,
+                                                               err);
+    return cudaGetLastError();
+}
+
 template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                        cudaStream_t s)
+                        int *err, cudaStream_t s)
 {
     dim3 grid(1u << plan.geom.n_nl, batch);
     if constexpr (sizeof(Real) == 4)
@@ -1677,32 +1935,37 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
     }
     if (plan.rounds > 0)
     {
-        const std::size_t smem = sizeof(Cx<Real>) << plan.geom.k;
         if constexpr (sizeof(Real) == 4)
         {
+            CUtensorMap map;
+            TileTma tt{};
+            const bool tma = use_persistent_pass() && use_tile_tma() && err != nullptr &&
+                             encode_tile_map(map, tt, states, batch, plan.geom);
             if (plan.rb == 6)
-            {
-                const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, 6>);
-                cudaError_t e = ensure_smem_attr<Real>(fn, smem);
-                if (e != cudaSuccess) return e;
-                const int threads = 1 << (plan.geom.k - 6);
-                const dim3 pgrid = pass_grid(fn, threads, smem, grid);
-                k_pass_rounds<Real, 6><<<pgrid, threads, smem, s>>>(
-                    states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-                    fuse_hist, use_packed_fma() ? 1 : 0, batch);
-                return cudaGetLastError();
-            }
+                return tma ? launch_rounds<Real, 6, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
+                                                          collapse_stride, meas, meas_stride, partials, fuse_hist,
+                                                          map, tt, err, s)
+                           : launch_rounds<Real, 6, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
+                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
+                                                           map, tt, err, s);
+            if (plan.rb == 5)
+                return tma ? launch_rounds<Real, 5, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
+                                                          collapse_stride, meas, meas_stride, partials, fuse_hist,
+                                                          map, tt, err, s)
+                           : launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
+                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
+                                                           map, tt, err, s);
+            return cudaErrorInvalidValue;
         }
-        if (plan.rb != 5) return cudaErrorInvalidValue;
-        const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, 5>);
-        cudaError_t e = ensure_smem_attr<Real>(fn, smem);
-        if (e != cudaSuccess) return e;
-        const int threads = 1 << (plan.geom.k - 5);
-        const dim3 pgrid = pass_grid(fn, threads, smem, grid);
-        k_pass_rounds<Real, 5><<<pgrid, threads, smem, s>>>(
-            states, plan, layer_gates, gate_stride, collapse_in, collapse_stride, meas, meas_stride, partials,
-            fuse_hist, use_packed_fma() ? 1 : 0, batch);
-        return cudaGetLastError();
+        else
+        {
+            if (plan.rb != 5) return cudaErrorInvalidValue;
+            CUtensorMap map;
+            std::memset(&map, 0, sizeof(map));
+            return launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
+                                                 collapse_stride, meas, meas_stride, partials, fuse_hist, map,
+                                                 TileTma{}, err, s);
+        }
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
     cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass<Real>), smem);
@@ -1756,7 +2019,7 @@ cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, cons
     template cudaError_t launch_init_zero<R>(Cx<R> *, std::uint64_t, int, cudaStream_t);                         \
     template cudaError_t launch_pass<R>(Cx<R> *, int, const PassPlan &, const Cx<R> *, std::size_t,              \
                                         const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
-                                        int, cudaStream_t);                                                      \
+                                        int, int *, cudaStream_t);                                               \
     template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
                                         const LayerMeas *, std::size_t, double *, cudaStream_t);                 \
     template cudaError_t launch_collapse<R>(Cx<R> *, std::uint64_t, int, const Collapse *, std::size_t,          \

@@ -53,6 +53,16 @@ struct ClusterRound
     std::int16_t slot[3];
 };
 
+// TMA view of a pass's tiles: dimension d of the tensor map covers global
+// index bits [lo[d], lo[d] + bits[d]) of the batch of states (the last one
+// also the trajectory bits above bit n); local runs are whole box dimensions.
+struct TileTma
+{
+    int rank;
+    int lo[5];
+    int bits[5];
+};
+
 struct PassPlan
 {
     PassGeom geom;
@@ -121,7 +131,7 @@ template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                        cudaStream_t s);
+                        int *err, cudaStream_t s);
 
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
