@@ -17,6 +17,7 @@
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <type_traits>
 
 #include <algorithm>
 #include <cmath>
@@ -101,11 +102,16 @@ __device__ __forceinline__ Cx<Real> gather(const Cx<Real> *__restrict__ psi, std
 
 // mode 0: write split partials of rho (full tile) to part_out;
 // mode 1: reduce the tile's contribution to Tr(rho^2) into pur_out.
-// Acc is the accumulation type: FP64 whenever rho is materialised (its
+// Acc is the type of the totals: FP64 whenever rho is materialised (its
 // small eigenvalues feed -lambda log lambda, so accumulation rounding must
 // stay below the state's own second-order error), the operand type for the
-// purity-only mode.
-template <typename Real, typename Acc>
+// purity-only mode. With kMixed (FP32 states, FP64 totals) the products are
+// summed in FP32 runs of 64 before each run joins the FP64 totals: FP32 FMA
+// throughput instead of GB300's FP64 rate. A run's rounding is about
+// 2^-24 * 64 * |amplitude|^2 ~ 2^(6 - 24 - n), which keeps the spurious
+// eigenvalues of rho, and their -lambda log lambda, negligible for n >= 20;
+// smaller states keep exact FP64 sums of the (exact) FP32 products.
+template <typename Real, typename Acc, bool kMixed = false>
 __global__ void __launch_bounds__(kGramThreads)
     k_gram(const Cx<Real> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
            const Collapse *__restrict__ col, std::size_t col_stride, int splits, std::uint64_t kchunk, int mode,
@@ -172,11 +178,23 @@ __global__ void __launch_bounds__(kGramThreads)
 
     const Cx<Real> *psi = states + (static_cast<std::size_t>(J.traj) << n);
     const int ty = tid / 16, tx = tid % 16;
+    // kMixed: products summed in FP32 runs of 2 * TK = 64 environment
+    // columns, each run added to the FP64 totals (the reference's
+    // mixed-precision sweep, cpp/include/mipt/cuda/reduce_sweep.cuh:59-96);
+    // otherwise the products go straight into Acc.
+    static_assert(!kMixed || (sizeof(Real) == 4 && sizeof(Acc) == 8), "mixed runs: FP32 states, FP64 totals");
+    using Run = typename std::conditional<kMixed, float, Acc>::type;
     Acc accr[4][4], acci[4][4];
+    Run runr[4][4], runi[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) accr[i][j] = acci[i][j] = Acc(0);
+        for (int j = 0; j < 4; ++j)
+        {
+            accr[i][j] = acci[i][j] = Acc(0);
+            runr[i][j] = runi[i][j] = Run(0);
+        }
+    int run_chunks = 0;
 
     for (std::uint64_t e0 = ebeg; e0 < eend; e0 += TK)
     {
@@ -225,14 +243,41 @@ __global__ void __launch_bounds__(kGramThreads)
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
                 {
-                    // a * conj(b); FP32 x FP32 products are exact in FP64
-                    accr[i][j] = fma(Acc(a[i].re), Acc(b[j].re), accr[i][j]);
-                    accr[i][j] = fma(Acc(a[i].im), Acc(b[j].im), accr[i][j]);
-                    acci[i][j] = fma(Acc(a[i].im), Acc(b[j].re), acci[i][j]);
-                    acci[i][j] = fma(-Acc(a[i].re), Acc(b[j].im), acci[i][j]);
+                    // a * conj(b)
+                    runr[i][j] = fma(Run(a[i].re), Run(b[j].re), runr[i][j]);
+                    runr[i][j] = fma(Run(a[i].im), Run(b[j].im), runr[i][j]);
+                    runi[i][j] = fma(Run(a[i].im), Run(b[j].re), runi[i][j]);
+                    runi[i][j] = fma(-Run(a[i].re), Run(b[j].im), runi[i][j]);
                 }
         }
+        if constexpr (kMixed)
+        {
+            if (++run_chunks == 2 || e0 + TK >= eend)
+            {
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                    {
+                        accr[i][j] += static_cast<Acc>(runr[i][j]);
+                        acci[i][j] += static_cast<Acc>(runi[i][j]);
+                        runr[i][j] = runi[i][j] = Run(0);
+                    }
+                run_chunks = 0;
+            }
+        }
         __syncthreads();
+    }
+    if constexpr (!kMixed)
+    {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+            {
+                accr[i][j] = runr[i][j];
+                acci[i][j] = runi[i][j];
+            }
     }
 
     if (mode == 0)
@@ -693,8 +738,12 @@ cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int n
     const std::uint64_t E = 1ull << (n - k);
     const std::uint64_t kchunk = (E + splits - 1) / splits;
     dim3 grid(gram_tiles(k), splits, njobs);
-    k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits, kchunk,
-                                                       0, static_cast<double *>(scratch), nullptr);
+    if (sizeof(Real) == 4 && n >= 20)
+        k_gram<Real, double, sizeof(Real) == 4><<<grid, kGramThreads, 0, s>>>(
+            states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0, static_cast<double *>(scratch), nullptr);
+    else
+        k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits,
+                                                           kchunk, 0, static_cast<double *>(scratch), nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int d = 1 << k;

@@ -264,3 +264,22 @@ def test_tensor_core_renyi2(mg, orc, n, kept, ferm):
     rho = orc.rdm(psi, kept, ferm)
     want = -np.log2(np.sum(np.abs(rho) ** 2))
     assert abs(got - want) < 1e-5, (got, want)
+
+
+def test_fp32_region_svn_large_state(mg):
+    """S_vN of 8-qubit regions of L=20 FP32 states, whose rho Gram sums FP32
+    runs of 64 products into FP64 totals, against the FP64 path on the same
+    measurement outcomes (|dS| within the FP32 path's 1e-5)."""
+    n, periods, p = 20, 3, 0.25
+    seeds = [mg.trajectory_seed(20, i) for i in range(2)]
+    regions = [list(range(8)), list(range(6, 14)), [0, 3, 5, 9, 12, 15, 17, 19]]
+    runs = {}
+    for fp64 in (True, False):
+        b = mg.Batch(n, periods, capacity=len(seeds), fp64=fp64, observe_every=1)
+        for r in regions:
+            b.add_region(r, 1)
+        got = b.run(seeds, p, forced=None if fp64 else runs[True][1])
+        runs[fp64] = (b.fetch_regions(), got["outcomes"])
+    np.testing.assert_array_equal(runs[False][1], runs[True][1])
+    assert runs[True][0].max() > 1.0  # entangled regions, not only product states
+    np.testing.assert_allclose(runs[False][0], runs[True][0], rtol=0, atol=1e-5)
