@@ -31,7 +31,7 @@ METRIC = "trajectory-layers/s at L=24 (batched FP32 vs plain FP64) at |dS|<=1e-5
 UNIT = "trajectory-layers/s"
 N_QUBITS = 24
 PERIODS = 24
-PASS_TRAFFIC_PER_TRAJ = 237.9e6  # DRAM bytes per trajectory per pass launch (ncu)
+PASS_TRAFFIC_PER_TRAJ = 239.3e6  # DRAM bytes per trajectory per pass launch (ncu)
 P_GRID = np.linspace(0.05, 0.35, 16)
 
 
@@ -239,8 +239,8 @@ def run_gb300(args):
         passes_per_layer = pass_n / T
         achieved = alg_bytes_step / (pass_ms / 1000.0) / 1e9
         peak, peak_kind = measured_peak_hbm()
-        # DRAM traffic per pass launch: ncu measured 237.9 MB per trajectory
-        # (read 134.3 MB + write 103.7 MB, the rest of the writes still in L2)
+        # DRAM traffic per pass launch: ncu measured 239.3 MB per trajectory
+        # (read 134.5 MB + write 104.8 MB, the rest of the writes still in L2)
         # on 2 trajectories; each launch streams every state once, so it
         # scales with the batch (profiles/k_pass_rounds_L24_batch2.md).
         traffic = PASS_TRAFFIC_PER_TRAJ * B
