@@ -159,7 +159,7 @@ struct EntReq
 
 struct Workspace
 {
-    DevBuf jobs, rho, scratch, vals, idx, eig, work, info, err;
+    DevBuf jobs, rho, scratch, vals, idx, eig, work, info, err, rows;
     cusolverDnHandle_t solver = nullptr;
     ~Workspace()
     {
@@ -168,6 +168,8 @@ struct Workspace
 };
 
 constexpr std::size_t kMaxRhoBytes = std::size_t{1} << 31;
+// Largest buffer of pre-split TF32 operand rows (16 bytes per amplitude).
+constexpr std::size_t kMaxRowsBytes = std::size_t{16} << 30;
 
 // Evaluates every request into d_out[req.out]; all requests share n.
 template <typename Real>
@@ -239,8 +241,20 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 }
                 MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
                 MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+                // Low cuts: TF32 operand rows split once per observation, in
+                // job groups of at most kMaxRowsBytes.
+                bool presplit = low_cut && k <= 13 && gram_tc_presplit_enabled();
+                if (presplit)
+                {
+                    const std::size_t per_job = gram_tc_rows_bytes_per_job(n);
+                    presplit = per_job <= kMaxRowsBytes &&
+                               ws.rows.ensure(std::min(kMaxRowsBytes / per_job, static_cast<std::size_t>(nb)) *
+                                              per_job) == cudaSuccess;
+                    if (!presplit) cudaGetLastError(); // no room: the Gram gathers its operands itself
+                }
                 MG_CUDA(gram_purity_tc(states, n, ws.jobs.as<GramJob>(), nb, k, col, col_stride, ws.vals.as<double>(),
-                                       ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s, low_cut ? traj_count : 0));
+                                       ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s, low_cut ? traj_count : 0,
+                                       presplit ? ws.rows.p : nullptr, presplit ? ws.rows.bytes : 0));
                 launches += 2;
                 k_scatter<<<(nb + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nb, d_out, 1);
                 ++launches;

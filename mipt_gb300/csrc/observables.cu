@@ -1359,6 +1359,279 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                      : "memory");
     }
 }
+
+// ------------------------------------------------- pre-split operand rows
+// For cuts that keep modes 0..k-1 (the Schmidt matrix of a trajectory is the
+// plain [E][d] block of its state), the 3xTF32 operands are built once per
+// observation by k_tf32_rows instead of once per (row block, column block)
+// pair inside the Gram: operand row (job j, chunk c, kept index a), at row
+// index (j * nchunks + c) * d + a, holds the 16 environment columns
+// e = 16c..16c+15 as 32 floats [Re psi(a, e) .. | Im psi(a, e) ..], TF32 hi
+// parts in rows [0, R) and lo parts in rows [R, 2R). The Gram then only
+// streams 128-byte rows into 128B-swizzled K-major stages by TMA.
+constexpr int TP_STAGES = 4;
+constexpr int TP_A_BYTES = TCM * 128;                     // hi or lo half of A: 16 KB
+constexpr int TP_B_BYTES = TCC * 128;                     // hi or lo half of B: 8 KB
+constexpr int TP_STAGE = 2 * TP_A_BYTES + 2 * TP_B_BYTES; // 48 KB
+constexpr std::size_t TP_SMEM = static_cast<std::size_t>(TP_STAGES) * TP_STAGE + 1024;
+constexpr int TP_THREADS = (TC_PWARPS + 2) * 32;          // drain warps, MMA warp, TMA warp
+// D = F32, A = B = TF32, K-major, N = TCC (Re or Im half of the block), M = 128;
+// bit 13 negates A.
+constexpr std::uint32_t kTpIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCC >> 3) << 17) | ((TCM >> 4) << 24);
+constexpr std::uint32_t kTpIdescNegA = kTpIdesc | (1u << 13);
+
+// One thread per operand row: 16 amplitudes of job j's state (pending
+// collapse applied), split into TF32 hi/lo.
+__global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, const GramJob *__restrict__ jobs,
+                            int njobs, const Collapse *__restrict__ col, std::size_t col_stride,
+                            float4 *__restrict__ rows, std::uint64_t lo_rows)
+{
+    const std::uint64_t d = 1ull << k;
+    const int cbits = n - k - 4;
+    const std::uint64_t total = (static_cast<std::uint64_t>(njobs) << cbits) << k;
+    for (std::uint64_t idx = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; idx < total;
+         idx += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const std::uint64_t a = idx & (d - 1);
+        const std::uint64_t c = (idx >> k) & ((1ull << cbits) - 1);
+        const int j = static_cast<int>(idx >> (k + cbits));
+        const int t = jobs[j].traj;
+        const Cx<float> *psi = states + (static_cast<std::size_t>(t) << n);
+        Collapse cl{0, 0, 1.0, 0.0};
+        if (col != nullptr) cl = col[t * col_stride];
+        const float scale = static_cast<float>(cl.scale);
+        float re[16], im[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+        {
+            const std::uint64_t gi = a | (((c << 4) + i) << k);
+            const Cx<float> v = psi[gi];
+            const bool keep = col == nullptr || (gi & cl.mask) == cl.value;
+            re[i] = keep ? v.re * scale : 0.f;
+            im[i] = keep ? v.im * scale : 0.f;
+        }
+        float4 *hi = rows + idx * 8, *lo = rows + (idx + lo_rows) * 8;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+        {
+            const float *src = q < 4 ? re + 4 * q : im + 4 * (q - 4);
+            float4 h, l;
+            tf32_split(src[0], h.x, l.x);
+            tf32_split(src[1], h.y, l.y);
+            tf32_split(src[2], h.z, l.z);
+            tf32_split(src[3], h.w, l.w);
+            hi[q] = h;
+            lo[q] = l;
+        }
+    }
+}
+
+__device__ __forceinline__ void tp_mma(std::uint32_t d, std::uint64_t a, std::uint64_t b, std::uint32_t idesc,
+                                       std::uint32_t acc)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+                 "l"(a), "l"(b), "r"(idesc), "r"(acc)
+                 : "memory");
+}
+
+// Purity partials of one 128 x 64 block of rho for job job0 + blockIdx.z from
+// the pre-split rows of the group's job blockIdx.z (tmap: 2-D FP32 view, 32 floats per row, box 32 x 64,
+// 128-byte swizzle). Warp TC_PWARPS issues the MMAs (Re rho = Re.Re + Im.Im
+// into TMEM columns [0, 64), Im rho = Im.Re - Re.Im into [64, 128), each term
+// as 3 TF32 products), warp TC_PWARPS + 1 the TMA loads, and warps
+// 0..TC_PWARPS-1 drain the TMEM segments into FP32 registers and reduce the
+// weighted squares as k_gram_tc does. Every wait is bounded (bit 4 of *err).
+__global__ void __launch_bounds__(TP_THREADS, 1)
+    k_gram_tc_pre(int n, int k, int job0, double *__restrict__ pur_out, int *__restrict__ err, std::uint32_t lo_rows,
+                  const __grid_constant__ CUtensorMap tmap)
+{
+    extern __shared__ __align__(1024) unsigned char tp_raw[];
+    __shared__ __align__(8) std::uint64_t full_bar[TP_STAGES], empty_bar[TP_STAGES], seg_bar[TC_TMEM_BUFS],
+        drained_bar[TC_TMEM_BUFS];
+    __shared__ std::uint32_t tmem_base;
+    __shared__ double red[TC_PWARPS];
+    __shared__ volatile int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const std::uint32_t raw_s = sm_addr(tp_raw);
+    unsigned char *smem = tp_raw + ((1024u - (raw_s & 1023u)) & 1023u);
+    const int job = blockIdx.z;
+    int tr, tc;
+    tile_coords(blockIdx.x, tr, tc);
+    if (tid == 0)
+    {
+        for (int st = 0; st < TP_STAGES; ++st)
+        {
+            mbar_init(&full_bar[st], 1);
+            mbar_init(&empty_bar[st], 1);
+        }
+        for (int b = 0; b < TC_TMEM_BUFS; ++b)
+        {
+            mbar_init(&seg_bar[b], 1);
+            mbar_init(&drained_bar[b], TC_PWARPS);
+        }
+        abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == TC_PWARPS)
+    {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sm_addr(&tmem_base)),
+                     "n"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const std::uint32_t tmem = tmem_base;
+    const int r0 = tr * TCM, c0 = tc * TCM + static_cast<int>(blockIdx.y) * TCC;
+    const int nchunks = 1 << (n - k - 4);
+    const int nseg = (nchunks + TC_SEG - 1) / TC_SEG;
+
+    if (warp < TC_PWARPS)
+    {
+        float acc[TC_DCOLS];
+#pragma unroll
+        for (int i = 0; i < TC_DCOLS; ++i) acc[i] = 0.f;
+        const std::uint32_t lane_base = static_cast<std::uint32_t>((warp & 3) * 32) << 16;
+        const int col_base = (warp >> 2) * TC_DCOLS;
+        for (int seg = 0; seg < nseg && !abort_flag; ++seg)
+        {
+            const int buf = seg % TC_TMEM_BUFS;
+            if (!mbar_wait(&seg_bar[buf], (seg / TC_TMEM_BUFS) & 1, &abort_flag, err)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int cb = 0; cb < TC_DCOLS / 32; ++cb)
+            {
+                std::uint32_t v[32];
+                const std::uint32_t taddr = tmem + lane_base + buf * TCN + col_base + cb * 32;
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                    "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]),
+                      "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]),
+                      "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int i = 0; i < 32; ++i) acc[cb * 32 + i] += __uint_as_float(v[i]);
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&drained_bar[buf]);
+        }
+        const int r = r0 + (warp & 3) * 32 + lane;
+        double sum = 0.0;
+        if (!abort_flag)
+        {
+#pragma unroll
+            for (int i = 0; i < TC_DCOLS; ++i)
+            {
+                const int c = c0 + ((col_base + i) & (TCC - 1));
+                const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
+                const double x = static_cast<double>(acc[i]);
+                sum += w * x * x;
+            }
+        }
+        for (int off = 16; off > 0; off /= 2) sum += __shfl_down_sync(0xffffffffu, sum, off);
+        if (lane == 0) red[warp] = sum;
+    }
+    else if (warp == TC_PWARPS && lane == 0)
+    {
+        for (int chunk = 0; chunk < nchunks; ++chunk)
+        {
+            const int st = chunk % TP_STAGES;
+            const int seg = chunk / TC_SEG;
+            const int buf = seg % TC_TMEM_BUFS;
+            if (chunk % TC_SEG == 0 && seg >= TC_TMEM_BUFS &&
+                !mbar_wait(&drained_bar[buf], ((seg / TC_TMEM_BUFS) - 1) & 1, &abort_flag, err))
+                break;
+            if (!mbar_wait(&full_bar[st], (chunk / TP_STAGES) & 1, &abort_flag, err)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const std::uint32_t base = sm_addr(smem + st * TP_STAGE);
+            const std::uint32_t Ahi = base, Alo = base + TP_A_BYTES;
+            const std::uint32_t Bhi = base + 2 * TP_A_BYTES, Blo = Bhi + TP_B_BYTES;
+            const std::uint32_t dre = tmem + buf * TCN, dim = dre + TCC;
+            const bool first = chunk % TC_SEG == 0;
+            // Re rho: 32 real K (16 Re then 16 Im) in four K = 8 steps.
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks)
+            {
+                const std::uint32_t ko = ks * 32;
+                tp_mma(dre, sw128_desc(Ahi + ko), sw128_desc(Bhi + ko), kTpIdesc, (first && ks == 0) ? 0u : 1u);
+                tp_mma(dre, sw128_desc(Ahi + ko), sw128_desc(Blo + ko), kTpIdesc, 1u);
+                tp_mma(dre, sw128_desc(Alo + ko), sw128_desc(Bhi + ko), kTpIdesc, 1u);
+            }
+            // Im rho = Im(A).Re(B) - Re(A).Im(B).
+#pragma unroll
+            for (int ps = 0; ps < 4; ++ps)
+            {
+                const std::uint32_t ka = (ps < 2 ? 64u : 0u) + (ps & 1) * 32u;
+                const std::uint32_t kb = (ps < 2 ? 0u : 64u) + (ps & 1) * 32u;
+                const std::uint32_t id = ps < 2 ? kTpIdesc : kTpIdescNegA;
+                tp_mma(dim, sw128_desc(Ahi + ka), sw128_desc(Bhi + kb), id, (first && ps == 0) ? 0u : 1u);
+                tp_mma(dim, sw128_desc(Ahi + ka), sw128_desc(Blo + kb), id, 1u);
+                tp_mma(dim, sw128_desc(Alo + ka), sw128_desc(Bhi + kb), id, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             sm_addr(&empty_bar[st]))
+                         : "memory");
+            if (chunk % TC_SEG == TC_SEG - 1 || chunk == nchunks - 1)
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 sm_addr(&seg_bar[buf]))
+                             : "memory");
+        }
+    }
+    else if (warp == TC_PWARPS + 1 && lane == 0)
+    {
+        int issued = 0;
+        const std::uint64_t tm = reinterpret_cast<std::uint64_t>(&tmap);
+        for (int chunk = 0; chunk < nchunks; ++chunk)
+        {
+            const int st = chunk % TP_STAGES;
+            if (chunk >= TP_STAGES &&
+                !mbar_wait(&empty_bar[st], ((chunk / TP_STAGES) - 1) & 1, &abort_flag, err))
+                break;
+            const std::uint32_t bar = sm_addr(&full_bar[st]);
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TP_STAGE)
+                         : "memory");
+            const std::uint32_t base = sm_addr(smem + st * TP_STAGE);
+            const int yb = static_cast<int>((static_cast<std::uint32_t>(job) * nchunks + chunk) << k);
+            const std::uint32_t dst[6] = {base, base + TP_A_BYTES / 2, base + TP_A_BYTES,
+                                          base + TP_A_BYTES + TP_A_BYTES / 2, base + 2 * TP_A_BYTES,
+                                          base + 2 * TP_A_BYTES + TP_B_BYTES};
+            const int ys[6] = {yb + r0, yb + r0 + 64, static_cast<int>(lo_rows) + yb + r0,
+                               static_cast<int>(lo_rows) + yb + r0 + 64, yb + c0, static_cast<int>(lo_rows) + yb + c0};
+#pragma unroll
+            for (int b = 0; b < 6; ++b)
+                asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                             "%3}], [%4];" ::"r"(dst[b]),
+                             "l"(tm), "r"(0), "r"(ys[b]), "r"(bar)
+                             : "memory");
+            issued = chunk + 1;
+        }
+        // After an abort, let the loads still in flight land.
+        for (int c = issued - TP_STAGES > 0 ? issued - TP_STAGES : 0; c < issued; ++c)
+            mbar_settle(&full_bar[c % TP_STAGES], (c / TP_STAGES) & 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid == 0)
+    {
+        double t = 0.0;
+        for (int w = 0; w < TC_PWARPS; ++w) t += red[w];
+        pur_out[(static_cast<std::size_t>(job0 + job) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
+    }
+    if (warp == TC_PWARPS)
+    {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TC_TMEM_COLS)
+                     : "memory");
+    }
+}
 } // namespace
 
 bool gram_tc_supported(int n, int k)
@@ -1403,22 +1676,76 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 }
 } // namespace
 
+bool gram_tc_presplit_enabled()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_TC_PRESPLIT");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+std::size_t gram_tc_rows_bytes_per_job(int n) { return (std::size_t{16}) << n; }
+
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
-                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count)
+                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count, void *rows,
+                           std::size_t rows_bytes)
 {
     if (njobs <= 0) return cudaSuccess;
     if (!gram_tc_supported(n, k)) return cudaErrorInvalidValue;
     const int tiles = gram_tc_tiles(k);
     if (gram_tc_scratch_bytes(k, njobs) > scratch_bytes) return cudaErrorInvalidValue;
+    const std::size_t per_job = gram_tc_rows_bytes_per_job(n);
+    // Measured: faster at k = 12 (L = 24 half cut, 85 -> 63 ms for 32 states);
+    // slower at k = 14 (L = 28), where a state's 4 GB of rows outgrow L2.
+    if (tma_traj_count > 0 && k <= 13 && rows != nullptr && rows_bytes >= per_job && tensor_map_encoder() != nullptr &&
+        (reinterpret_cast<std::uintptr_t>(rows) & 15u) == 0)
+    {
+        // Pre-split operand rows, jobs in groups that fit `rows`.
+        const int group = static_cast<int>(std::min<std::size_t>(static_cast<std::size_t>(njobs), rows_bytes / per_job));
+        cudaError_t e = cudaFuncSetAttribute(k_gram_tc_pre, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(TP_SMEM));
+        if (e != cudaSuccess) return e;
+        for (int g0 = 0; g0 < njobs; g0 += group)
+        {
+            const int g = std::min(group, njobs - g0);
+            const std::uint64_t lo_rows = static_cast<std::uint64_t>(g) << (n - 4);
+            if (2 * lo_rows >= (1ull << 31)) return cudaErrorInvalidValue;
+            CUtensorMap map;
+            std::memset(&map, 0, sizeof(map));
+            const cuuint64_t dims[2] = {32, 2 * lo_rows};
+            const cuuint64_t strides[1] = {128};
+            const cuuint32_t box[2] = {32, 64};
+            const cuuint32_t estr[2] = {1, 1};
+            if (tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, rows, dims, strides, box, estr,
+                                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return cudaErrorInvalidValue;
+            const std::uint64_t nrows = lo_rows;
+            const int blocks = static_cast<int>(std::min<std::uint64_t>((nrows + 255) / 256, 152ull * 8));
+            k_tf32_rows<<<blocks, 256, 0, s>>>(states, n, k, d_jobs + g0, g, collapse, collapse_stride,
+                                               static_cast<float4 *>(rows), lo_rows);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            dim3 grid(gram_tc_blocks(k), 2, g);
+            k_gram_tc_pre<<<grid, TP_THREADS, TP_SMEM, s>>>(n, k, g0, static_cast<double *>(scratch), err,
+                                                            static_cast<std::uint32_t>(lo_rows), map);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
+        k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
+        return cudaGetLastError();
+    }
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
-    const std::uint64_t rows = static_cast<std::uint64_t>(tma_traj_count) << (n - k);
-    bool tma = tma_traj_count > 0 && rows < (1ull << 31) && tensor_map_encoder() != nullptr &&
+    const std::uint64_t state_rows = static_cast<std::uint64_t>(tma_traj_count) << (n - k);
+    bool tma = tma_traj_count > 0 && state_rows < (1ull << 31) && tensor_map_encoder() != nullptr &&
                (reinterpret_cast<std::uintptr_t>(states) & 15u) == 0;
     if (tma)
     {
-        const cuuint64_t dims[2] = {1ull << k, rows};
+        const cuuint64_t dims[2] = {1ull << k, state_rows};
         const cuuint64_t strides[1] = {(1ull << k) * sizeof(Cx<float>)};
         const cuuint32_t box[2] = {64, 16};
         const cuuint32_t estr[2] = {1, 1};

@@ -67,9 +67,16 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
 // tma_traj_count state vectors; the operands then arrive by TMA.
 bool gram_tc_supported(int n, int k);
 std::size_t gram_tc_scratch_bytes(int k, int njobs);
+// With tma_traj_count > 0, k <= 13 and a `rows` buffer of at least
+// gram_tc_rows_bytes_per_job(n) bytes (16-byte aligned), the operands are
+// first split into TF32 hi/lo rows (jobs in groups that fit the buffer) and
+// the Gram streams them by TMA alone; MIPT_GB300_TC_PRESPLIT=0 turns that off.
+bool gram_tc_presplit_enabled();
+std::size_t gram_tc_rows_bytes_per_job(int n);
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
-                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count = 0);
+                           std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count = 0,
+                           void *rows = nullptr, std::size_t rows_bytes = 0);
 
 // Purity of full matrices rho[job][d][d].
 cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, cudaStream_t s);
