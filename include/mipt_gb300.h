@@ -309,6 +309,16 @@ typedef struct mipt_gb300_gmn_config
 int mipt_gb300_gmn_solve(const mipt_gb300_gmn_config *config, const double *rho, int count,
                          const float *warm_start, double *gmn, double *gap, int *iterations, double *solution);
 
+/* Negativity of the three single-qubit cuts of each 8x8 state (the
+ * bipartite-negativity prefilter of the reference's gmn.exe,
+ * cpp/apps/gmn.cpp:413-424, compute_min_bipartite_negativity_8x8_cpp
+ * cpp/src/analysis/fgmn.cpp:1443-1453 over cut_negativity
+ * cpp/include/mipt/analysis/cut_negativity.hpp:139-200): negativity[3 * i + m]
+ * = (||rho_i^{T_m}||_1 - 1) / 2 for the partial transpose on qubit m (index
+ * bit m), values in (-1e-10, 0) set to 0. FP64 Jacobi on the GPU.
+ * rho: [count][128] as for mipt_gb300_gmn_solve. */
+int mipt_gb300_cut_negativities(const double *rho, int count, double *negativity);
+
 /* Learned warm start: a multilayer perceptron (dims[0] inputs, ReLU between
  * layers, linear output) trained and evaluated on the GPU by the library's
  * own kernels. Weights are FP32 master copies (Adam) and BF16 copies that

@@ -87,6 +87,7 @@ def lib():
     L.mipt_gb300_batch_fetch_rho3_points.argtypes = [vp, vp]
     L.mipt_gb300_lattice_bonds.argtypes = [ci, ci, ci, vp, vp]
     L.mipt_gb300_gmn_solve.argtypes = [vp, vp, ci, vp, vp, vp, vp, vp]
+    L.mipt_gb300_cut_negativities.argtypes = [vp, ci, vp]
     L.mipt_gb300_draw_haar_lattice.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
@@ -390,6 +391,15 @@ def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6
     out = dict(gmn=g, gap=gap, iters=it)
     if want_solution:
         out["solution"] = ri_to_rho(sol)
+    return out
+
+
+def cut_negativities(rho):
+    """Negativity of the three single-qubit cuts of states rho[N, 8, 8] (FP64
+    on the GPU); the minimum is gmn.exe's bipartite-negativity prefilter."""
+    r = rho_to_ri(np.asarray(rho).reshape(-1, 8, 8))
+    out = np.zeros((len(r), 3))
+    _check(lib().mipt_gb300_cut_negativities(_p(r), len(r), _p(out)))
     return out
 
 

@@ -8,7 +8,7 @@
 //   even-site check for brickwork circuits         cpp/include/mipt/types.hpp:417-431
 //   17-significant-digit CSV numbers               cpp/include/mipt/tmi/linalg.hpp:223-234
 //   host pause sentinel (PAUSE_MIPT)               cpp/include/mipt/util/pause.hpp
-//   rho3.bin version-2 writer                      cpp/include/mipt/density.hpp:12-235
+//   rho3.bin version-2 writer and reader           cpp/include/mipt/density.hpp:12-345
 #pragma once
 
 #include "mipt_gb300.h"
@@ -285,6 +285,75 @@ class Rho3Writer
     std::uint32_t subsystems_ = 0;
     std::size_t values_ = 0;
     std::uint64_t written_ = 0;
+};
+
+// rho3.bin version-2 reader (the layout Rho3Writer writes; the reference's
+// DensityMatrixReader, cpp/include/mipt/density.hpp:253-345, with its checks).
+struct Rho3Record
+{
+    std::uint32_t p_index = 0, realization = 0;
+    double p = 0.0;
+    std::vector<double> rho_ri; // [subsystem][D][D][re, im]
+};
+
+class Rho3Reader
+{
+  public:
+    explicit Rho3Reader(const std::string &path) : in_(path, std::ios::binary)
+    {
+        if (!in_) throw std::runtime_error("Could not open density-matrix file: " + path);
+        char magic[8]{};
+        in_.read(magic, 8);
+        if (!in_) throw std::runtime_error("Could not read density-matrix file header.");
+        if (std::memcmp(magic, "MIPTRHO2", 8) != 0) throw std::runtime_error("Not a version-2 MIPT density-matrix file.");
+        std::uint32_t endian = 0, version = 0, subsystems = 0;
+        get(endian);
+        get(version);
+        if (endian != 0x01020304u) throw std::runtime_error("Density-matrix file endianness is not supported on this host.");
+        if (version != 2u) throw std::runtime_error("Unsupported density-matrix file version.");
+        for (std::uint32_t *v : {&m_.spatial_dimension, &m_.total_qubits, &m_.kept_qubits, &m_.matrix_dimension,
+                                 &m_.periods, &m_.realizations, &m_.resolution, &m_.grid_x, &m_.grid_y, &subsystems})
+            get(*v);
+        get(m_.record_count);
+        get(m_.p_min);
+        get(m_.p_max);
+        if (m_.kept_qubits == 0 || m_.kept_qubits >= 31 || m_.matrix_dimension != (1u << m_.kept_qubits) ||
+            subsystems == 0)
+            throw std::runtime_error("Inconsistent density-matrix metadata.");
+        m_.subsystem_qubits.resize(static_cast<std::size_t>(subsystems) * m_.kept_qubits);
+        in_.read(reinterpret_cast<char *>(m_.subsystem_qubits.data()),
+                 static_cast<std::streamsize>(m_.subsystem_qubits.size() * sizeof(std::uint32_t)));
+        if (!in_) throw std::runtime_error("Density-matrix subsystem metadata is incomplete.");
+        values_ = static_cast<std::size_t>(subsystems) * 2u * m_.matrix_dimension * m_.matrix_dimension;
+    }
+    const Rho3Metadata &metadata() const { return m_; }
+    std::uint32_t subsystem_count() const
+    {
+        return static_cast<std::uint32_t>(m_.subsystem_qubits.size() / m_.kept_qubits);
+    }
+    bool read_record(Rho3Record &r)
+    {
+        if (read_ >= m_.record_count) return false;
+        get(r.p_index);
+        get(r.realization);
+        get(r.p);
+        r.rho_ri.resize(values_);
+        in_.read(reinterpret_cast<char *>(r.rho_ri.data()), static_cast<std::streamsize>(values_ * sizeof(double)));
+        if (!in_) throw std::runtime_error("Density-matrix record payload is incomplete.");
+        ++read_;
+        return true;
+    }
+
+  private:
+    template <typename T> void get(T &v)
+    {
+        in_.read(reinterpret_cast<char *>(&v), sizeof(T));
+        if (!in_) throw std::runtime_error("Density-matrix file is truncated.");
+    }
+    std::ifstream in_;
+    Rho3Metadata m_;
+    std::size_t values_ = 0;
+    std::uint64_t read_ = 0;
 };
 
 } // namespace mgcli

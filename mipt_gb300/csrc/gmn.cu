@@ -659,6 +659,63 @@ int gmn_solve(const mipt_gb300_gmn_config &cfg, const double *h_rho, int count, 
 }
 } // namespace
 
+namespace
+{
+// Negativity of every single-qubit cut of 8x8 states: 8-lane group g handles
+// (state g / 3, cut g % 3). Lane c loads column c of the partial transpose on
+// qubit m (entry (r, c) from (r & ~mask | c & mask, c & ~mask | r & mask),
+// mask = 1 << m), the FP64 Jacobi diagonalises it, and
+// N = (sum_c |lambda_c| - 1) / 2, values in (-1e-10, 0) set to 0
+// (cpp/include/mipt/analysis/cut_negativity.hpp:139-200).
+__global__ void __launch_bounds__(kThreads) k_cut_negativity(int count, const double *__restrict__ rho,
+                                                              double *__restrict__ neg)
+{
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = tid / kLanes, c = tid % kLanes;
+    const int gbase = (threadIdx.x % 32) / kLanes * kLanes;
+    const unsigned gmask = 0xffu << gbase;
+    const bool live = g < 3 * count;
+    const int st = live ? g / 3 : 0, mask = 1 << (live ? g % 3 : 0);
+    const double *R = rho + static_cast<std::size_t>(st) * 128;
+    C2<double> A[8], V[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+    {
+        const int sr = (r & ~mask) | (c & mask), sc = (c & ~mask) | (r & mask);
+        A[r] = live ? C2<double>{R[2 * (sr * 8 + sc)], R[2 * (sr * 8 + sc) + 1]} : C2<double>{r == c ? 1.0 : 0.0, 0.0};
+        V[r] = C2<double>{0.0, 0.0};
+    }
+    jacobi8<double, false>(A, V, c, gbase, gmask, 10);
+    double t = fabs(pick(A, c).re);
+#pragma unroll
+    for (int off = 4; off > 0; off >>= 1) t += __shfl_xor_sync(gmask, t, off);
+    if (live && c == 0)
+    {
+        double n = 0.5 * (t - 1.0);
+        if (n < 0.0 && n > -1e-10) n = 0.0;
+        neg[g] = n;
+    }
+}
+} // namespace
+
+extern "C" int mipt_gb300_cut_negativities(const double *rho, int count, double *negativity)
+{
+    if (!rho || !negativity || count <= 0) return api_fail(MIPT_GB300_E_INVALID, "bad negativity arguments");
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return api_fail(MIPT_GB300_E_NODEVICE, "no CUDA device");
+    const std::size_t P = static_cast<std::size_t>(count);
+    DevMem d_rho, d_neg;
+    GMN_CUDA(d_rho.ensure(P * 128 * sizeof(double)));
+    GMN_CUDA(d_neg.ensure(P * 3 * sizeof(double)));
+    GMN_CUDA(cudaMemcpy(d_rho.p, rho, P * 128 * sizeof(double), cudaMemcpyHostToDevice));
+    const std::size_t threads = P * 3 * kLanes;
+    k_cut_negativity<<<static_cast<unsigned>((threads + kThreads - 1) / kThreads), kThreads>>>(
+        count, static_cast<const double *>(d_rho.p), static_cast<double *>(d_neg.p));
+    GMN_CUDA(cudaGetLastError());
+    GMN_CUDA(cudaMemcpy(negativity, d_neg.p, P * 3 * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
 extern "C" int mipt_gb300_gmn_solve(const mipt_gb300_gmn_config *cfg, const double *rho, int count,
                                     const float *warm_start, double *gmn, double *gap, int *iterations,
                                     double *solution)

@@ -51,3 +51,35 @@ def read(path):
     records = dict(p_index=raw["p_index"].copy(), realization=raw["realization"].copy(), p=raw["p"].copy(),
                    rho=rho[..., 0] + 1j * rho[..., 1])
     return meta, records
+
+
+def write(path, rho, p, p_index, realization=None, *, total_qubits=0, periods=0, realizations=0, resolution=None,
+          p_min=None, p_max=None, subsystem_qubits=None, spatial_dimension=1, grid_x=None, grid_y=1):
+    """Writes records rho[n][S][D][D] (complex) with per-record p and p_index
+    in the same version-2 layout (the inverse of read)."""
+    rho = np.asarray(rho, np.complex128)
+    n, S, D = rho.shape[0], rho.shape[1], rho.shape[2]
+    K = D.bit_length() - 1
+    if D != 1 << K or rho.shape[3] != D:
+        raise ValueError("rho must be [n][S][D][D] with D a power of two")
+    p = np.asarray(p, np.float64).reshape(n)
+    p_index = np.asarray(p_index, np.uint32).reshape(n)
+    realization = np.zeros(n, np.uint32) if realization is None else np.asarray(realization, np.uint32).reshape(n)
+    if subsystem_qubits is None:
+        subsystem_qubits = np.arange(S * K, dtype=np.uint32).reshape(S, K)
+    subsystem_qubits = np.asarray(subsystem_qubits, np.uint32).reshape(S, K)
+    resolution = int(p_index.max()) + 1 if resolution is None else resolution
+    p_min = float(p.min()) if p_min is None else p_min
+    p_max = float(p.max()) if p_max is None else p_max
+    grid_x = total_qubits if grid_x is None else grid_x
+    head = MAGIC + struct.pack("<II", 0x01020304, 2)
+    head += struct.pack("<10I", spatial_dimension, total_qubits, K, D, periods, realizations, resolution, grid_x,
+                        grid_y, S)
+    head += struct.pack("<Q", n) + struct.pack("<dd", p_min, p_max) + subsystem_qubits.tobytes()
+    rec = np.dtype([("p_index", "<u4"), ("realization", "<u4"), ("p", "<f8"), ("rho", "<f8", (S * 2 * D * D,))])
+    out = np.zeros(n, rec)
+    out["p_index"], out["realization"], out["p"] = p_index, realization, p
+    out["rho"] = np.stack([rho.real, rho.imag], -1).reshape(n, -1)
+    with open(path, "wb") as f:
+        f.write(head)
+        f.write(out.tobytes())

@@ -117,6 +117,21 @@ def solve(rho, sigma=1.0, gap_tol=1e-9, max_iter=200000, check_every=10, state=N
                 W=W, Q=Q, Z=[sigma * z for z in Zh], state=(U, V, Yh, Zh))
 
 
+def cut_negativities(rho):
+    """Negativity (||rho^{T_m}||_1 - 1) / 2 of the three single-qubit cuts
+    (partial transpose on index bit m), values in (-1e-10, 0) set to 0: the
+    reference's cut_negativity (cpp/include/mipt/analysis/cut_negativity.hpp:139-200,
+    qubit case); gmn.exe's prefilter is their minimum
+    (cpp/src/analysis/fgmn.cpp:972-986, cpp/apps/gmn.cpp:413-424)."""
+    rho = np.asarray(rho, np.complex128)
+    out = np.zeros(3)
+    for m in range(3):
+        w = np.linalg.eigvalsh(pt(rho, 1 << m))
+        n = 0.5 * (np.sum(np.abs(w)) - 1.0)
+        out[m] = 0.0 if -1e-10 < n < 0.0 else n
+    return out
+
+
 # --------------------------------------------------------- reference states
 def pure(amplitudes):
     v = np.asarray(amplitudes, complex)

@@ -1,6 +1,6 @@
-"""The drop-in executables (mipt.exe, sim_tmi.exe) on the host: argument
-handling, exit codes and messages of the reference apps
-(cpp/apps/mipt.cpp:312-414, cpp/apps/sim_tmi.cpp), the rho3.bin / info.csv
+"""The drop-in executables (mipt.exe, sim_tmi.exe, gmn.exe) on the host:
+argument handling, exit codes and messages of the reference apps
+(cpp/apps/mipt.cpp:312-414, cpp/apps/sim_tmi.cpp, cpp/apps/gmn.cpp:330-516), the rho3.bin / info.csv
 formats (cpp/include/mipt/density.hpp, cpp/apps/mipt.cpp:91-97) and the
 sim_tmi resume contract (cpp/include/mipt/tmi/resume.hpp). Nothing here
 needs a GPU: every case ends before device work (or runs none)."""
@@ -125,3 +125,33 @@ def test_sim_tmi_refuses_foreign_checkpoint(exes, tmp_path):
     other.write_text("p,tmi\n")
     r = run([tmi, "8", "2", "2", "2", "0.1", "0.3", "1", "0", str(other)], tmp_path)
     assert r.returncode == 1 and "n=12 (this run uses 8)" in r.stderr
+
+
+def test_gmn_usage_and_argument_errors(exes, tmp_path):
+    """gmn.exe's argument contract (cpp/apps/gmn.cpp:253-280,330-370); every
+    case ends before device work."""
+    gmn = os.path.join(os.path.dirname(exes[0]), "gmn.exe")
+    r = run([gmn, "--help"], tmp_path)
+    assert r.returncode == 0 and "Usage:" in r.stdout and "limit_per_p" in r.stdout
+    r = run([gmn, "3"], tmp_path)
+    assert r.returncode == 1 and "gmn.exe error: The former leading argument '3' has been removed." in r.stderr
+    r = run([gmn, "6"], tmp_path)
+    assert r.returncode == 1 and "Six-qubit retained-subsystem analysis has been removed" in r.stderr
+    r = run([gmn, "2"], tmp_path)
+    assert r.returncode == 1 and "First argument must be evaluation mode 0 or 1." in r.stderr
+    r = run([gmn, "1", "a.bin", "b.csv", "0", "extra"], tmp_path)
+    assert r.returncode == 1 and "Too many command-line arguments." in r.stderr
+    r = run([gmn, "1", "a.bin", "b.csv", "-1"], tmp_path)
+    assert r.returncode == 1 and "limit_per_p must be a non-negative integer." in r.stderr
+    r = run([gmn, "1", "missing.bin", "b.csv"], tmp_path)
+    assert r.returncode == 1 and "Could not open density-matrix file: missing.bin" in r.stderr
+    (tmp_path / "bad.bin").write_bytes(b"NOTARHO2" + bytes(64))
+    r = run([gmn, "1", "bad.bin", "b.csv"], tmp_path)
+    assert r.returncode == 1 and "Not a version-2 MIPT density-matrix file." in r.stderr
+    two = np.zeros((2, 1, 4, 4), complex)
+    two[:, 0, 0, 0] = 1
+    rho3file.write(tmp_path / "two.bin", two, p=[0.1, 0.2], p_index=[0, 1], total_qubits=4)
+    r = run([gmn, "1", "two.bin", "b.csv"], tmp_path)
+    assert r.returncode == 1 and "three-qubit 8x8 reduced density matrices" in r.stderr
+    r = run([gmn, "1", "two.bin", "b.csv"], tmp_path, {"GMN_LIMIT_PER_P": "x"})
+    assert r.returncode == 1 and "GMN_LIMIT_PER_P must be a non-negative integer." in r.stderr
