@@ -155,3 +155,59 @@ def test_gmn_usage_and_argument_errors(exes, tmp_path):
     assert r.returncode == 1 and "three-qubit 8x8 reduced density matrices" in r.stderr
     r = run([gmn, "1", "two.bin", "b.csv"], tmp_path, {"GMN_LIMIT_PER_P": "x"})
     assert r.returncode == 1 and "GMN_LIMIT_PER_P must be a non-negative integer." in r.stderr
+
+
+ENTROPY_HEADER = ("N,periods,p,requested_realizations,completed_realizations,circ_type,circuit_name,fermionic_trace,"
+                  "L_A,x,ln_x,S1_mean,S1_stddev,S1_stderr,S2_mean,S2_stddev,S2_stderr,subsystems_per_realization,"
+                  "total_subsystems")
+
+
+def entropy_rows(n, periods, p, requested, done, circ=1):
+    """A well-formed entropy.exe checkpoint (cpp/include/mipt/entropy.hpp:580-636)."""
+    rows = [ENTROPY_HEADER]
+    for kept in range(2, n // 2 + 1):
+        x = float((n / np.pi) * np.sin(np.pi * kept / n))
+        sd = 0.25
+        se = float(sd / np.sqrt(done)) if done > 1 else 0.0
+        rows.append(f'{n},{periods},{p!r},{requested},{done},{circ},"Random Haar Unitary",0,{kept},{x!r},'
+                    f'{float(np.log(x))!r},{0.5 * kept!r},{sd!r},{se!r},{0.4 * kept!r},{sd!r},{se!r},{n},{n * done}')
+    return "\n".join(rows) + "\n"
+
+
+def test_entropy_usage_argument_errors_and_checkpoints(exes, tmp_path):
+    """entropy.exe's argument contract (cpp/apps/entropy.cpp:16-60) and the
+    checkpoint refusals of cpp/include/mipt/entropy_resume.hpp:96-244; every
+    case ends before device work."""
+    ent = os.path.join(os.path.dirname(exes[0]), "entropy.exe")
+    r = run([ent, "--help"], tmp_path)
+    assert r.returncode == 0 and "Usage:" in r.stdout and "MIPT_ENTROPY_S1_MAX_LA" in r.stdout
+    r = run([ent, "8", "2"], tmp_path)
+    assert r.returncode == 2 and "Usage:" in r.stdout
+    for args, msg in [(["3", "2", "0.1", "2", "1"], "N must be at least 4"),
+                      (["8", "-1", "0.1", "2", "1"], "periods must be non-negative."),
+                      (["8", "2", "1.5", "2", "1"], "p must be in [0,1]."),
+                      (["8", "2", "0.1", "0", "1"], "realizations must be positive."),
+                      (["9", "2", "0.1", "2", "1"], "requires an even N"),
+                      (["8", "2", "0.1", "2", "0"], "not on the GB300 trajectory path"),
+                      (["8", "2", "0.1", "2", "7"], "circ_type must be one of")]:
+        r = run([ent] + args + ["out.csv"], tmp_path)
+        assert r.returncode == 1 and "entropy.exe error: " in r.stderr and msg in r.stderr, (args, r.stderr)
+    (tmp_path / "done.csv").write_text(entropy_rows(8, 2, 0.1, 2, 2))
+    r = run([ent, "8", "2", "0.1", "2", "1", "done.csv"], tmp_path)
+    assert r.returncode == 0 and "already complete. Nothing to do." in r.stdout, r.stdout + r.stderr
+    r = run([ent, "10", "2", "0.1", "2", "1", "done.csv"], tmp_path)
+    assert r.returncode == 1 and "The checkpoint belongs to a different N." in r.stderr
+    r = run([ent, "8", "2", "0.2", "2", "1", "done.csv"], tmp_path)
+    assert r.returncode == 1 and "different p" in r.stderr
+    r = run([ent, "8", "2", "0.1", "2", "1", "done.csv"], tmp_path, {"MIPT_ENTROPY_S1_MAX_LA": "3"})
+    assert r.returncode == 1 and "records S1 for L_A up to 4 but this run is configured for L_A up to 3" in r.stderr
+    lines = entropy_rows(8, 2, 0.1, 4, 3).splitlines()
+    cells = lines[1].split(",")
+    cells[16] = "0.2"  # S2_stderr no longer stddev / sqrt(3)
+    lines[1] = ",".join(cells)
+    (tmp_path / "edited.csv").write_text("\n".join(lines) + "\n")
+    r = run([ent, "8", "2", "0.1", "4", "1", "edited.csv"], tmp_path)
+    assert r.returncode == 1 and "two runs were concatenated" in r.stderr, r.stderr
+    (tmp_path / "other.csv").write_text("a,b\n1,2\n")
+    r = run([ent, "8", "2", "0.1", "2", "1", "other.csv"], tmp_path)
+    assert r.returncode == 1 and "different column layout" in r.stderr

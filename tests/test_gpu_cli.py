@@ -96,3 +96,74 @@ def test_sim_tmi_exe_resumes_to_the_same_file(exes, tmp_path):
     r = run(args, tmp_path, True)
     assert "RESUMED" in r.stderr
     assert path.read_text() == full
+
+
+def _entropy_rows(path):
+    lines = path.read_text().splitlines()
+    head = lines[0].split(",")
+    rows = []
+    for ln in lines[1:]:
+        cells = ln.replace('"Random Haar Unitary"', "haar").split(",")
+        rows.append({h: (float(c) if h != "circuit_name" else c) for h, c in zip(head, cells)})
+    return head, rows
+
+
+def test_entropy_exe_matches_oracle(orc, tmp_path):
+    """entropy.exe (FP64 path) against the oracle's final states for the same
+    trajectory seeds: per L_A the S1 / S2 (natural log) of the N cyclic
+    blocks, averaged over translations, then mean / sample stddev / stderr
+    over trajectories (cpp/include/mipt/entropy.hpp:580-636)."""
+    exe = os.path.join(ROOT, "mipt_gb300", "_build", "entropy.exe")
+    n, periods, p, R = 8, 3, 0.3, 5
+    run([exe, str(n), str(periods), str(p), str(R), "1", "e.csv"], tmp_path, True, {"MIPT_GB300_BATCH": "2"})
+    head, rows = _entropy_rows(tmp_path / "e.csv")
+    assert len(rows) == n // 2 - 1
+    per = {k: ([], []) for k in range(2, n // 2 + 1)}
+    for r in range(R):
+        psi = orc.run_trajectory(orc.trajectory_seed(SEED, r), n, periods, p, closed=True, want_state=True)["psi"]
+        for kept in per:
+            s1 = s2 = 0.0
+            for c in range(n):
+                rho = orc.rdm(psi, [(c + j) % n for j in range(kept)])
+                w = np.linalg.eigvalsh(rho)
+                w = w[w > 1e-15]
+                s1 += -np.sum(w * np.log(w)) / n
+                s2 += -np.log(np.sum(np.abs(rho) ** 2)) / n
+            per[kept][0].append(s1)
+            per[kept][1].append(s2)
+    for row in rows:
+        kept = int(row["L_A"])
+        assert (row["N"], row["periods"], row["requested_realizations"], row["completed_realizations"]) == (n, periods, R, R)
+        assert row["p"] == p and row["circ_type"] == 1 and row["subsystems_per_realization"] == n
+        x = n / np.pi * np.sin(np.pi * kept / n)
+        assert abs(row["x"] - x) < 1e-14 and abs(row["ln_x"] - np.log(x)) < 1e-14
+        for name, vals in (("S1", per[kept][0]), ("S2", per[kept][1])):
+            v = np.array(vals)
+            assert abs(row[name + "_mean"] - v.mean()) < 1e-9, (kept, name)
+            assert abs(row[name + "_stddev"] - v.std(ddof=1)) < 1e-9, (kept, name)
+            assert abs(row[name + "_stderr"] - v.std(ddof=1) / np.sqrt(R)) < 1e-9, (kept, name)
+
+
+def test_entropy_exe_resumes_its_checkpoint(tmp_path):
+    """A 2-trajectory checkpoint re-labelled as part of a 5-trajectory run and
+    resumed gives the same file as an uninterrupted 5-trajectory run (up to
+    the rounding of restoring the accumulators from mean and stddev); with
+    MIPT_ENTROPY_S1_MAX_LA=2 the larger blocks report NaN S1."""
+    exe = os.path.join(ROOT, "mipt_gb300", "_build", "entropy.exe")
+    base = ["8", "2", "0.2"]
+    run([exe] + base + ["2", "1", "part.csv"], tmp_path, True)
+    text = (tmp_path / "part.csv").read_text().splitlines()
+    relabel = [text[0]] + [ln.replace("8,2,0.20000000000000001,2,", "8,2,0.20000000000000001,5,", 1) for ln in text[1:]]
+    (tmp_path / "resumed.csv").write_text("\n".join(relabel) + "\n")
+    r = run([exe] + base + ["5", "1", "resumed.csv"], tmp_path, True)
+    assert "Resuming from resumed.csv: 2/5" in r.stdout
+    run([exe] + base + ["5", "1", "full.csv"], tmp_path, True)
+    _, a = _entropy_rows(tmp_path / "resumed.csv")
+    _, b = _entropy_rows(tmp_path / "full.csv")
+    for ra, rb in zip(a, b):
+        for k, v in ra.items():
+            if isinstance(v, float):
+                assert abs(v - rb[k]) <= 1e-12 * max(1.0, abs(rb[k])), (k, v, rb[k])
+    run([exe] + base + ["2", "1", "s1cap.csv"], tmp_path, True, {"MIPT_ENTROPY_S1_MAX_LA": "2"})
+    _, c = _entropy_rows(tmp_path / "s1cap.csv")
+    assert np.isfinite(c[0]["S1_mean"]) and all(np.isnan(row["S1_mean"]) for row in c[1:])
