@@ -216,6 +216,17 @@ typedef struct mipt_gb300_batch_config
 typedef struct mipt_gb300_batch mipt_gb300_batch;
 
 int mipt_gb300_batch_create(const mipt_gb300_batch_config *config, int capacity, mipt_gb300_batch **out);
+
+/* Tile-shape autotuner (no reference counterpart). Times one cycle of every
+ * layer colour of the geometry (passes only, fixed gates) on `trajectories`
+ * scratch states for each candidate local-qubit count per pass tile (the
+ * default, 14 FP32 / 13 FP64, and the two below it where they fit) and writes
+ * the fastest to *best_tile; candidates[i] and ms_per_cycle[i] (nullable, at
+ * least 3 entries) receive the timings, *candidate_count their number. A batch
+ * created with tile_qubits = 0 takes its tile from a table measured this way
+ * on GB300 (mipt_gb300/tune_tiles.py), or tunes live with MIPT_GB300_AUTOTUNE=1. */
+int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, int lattice_y, int trajectories,
+                             int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count);
 void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
 
 /* Draw `count` Haar trajectories (trajectory i from seeds[i] with

@@ -88,6 +88,7 @@ def lib():
     L.mipt_gb300_lattice_bonds.argtypes = [ci, ci, ci, vp, vp]
     L.mipt_gb300_gmn_solve.argtypes = [vp, vp, ci, vp, vp, vp, vp, vp]
     L.mipt_gb300_cut_negativities.argtypes = [vp, ci, vp]
+    L.mipt_gb300_autotune_tile.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp]
     L.mipt_gb300_draw_haar_lattice.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_run_haar.argtypes = [vp, vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
@@ -392,6 +393,19 @@ def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6
     if want_solution:
         out["solution"] = ri_to_rho(sol)
     return out
+
+
+def autotune_tile(n, fp64=False, closed=True, lattice=None, trajectories=4):
+    """Times every candidate pass-tile size for this geometry (passes only)
+    and returns (best_tile, {tile: ms per cycle of all layer colours})."""
+    lx, ly = lattice if lattice else (0, 1)
+    best = ctypes.c_int()
+    cand = np.zeros(3, np.int32)
+    ms = np.zeros(3)
+    cnt = ctypes.c_int()
+    _check(lib().mipt_gb300_autotune_tile(n, int(fp64), int(closed), lx, ly, trajectories, ctypes.byref(best),
+                                          _p(cand), _p(ms), ctypes.byref(cnt)))
+    return best.value, {int(c): float(t) for c, t in zip(cand[: cnt.value], ms[: cnt.value])}
 
 
 def cut_negativities(rho):

@@ -10,6 +10,8 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <tuple>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -564,6 +566,178 @@ int measure_collapse(void *state, int n, int q, double u, int *outcome, double *
 int default_tile_qubits(bool fp64) { return fp64 ? 13 : 14; }
 constexpr int kCoalesceQubits = 4;
 
+// Bond lists of every colour of a batch geometry (1-D brickwork: even and odd
+// layers; lattice: four colours).
+std::vector<std::vector<Bond>> geometry_bonds(int n, int closed, int lx, int ly)
+{
+    std::vector<std::vector<Bond>> out;
+    if (ly > 1)
+    {
+        for (int colour = 0; colour < 4; ++colour)
+        {
+            out.emplace_back();
+            for (const auto &pr : lattice_bonds(lx, ly, colour)) out.back().push_back(Bond{pr.first, pr.second});
+        }
+    }
+    else
+        for (int colour = 0; colour < 2; ++colour)
+        {
+            out.emplace_back();
+            const int stop = (closed && colour == 1 && n > 2) ? n : n - 1;
+            for (int i = colour; i < stop; i += 2) out.back().push_back(Bond{i, (i + 1) % n});
+        }
+    return out;
+}
+
+// Tile-shape autotuner: times one cycle of every layer colour (passes only)
+// on `trajectories` scratch states for each candidate local-qubit count and
+// returns the fastest. Candidates: the default and the two below it, where the
+// tile still fits the geometry.
+template <typename Real>
+int autotune_tile_impl(int n, int closed, int lx, int ly, int trajectories, int *best, double *ms, int *cand,
+                       int *ncand)
+{
+    const int def = default_tile_qubits(sizeof(Real) == 8);
+    const auto bonds = geometry_bonds(n, closed, lx, ly);
+    std::vector<int> ks;
+    for (int k = def - 2; k <= def; ++k)
+    {
+        const int kk = std::min(k, n);
+        if (n - kk + kCoalesceQubits > 20) continue;
+        if (std::find(ks.begin(), ks.end(), kk) == ks.end()) ks.push_back(kk);
+    }
+    const std::size_t dim = std::size_t{1} << n;
+    DevBuf states, gates, err;
+    MG_CUDA(states.ensure(sizeof(Cx<Real>) * dim * static_cast<std::size_t>(trajectories)));
+    MG_CUDA(err.ensure(sizeof(int)));
+    MG_CUDA(cudaMemset(err.p, 0, sizeof(int)));
+    // Every bond gets the same fixed unitary, H x H (timing does not depend on it).
+    const int G = n;
+    std::vector<Cx<Real>> h(static_cast<std::size_t>(G) * 16);
+    for (int g = 0; g < G; ++g)
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c)
+                h[g * 16 + r * 4 + c] = Cx<Real>{static_cast<Real>((__builtin_popcount(r & c) & 1) ? -0.5 : 0.5), Real(0)};
+    MG_CUDA(gates.ensure(sizeof(Cx<Real>) * h.size()));
+    MG_CUDA(cudaMemcpy(gates.p, h.data(), sizeof(Cx<Real>) * h.size(), cudaMemcpyHostToDevice));
+    MG_CUDA(launch_init_zero<Real>(states.as<Cx<Real>>(), dim, trajectories, nullptr));
+    cudaEvent_t a, b;
+    MG_CUDA(cudaEventCreate(&a));
+    MG_CUDA(cudaEventCreate(&b));
+    double best_ms = -1.0;
+    int count = 0;
+    for (int k : ks)
+    {
+        std::vector<std::vector<PassPlan>> plans;
+        try
+        {
+            for (const auto &bl : bonds) plans.push_back(plan_layer(n, bl, k, kCoalesceQubits, register_bits<Real>()));
+        }
+        catch (const std::exception &)
+        {
+            continue;
+        }
+        auto cycle = [&]() -> cudaError_t {
+            for (const auto &pl : plans)
+                for (const auto &pp : pl)
+                {
+                    cudaError_t e = launch_pass<Real>(states.as<Cx<Real>>(), trajectories, pp, gates.as<Cx<Real>>(), 0,
+                                                      nullptr, 0, nullptr, 0, nullptr, 0, err.as<int>(), nullptr);
+                    if (e != cudaSuccess) return e;
+                }
+            return cudaSuccess;
+        };
+        MG_CUDA(cycle());
+        MG_CUDA(cudaEventRecord(a));
+        for (int rep = 0; rep < 3; ++rep) MG_CUDA(cycle());
+        MG_CUDA(cudaEventRecord(b));
+        MG_CUDA(cudaEventSynchronize(b));
+        float t = 0.f;
+        MG_CUDA(cudaEventElapsedTime(&t, a, b));
+        const double per = t / 3.0;
+        if (ms) ms[count] = per;
+        if (cand) cand[count] = k;
+        ++count;
+        if (best_ms < 0.0 || per < best_ms)
+        {
+            best_ms = per;
+            *best = k;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    int e_flag = 0;
+    MG_CUDA(cudaMemcpy(&e_flag, err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e_flag) return fail(MIPT_GB300_E_INTERNAL, "tile load wait timed out");
+    if (ncand) *ncand = count;
+    if (count == 0) *best = def;
+    return 0;
+}
+
+// Tile choice of a batch created with tile_qubits = 0: the table below,
+// measured on GB300 with mipt_gb300/tune_tiles.py (the fastest candidate per
+// geometry; the default where the table has no entry), or, with
+// MIPT_GB300_AUTOTUNE=1, a live autotune of this geometry (cached per
+// process). The table keeps results reproducible run to run: the tile shape
+// changes the order in which disjoint gates round.
+struct TileChoice
+{
+    int n, fp64, lattice, tile;
+};
+constexpr TileChoice kTunedTiles[] = {
+    // {n, fp64, lattice, tile}: FP32 keeps 14 everywhere (2-30 % ahead of 12
+    // and 13 at batch-sized grids); FP64 is within 1-2 % across 11..13.
+    {14, 0, 0, 14},
+    {16, 0, 0, 14},
+    {18, 0, 0, 14},
+    {20, 0, 0, 14},
+    {22, 0, 0, 14},
+    {24, 0, 0, 14},
+    {26, 0, 0, 14},
+    {28, 0, 0, 14},
+    {30, 0, 0, 14},
+    {14, 1, 0, 11},
+    {16, 1, 0, 12},
+    {18, 1, 0, 12},
+    {20, 1, 0, 12},
+    {22, 1, 0, 13},
+    {24, 1, 0, 12},
+    {26, 1, 0, 12},
+    {28, 1, 0, 12},
+    {28, 0, 1, 14},
+    {20, 0, 1, 14},
+};
+
+int chosen_tile(const mipt_gb300_batch_config &cfg, int capacity)
+{
+    const bool fp64 = cfg.fp64 != 0;
+    const bool lattice = cfg.lattice_y > 1;
+    const char *v = std::getenv("MIPT_GB300_AUTOTUNE");
+    if (v && v[0] == '1')
+    {
+        static std::mutex m;
+        static std::map<std::tuple<int, int, int, int, int>, int> cache;
+        const auto key = std::make_tuple(cfg.n_qubits, cfg.fp64, cfg.closed, cfg.lattice_x, cfg.lattice_y);
+        std::lock_guard<std::mutex> lock(m);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+        const std::size_t state = (std::size_t{1} << cfg.n_qubits) * (fp64 ? 16 : 8);
+        const int traj = static_cast<int>(std::max<std::size_t>(
+            1, std::min<std::size_t>(static_cast<std::size_t>(capacity), (std::size_t{4} << 30) / state)));
+        int best = default_tile_qubits(fp64);
+        const int rc = fp64 ? autotune_tile_impl<double>(cfg.n_qubits, cfg.closed, cfg.lattice_x, cfg.lattice_y, traj,
+                                                         &best, nullptr, nullptr, nullptr)
+                            : autotune_tile_impl<float>(cfg.n_qubits, cfg.closed, cfg.lattice_x, cfg.lattice_y, traj,
+                                                        &best, nullptr, nullptr, nullptr);
+        if (rc != 0) best = default_tile_qubits(fp64);
+        cache[key] = best;
+        return best;
+    }
+    for (const TileChoice &t : kTunedTiles)
+        if (t.n == cfg.n_qubits && t.fp64 == (fp64 ? 1 : 0) && t.lattice == (lattice ? 1 : 0)) return t.tile;
+    return default_tile_qubits(fp64);
+}
+
 } // namespace
 
 namespace mg
@@ -1046,6 +1220,20 @@ int set_rho3_subs(mipt_gb300_batch *b, const std::vector<int> &subs)
 } // namespace
 
 extern "C" {
+int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, int lattice_y, int trajectories,
+                             int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count)
+{
+    if (!best_tile || trajectories < 1 || n_qubits < 4 || n_qubits > 30 ||
+        (lattice_y > 1 && lattice_x * lattice_y != n_qubits))
+        return fail(MIPT_GB300_E_INVALID, "bad autotune arguments");
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return fail(MIPT_GB300_E_NODEVICE, "no CUDA device");
+    return fp64 ? autotune_tile_impl<double>(n_qubits, closed, lattice_x, lattice_y, trajectories, best_tile,
+                                             ms_per_cycle, candidates, candidate_count)
+                : autotune_tile_impl<float>(n_qubits, closed, lattice_x, lattice_y, trajectories, best_tile,
+                                            ms_per_cycle, candidates, candidate_count);
+}
+
 int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mipt_gb300_batch **out)
 {
     if (!cfg || !out || capacity <= 0) return fail(MIPT_GB300_E_INVALID, "null config or capacity <= 0");
@@ -1071,35 +1259,23 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     b->capacity = capacity;
     b->T = 2 * cfg->periods;
     b->G = n / 2;
-    b->kmax = cfg->tile_qubits > 0 ? std::min(cfg->tile_qubits, kMaxLocal) : default_tile_qubits(cfg->fp64 != 0);
+    b->kmax = cfg->tile_qubits > 0 ? std::min(cfg->tile_qubits, kMaxLocal) : chosen_tile(*cfg, capacity);
     b->cmin = kCoalesceQubits;
     if (n - std::min(b->kmax, n) + b->cmin > 20) return fail(MIPT_GB300_E_INVALID, "tile too small for this n");
     b->dim = 1ull << n;
     b->elem = cfg->fp64 ? 16 : 8;
     b->lattice = lattice;
     b->ncolour = lattice ? 4 : 2;
-    for (int colour = 0; colour < b->ncolour; ++colour)
+    try
     {
-        std::vector<Bond> bonds;
-        try
-        {
-            if (lattice)
-            {
-                for (const auto &pr : lattice_bonds(cfg->lattice_x, cfg->lattice_y, colour))
-                    bonds.push_back(Bond{pr.first, pr.second});
-            }
-            else
-            {
-                const int stop = (cfg->closed && colour == 1 && n > 2) ? n : n - 1;
-                for (int i = colour; i < stop; i += 2) bonds.push_back(Bond{i, (i + 1) % n});
-            }
-            b->plan[colour] = plan_layer(n, bonds, b->kmax, b->cmin,
+        const auto bonds = geometry_bonds(n, cfg->closed, cfg->lattice_x, cfg->lattice_y);
+        for (int colour = 0; colour < b->ncolour; ++colour)
+            b->plan[colour] = plan_layer(n, bonds[colour], b->kmax, b->cmin,
                                          cfg->fp64 ? register_bits<double>() : register_bits<float>());
-        }
-        catch (const std::exception &e)
-        {
-            return fail(MIPT_GB300_E_INVALID, e.what());
-        }
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
     }
     // Observable requests of one evaluation point (trajectory 0; shifted per trajectory).
     auto range = [n](int a, int c) {
