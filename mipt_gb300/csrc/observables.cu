@@ -1369,15 +1369,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // e = 16c..16c+15 as 32 floats [Re psi(a, e) .. | Im psi(a, e) ..], TF32 hi
 // parts in rows [0, R) and lo parts in rows [R, 2R). The Gram then only
 // streams 128-byte rows into 128B-swizzled K-major stages by TMA.
-constexpr int TP_STAGES = 4;
+constexpr int TP_C = 128;                                 // complex columns of a rho block (B rows)
+constexpr int TP_N = 2 * TP_C;                            // TMEM columns per buffer: Re, then Im
+constexpr int TP_BUFS = 2;                                // accumulation buffers (512 TMEM columns)
+constexpr int TP_DCOLS = TP_N / (TC_PWARPS / 4);          // D columns drained per thread
+constexpr int TP_STAGES = 3;
 constexpr int TP_A_BYTES = TCM * 128;                     // hi or lo half of A: 16 KB
-constexpr int TP_B_BYTES = TCC * 128;                     // hi or lo half of B: 8 KB
-constexpr int TP_STAGE = 2 * TP_A_BYTES + 2 * TP_B_BYTES; // 48 KB
+constexpr int TP_B_BYTES = TP_C * 128;                    // hi or lo half of B: 16 KB
+constexpr int TP_STAGE = 2 * TP_A_BYTES + 2 * TP_B_BYTES; // 64 KB
 constexpr std::size_t TP_SMEM = static_cast<std::size_t>(TP_STAGES) * TP_STAGE + 1024;
 constexpr int TP_THREADS = (TC_PWARPS + 2) * 32;          // drain warps, MMA warp, TMA warp
-// D = F32, A = B = TF32, K-major, N = TCC (Re or Im half of the block), M = 128;
+static_assert(TP_BUFS * TP_N <= 512 && TP_DCOLS % 32 == 0, "tensor memory or drain split");
+// D = F32, A = B = TF32, K-major, N = TP_C (the Re or Im half of the block), M = 128;
 // bit 13 negates A.
-constexpr std::uint32_t kTpIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TCC >> 3) << 17) | ((TCM >> 4) << 24);
+constexpr std::uint32_t kTpIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TP_C >> 3) << 17) | ((TCM >> 4) << 24);
 constexpr std::uint32_t kTpIdescNegA = kTpIdesc | (1u << 13);
 
 // One thread per operand row: 16 amplitudes of job j's state (pending
@@ -1435,20 +1440,21 @@ __device__ __forceinline__ void tp_mma(std::uint32_t d, std::uint64_t a, std::ui
                  : "memory");
 }
 
-// Purity partials of one 128 x 64 block of rho for job job0 + blockIdx.z from
-// the pre-split rows of the group's job blockIdx.z (tmap: 2-D FP32 view, 32 floats per row, box 32 x 64,
-// 128-byte swizzle). Warp TC_PWARPS issues the MMAs (Re rho = Re.Re + Im.Im
-// into TMEM columns [0, 64), Im rho = Im.Re - Re.Im into [64, 128), each term
-// as 3 TF32 products), warp TC_PWARPS + 1 the TMA loads, and warps
-// 0..TC_PWARPS-1 drain the TMEM segments into FP32 registers and reduce the
+// Purity partials of one 128 x 128 block of rho for job job0 + blockIdx.z
+// from the pre-split rows of the group's job blockIdx.z (tmap: 2-D FP32 view,
+// 32 floats per row, box 32 x 64, 128-byte swizzle). Warp TC_PWARPS issues the
+// MMAs (Re rho = Re.Re + Im.Im into TMEM columns [0, 128), Im rho = Im.Re -
+// Re.Im into [128, 256) of a buffer, each term as 3 TF32 products, N = 128),
+// warp TC_PWARPS + 1 the TMA loads (8 boxes per 64 KB stage), and warps
+// 0..TC_PWARPS-1 drain the two TMEM buffers into FP32 registers and reduce the
 // weighted squares as k_gram_tc does. Every wait is bounded (bit 4 of *err).
 __global__ void __launch_bounds__(TP_THREADS, 1)
     k_gram_tc_pre(int n, int k, int job0, double *__restrict__ pur_out, int *__restrict__ err, std::uint32_t lo_rows,
                   const __grid_constant__ CUtensorMap tmap)
 {
     extern __shared__ __align__(1024) unsigned char tp_raw[];
-    __shared__ __align__(8) std::uint64_t full_bar[TP_STAGES], empty_bar[TP_STAGES], seg_bar[TC_TMEM_BUFS],
-        drained_bar[TC_TMEM_BUFS];
+    __shared__ __align__(8) std::uint64_t full_bar[TP_STAGES], empty_bar[TP_STAGES], seg_bar[TP_BUFS],
+        drained_bar[TP_BUFS];
     __shared__ std::uint32_t tmem_base;
     __shared__ double red[TC_PWARPS];
     __shared__ volatile int abort_flag;
@@ -1466,7 +1472,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
             mbar_init(&full_bar[st], 1);
             mbar_init(&empty_bar[st], 1);
         }
-        for (int b = 0; b < TC_TMEM_BUFS; ++b)
+        for (int b = 0; b < TP_BUFS; ++b)
         {
             mbar_init(&seg_bar[b], 1);
             mbar_init(&drained_bar[b], TC_PWARPS);
@@ -1477,7 +1483,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
     if (warp == TC_PWARPS)
     {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sm_addr(&tmem_base)),
-                     "n"(TC_TMEM_COLS)
+                     "n"(TP_BUFS * TP_N)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1485,27 +1491,27 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const std::uint32_t tmem = tmem_base;
-    const int r0 = tr * TCM, c0 = tc * TCM + static_cast<int>(blockIdx.y) * TCC;
+    const int r0 = tr * TCM, c0 = tc * TCM;
     const int nchunks = 1 << (n - k - 4);
     const int nseg = (nchunks + TC_SEG - 1) / TC_SEG;
 
     if (warp < TC_PWARPS)
     {
-        float acc[TC_DCOLS];
+        float acc[TP_DCOLS];
 #pragma unroll
-        for (int i = 0; i < TC_DCOLS; ++i) acc[i] = 0.f;
+        for (int i = 0; i < TP_DCOLS; ++i) acc[i] = 0.f;
         const std::uint32_t lane_base = static_cast<std::uint32_t>((warp & 3) * 32) << 16;
-        const int col_base = (warp >> 2) * TC_DCOLS;
+        const int col_base = (warp >> 2) * TP_DCOLS;
         for (int seg = 0; seg < nseg && !abort_flag; ++seg)
         {
-            const int buf = seg % TC_TMEM_BUFS;
-            if (!mbar_wait(&seg_bar[buf], (seg / TC_TMEM_BUFS) & 1, &abort_flag, err)) break;
+            const int buf = seg % TP_BUFS;
+            if (!mbar_wait(&seg_bar[buf], (seg / TP_BUFS) & 1, &abort_flag, err)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
-            for (int cb = 0; cb < TC_DCOLS / 32; ++cb)
+            for (int cb = 0; cb < TP_DCOLS / 32; ++cb)
             {
                 std::uint32_t v[32];
-                const std::uint32_t taddr = tmem + lane_base + buf * TCN + col_base + cb * 32;
+                const std::uint32_t taddr = tmem + lane_base + buf * TP_N + col_base + cb * 32;
                 asm volatile(
                     "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                     "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -1528,9 +1534,9 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
         if (!abort_flag)
         {
 #pragma unroll
-            for (int i = 0; i < TC_DCOLS; ++i)
+            for (int i = 0; i < TP_DCOLS; ++i)
             {
-                const int c = c0 + ((col_base + i) & (TCC - 1));
+                const int c = c0 + ((col_base + i) & (TP_C - 1));
                 const double w = (r > c) ? 2.0 : ((r == c) ? 1.0 : 0.0);
                 const double x = static_cast<double>(acc[i]);
                 sum += w * x * x;
@@ -1545,16 +1551,16 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
         {
             const int st = chunk % TP_STAGES;
             const int seg = chunk / TC_SEG;
-            const int buf = seg % TC_TMEM_BUFS;
-            if (chunk % TC_SEG == 0 && seg >= TC_TMEM_BUFS &&
-                !mbar_wait(&drained_bar[buf], ((seg / TC_TMEM_BUFS) - 1) & 1, &abort_flag, err))
+            const int buf = seg % TP_BUFS;
+            if (chunk % TC_SEG == 0 && seg >= TP_BUFS &&
+                !mbar_wait(&drained_bar[buf], ((seg / TP_BUFS) - 1) & 1, &abort_flag, err))
                 break;
             if (!mbar_wait(&full_bar[st], (chunk / TP_STAGES) & 1, &abort_flag, err)) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const std::uint32_t base = sm_addr(smem + st * TP_STAGE);
             const std::uint32_t Ahi = base, Alo = base + TP_A_BYTES;
             const std::uint32_t Bhi = base + 2 * TP_A_BYTES, Blo = Bhi + TP_B_BYTES;
-            const std::uint32_t dre = tmem + buf * TCN, dim = dre + TCC;
+            const std::uint32_t dre = tmem + buf * TP_N, dim = dre + TP_C;
             const bool first = chunk % TC_SEG == 0;
             // Re rho: 32 real K (16 Re then 16 Im) in four K = 8 steps.
 #pragma unroll
@@ -1600,13 +1606,14 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
                          : "memory");
             const std::uint32_t base = sm_addr(smem + st * TP_STAGE);
             const int yb = static_cast<int>((static_cast<std::uint32_t>(job) * nchunks + chunk) << k);
-            const std::uint32_t dst[6] = {base, base + TP_A_BYTES / 2, base + TP_A_BYTES,
-                                          base + TP_A_BYTES + TP_A_BYTES / 2, base + 2 * TP_A_BYTES,
-                                          base + 2 * TP_A_BYTES + TP_B_BYTES};
-            const int ys[6] = {yb + r0, yb + r0 + 64, static_cast<int>(lo_rows) + yb + r0,
-                               static_cast<int>(lo_rows) + yb + r0 + 64, yb + c0, static_cast<int>(lo_rows) + yb + c0};
+            const int lo = static_cast<int>(lo_rows);
+            const std::uint32_t Bb = base + 2 * TP_A_BYTES;
+            const std::uint32_t dst[8] = {base, base + 8192, base + TP_A_BYTES, base + TP_A_BYTES + 8192,
+                                          Bb, Bb + 8192, Bb + TP_B_BYTES, Bb + TP_B_BYTES + 8192};
+            const int ys[8] = {yb + r0, yb + r0 + 64, lo + yb + r0, lo + yb + r0 + 64,
+                               yb + c0, yb + c0 + 64, lo + yb + c0, lo + yb + c0 + 64};
 #pragma unroll
-            for (int b = 0; b < 6; ++b)
+            for (int b = 0; b < 8; ++b)
                 asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
                              "%3}], [%4];" ::"r"(dst[b]),
                              "l"(tm), "r"(0), "r"(ys[b]), "r"(bar)
@@ -1623,12 +1630,12 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
     {
         double t = 0.0;
         for (int w = 0; w < TC_PWARPS; ++w) t += red[w];
-        pur_out[(static_cast<std::size_t>(job0 + job) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] = t;
+        pur_out[static_cast<std::size_t>(job0 + job) * gridDim.x + blockIdx.x] = t;
     }
     if (warp == TC_PWARPS)
     {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TC_TMEM_COLS)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TP_BUFS * TP_N)
                      : "memory");
     }
 }
@@ -1729,13 +1736,13 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
                                                static_cast<float4 *>(rows), lo_rows);
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
-            dim3 grid(gram_tc_blocks(k), 2, g);
+            dim3 grid(gram_tc_blocks(k), 1, g);
             k_gram_tc_pre<<<grid, TP_THREADS, TP_SMEM, s>>>(n, k, g0, static_cast<double *>(scratch), err,
                                                             static_cast<std::uint32_t>(lo_rows), map);
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
-        k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
+        k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), gram_tc_blocks(k), purity_out);
         return cudaGetLastError();
     }
     CUtensorMap map;
