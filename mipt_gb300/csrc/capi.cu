@@ -245,7 +245,7 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
                 // Low cuts: TF32 operand rows split once per observation, in
                 // job groups of at most kMaxRowsBytes.
-                bool presplit = low_cut && k <= 13 && gram_tc_presplit_enabled();
+                bool presplit = low_cut && k <= gram_tc_presplit_max_k() && gram_tc_presplit_enabled();
                 if (presplit)
                 {
                     const std::size_t per_job = gram_tc_rows_bytes_per_job(n);

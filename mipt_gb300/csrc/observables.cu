@@ -1694,6 +1694,15 @@ bool gram_tc_presplit_enabled()
 
 std::size_t gram_tc_rows_bytes_per_job(int n) { return (std::size_t{16}) << n; }
 
+int gram_tc_presplit_max_k()
+{
+    static const int k = [] {
+        const char *v = std::getenv("MIPT_GB300_TC_PRESPLIT_MAX_K");
+        return (v && *v) ? std::atoi(v) : 14;
+    }();
+    return k;
+}
+
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
                            std::size_t scratch_bytes, int *err, cudaStream_t s, int tma_traj_count, void *rows,
@@ -1704,9 +1713,11 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
     const int tiles = gram_tc_tiles(k);
     if (gram_tc_scratch_bytes(k, njobs) > scratch_bytes) return cudaErrorInvalidValue;
     const std::size_t per_job = gram_tc_rows_bytes_per_job(n);
-    // Measured: faster at k = 12 (L = 24 half cut, 85 -> 63 ms for 32 states);
-    // slower at k = 14 (L = 28), where a state's 4 GB of rows outgrow L2.
-    if (tma_traj_count > 0 && k <= 13 && rows != nullptr && rows_bytes >= per_job && tensor_map_encoder() != nullptr &&
+    // Measured against the gathered path: L = 24 half cut (k = 12) 85 -> 39 ms
+    // for 32 states, L = 28 lattice half (k = 14) 1.8x faster per layer; k = 15
+    // and 16 stay on the gathered path (not measured).
+    if (tma_traj_count > 0 && k <= gram_tc_presplit_max_k() && rows != nullptr && rows_bytes >= per_job &&
+        tensor_map_encoder() != nullptr &&
         (reinterpret_cast<std::uintptr_t>(rows) & 15u) == 0)
     {
         // Pre-split operand rows, jobs in groups that fit `rows`.

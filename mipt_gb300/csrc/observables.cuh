@@ -67,11 +67,12 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
 // tma_traj_count state vectors; the operands then arrive by TMA.
 bool gram_tc_supported(int n, int k);
 std::size_t gram_tc_scratch_bytes(int k, int njobs);
-// With tma_traj_count > 0, k <= 13 and a `rows` buffer of at least
+// With tma_traj_count > 0, k <= gram_tc_presplit_max_k() and a `rows` buffer of at least
 // gram_tc_rows_bytes_per_job(n) bytes (16-byte aligned), the operands are
 // first split into TF32 hi/lo rows (jobs in groups that fit the buffer) and
 // the Gram streams them by TMA alone; MIPT_GB300_TC_PRESPLIT=0 turns that off.
 bool gram_tc_presplit_enabled();
+int gram_tc_presplit_max_k(); // largest k for the pre-split path (MIPT_GB300_TC_PRESPLIT_MAX_K, default 14)
 std::size_t gram_tc_rows_bytes_per_job(int n);
 cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs, int njobs, int k,
                            const Collapse *collapse, std::size_t collapse_stride, double *purity_out, void *scratch,
