@@ -32,6 +32,7 @@ UNIT = "trajectory-layers/s"
 N_QUBITS = 24
 PERIODS = 24
 PASS_TRAFFIC_PER_TRAJ = 239.3e6  # DRAM bytes per trajectory per pass launch (ncu)
+GRAM_TENSOR_PIPE_PCT = 66.5  # ncu sm__pipe_tensor_cycles_active of the final S_2 Gram
 P_GRID = np.linspace(0.05, 0.35, 16)
 
 
@@ -255,8 +256,11 @@ def run_gb300(args):
         # trajectory for the Hermitian half (d_A = d_B = 2^12).
         obs_ms = stats["observables"][0]
         gram_flops = B * 4.0 * float(1 << (N_QUBITS // 2)) ** 3
-        gram = {"kernel": "k_gram_tc (tcgen05 3xTF32)", "ms_per_step": obs_ms,
-                "alg_tflops": gram_flops / (obs_ms / 1000.0) / 1e12 if obs_ms > 0 else None}
+        gram = {"kernel": "k_tf32_rows + k_gram_tc_pre (tcgen05 3xTF32, TMA-fed)", "ms_per_step": obs_ms,
+                "alg_tflops": gram_flops / (obs_ms / 1000.0) / 1e12 if obs_ms > 0 else None,
+                "tensor_pipe_active_pct": GRAM_TENSOR_PIPE_PCT,
+                "tensor_pipe_source": "ncu sm__pipe_tensor_cycles_active, 2-trajectory capture of the same kernel "
+                                      "(profiles/k_gram_tc_L24_halfcut_batch2.md)"}
 
         # Plain FP64 per-trajectory path on the same GPU, one trajectory.
         plain = mg.Batch(N_QUBITS, PERIODS, capacity=1, fp64=True, observables=mg.OBS_S2_HALF)
