@@ -441,13 +441,18 @@ def config4():
     rho = np.concatenate([traj, gmn_warm.mixtures(len(traj), 5)])
     cold, dt = _timed(lambda: mg.gmn_solve(rho, gap_tol=1e-6, max_iter=3000, check_every=10))
     ok = cold["iters"] > 0
+    # The learned warm start, at the penalty it is trained for, against a
+    # cold start at that same penalty.
+    ws = gmn_warm.WARM_SIGMA
     train = gmn_warm.mixtures(24000, 6)
-    x, t, _ = gmn_warm.solve_pairs(train, gap_tol=1e-6, max_iter=3000)
+    x, t, _ = gmn_warm.solve_pairs(train, gap_tol=1e-6, max_iter=3000, sigma=ws)
     model = gmn_warm.WarmStartModel(seed=0)
     (_, tdt) = _timed(lambda: model.fit(x, t))
     guess = model.predict(rho)
-    warm, wdt = _timed(lambda: mg.gmn_solve(rho, warm_start=guess, gap_tol=1e-6, max_iter=3000, check_every=10))
-    both = ok & (warm["iters"] > 0)
+    cold_ws, cwdt = _timed(lambda: mg.gmn_solve(rho, gap_tol=1e-6, max_iter=3000, check_every=10, sigma=ws))
+    warm, wdt = _timed(lambda: mg.gmn_solve(rho, warm_start=guess, gap_tol=1e-6, max_iter=3000, check_every=10,
+                                            sigma=ws))
+    both = (cold_ws["iters"] > 0) & (warm["iters"] > 0)
     sample = list(range(0, len(rho), len(rho) // 16))
     _, cdt = _oracle_pool(lambda i: ogmn.solve(rho[i], gap_tol=1e-6, max_iter=3000), sample, 16)
     return {"config": "4: 65536 rho3 (half L=16 trajectories, half GHZ/W/product mixtures), GMN to gap 1e-6",
@@ -456,8 +461,10 @@ def config4():
             "certified_fraction_trajectory_states": float(ok[:len(traj)].mean()),
             "certified_fraction_mixtures": float(ok[len(traj):].mean()),
             "mean_iterations_certified": float(cold["iters"][ok].mean()),
-            "warm_start": {"value": len(rho) / wdt, "certified_fraction": float((warm["iters"] > 0).mean()),
-                           "iterations_on_states_both_certify": [float(cold["iters"][both].mean()),
+            "warm_start": {"sigma": ws, "value": len(rho) / wdt, "cold_value_same_sigma": len(rho) / cwdt,
+                           "certified_fraction": float((warm["iters"] > 0).mean()),
+                           "cold_certified_fraction_same_sigma": float((cold_ws["iters"] > 0).mean()),
+                           "iterations_on_states_both_certify": [float(cold_ws["iters"][both].mean()),
                                                                  float(warm["iters"][both].mean())],
                            "train_pairs": int(len(x)), "train_seconds": tdt},
             "cpu_baseline": {"value": len(sample) / cdt, "unit": "SDPs/s", "cores": 16, "kind": "port",

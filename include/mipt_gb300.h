@@ -307,7 +307,7 @@ typedef struct mipt_gb300_gmn_config
     int check_every; /* iterations between FP64 certificates */
     double gap_tol;  /* duality gap, e.g. 1e-6 */
     double feas_tol; /* eigenvalue violation of the box constraints */
-    double sigma;    /* ADMM penalty (0: 1.0) */
+    double sigma;    /* ADMM penalty (0: 0.1) */
     int fp64;        /* 1: FP64 iterations */
 } mipt_gb300_gmn_config;
 
@@ -319,6 +319,10 @@ typedef struct mipt_gb300_gmn_config
  * solution[count][7][128] (W, Q_1..3, Z_1..3, same layout). */
 int mipt_gb300_gmn_solve(const mipt_gb300_gmn_config *config, const double *rho, int count,
                          const float *warm_start, double *gmn, double *gap, int *iterations, double *solution);
+/* As mipt_gb300_gmn_solve with a per-state ADMM penalty sigma[count] (> 0). */
+int mipt_gb300_gmn_solve_sigma(const mipt_gb300_gmn_config *config, const double *rho, int count,
+                               const double *sigma, const float *warm_start, double *gmn, double *gap,
+                               int *iterations, double *solution);
 
 /* Negativity of the three single-qubit cuts of each 8x8 state (the
  * bipartite-negativity prefilter of the reference's gmn.exe,

@@ -87,6 +87,7 @@ def lib():
     L.mipt_gb300_batch_fetch_rho3_points.argtypes = [vp, vp]
     L.mipt_gb300_lattice_bonds.argtypes = [ci, ci, ci, vp, vp]
     L.mipt_gb300_gmn_solve.argtypes = [vp, vp, ci, vp, vp, vp, vp, vp]
+    L.mipt_gb300_gmn_solve_sigma.argtypes = [vp, vp, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_cut_negativities.argtypes = [vp, ci, vp]
     L.mipt_gb300_autotune_tile.argtypes = [ci, ci, ci, ci, ci, ci, vp, vp, vp, vp]
     L.mipt_gb300_draw_haar_lattice.argtypes = [u64, ci, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
@@ -374,13 +375,15 @@ def ri_to_rho(ri):
     return (ri[..., 0::2] + 1j * ri[..., 1::2]).reshape(ri.shape[:-1] + (8, 8))
 
 
-def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6, feas_tol=1e-6, sigma=1.0,
+def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6, feas_tol=1e-6, sigma=0.0,
               fp64=False, want_solution=False):
     """GMN of three-qubit states rho[N, 8, 8] by the batched GPU ADMM.
-    warm_start: [N, 7, 8, 8] (W, Q_1..3, Z_1..3) or None."""
+    warm_start: [N, 7, 8, 8] (W, Q_1..3, Z_1..3) or None. sigma: the ADMM
+    penalty, a scalar (0: the library default, 0.1) or one per state."""
     r = rho_to_ri(np.asarray(rho).reshape(-1, 8, 8))
     n = len(r)
-    cfg = GmnConfig(max_iter, check_every, gap_tol, feas_tol, sigma, int(fp64))
+    per_state = np.ndim(sigma) > 0
+    cfg = GmnConfig(max_iter, check_every, gap_tol, feas_tol, 0.0 if per_state else float(sigma), int(fp64))
     ws = None
     if warm_start is not None:
         ws = np.ascontiguousarray(rho_to_ri(np.asarray(warm_start).reshape(n, 7, 8, 8)), np.float32)
@@ -388,7 +391,12 @@ def gmn_solve(rho, warm_start=None, max_iter=20000, check_every=10, gap_tol=1e-6
     gap = np.zeros(n)
     it = np.zeros(n, np.int32)
     sol = np.zeros((n, 7, 128)) if want_solution else None
-    _check(lib().mipt_gb300_gmn_solve(ctypes.byref(cfg), _p(r), n, _p(ws), _p(g), _p(gap), _p(it), _p(sol)))
+    if per_state:
+        sg = np.ascontiguousarray(np.broadcast_to(np.asarray(sigma, np.float64), (n,)))
+        _check(lib().mipt_gb300_gmn_solve_sigma(ctypes.byref(cfg), _p(r), n, _p(sg), _p(ws), _p(g), _p(gap), _p(it),
+                                                _p(sol)))
+    else:
+        _check(lib().mipt_gb300_gmn_solve(ctypes.byref(cfg), _p(r), n, _p(ws), _p(g), _p(gap), _p(it), _p(sol)))
     out = dict(gmn=g, gap=gap, iters=it)
     if want_solution:
         out["solution"] = ri_to_rho(sol)

@@ -211,7 +211,7 @@ int main(int argc, char **argv)
         const char *gv = std::getenv("MIPT_GB300_GMN_GAP");
         cfg.gap_tol = (gv && *gv) ? std::stod(gv) : 1e-7;
         cfg.feas_tol = cfg.gap_tol;
-        cfg.sigma = 1.0;
+        cfg.sigma = 0.0; // the library's default penalty
         cfg.fp64 = use_fp64() ? 1 : 0;
 
         std::ofstream out(output);

@@ -80,7 +80,7 @@ def infeasibility(W, Q):
     return e
 
 
-def solve(rho, sigma=1.0, gap_tol=1e-9, max_iter=200000, check_every=10, state=None):
+def solve(rho, sigma=0.1, gap_tol=1e-9, max_iter=200000, check_every=10, state=None):
     """FP64 ADMM. Returns dict(gmn, primal, dual, gap, infeas, iters, W, Q, Z)."""
     rho = np.asarray(rho, np.complex128)
     rho = 0.5 * (rho + rho.conj().T)
