@@ -236,6 +236,31 @@ void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
  * (nullable, [count][2*periods] bit masks) replays recorded outcomes. */
 int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *batch, const uint64_t *seeds, const double *p, int count,
                                   const uint64_t *forced_outcomes);
+/* Free-energy protocol (cpp/apps/free_energy.cpp:460-533): the same Haar
+ * brickwork, `2 * periods` layers drawn from the probed circuit workspace's
+ * streams (cpp/include/mipt/probed.hpp:103-108,196-206) -- layer stream
+ * mt19937(seed), measurement stream mt19937(seed ^ 0x9e3779b9) -- for the
+ * 32-bit workspace seed of each trajectory. */
+int mipt_gb300_batch_prepare_haar_workspace(mipt_gb300_batch *batch, const uint32_t *workspace_seeds,
+                                            const double *p, int count);
+/* Initial states for the next execute instead of |0...0>: trajectory i from
+ * the reference's random initial-state draw (cpp/include/mipt/free_energy.hpp:
+ * 125-222; kind 0 random product, 1 random Haar; fixed_parity for the
+ * parity-preserving circuits) with an mt19937_64 seeded by seeds[i], drawn on
+ * host threads; parity_sectors[i] (nullable) gets the sector or -1. Or one
+ * trajectory from host amplitudes (host_ri[2^n][2]). Consumed by the next
+ * mipt_gb300_batch_execute; other trajectories start from |0...0>. */
+int mipt_gb300_batch_set_initial_states(mipt_gb300_batch *batch, const uint64_t *seeds, int kind, int fixed_parity,
+                                        int count, int *parity_sectors);
+int mipt_gb300_batch_set_initial_state(mipt_gb300_batch *batch, int index, const double *host_ri);
+/* The same initial-state draw on the host: host_ri[2^n][2], amplitudes
+ * rounded as an FP32 (fp64 = 0) or FP64 state stores them. */
+int mipt_gb300_draw_initial_state(uint64_t seed, int n_qubits, int kind, int fixed_parity, int fp64,
+                                  double *host_ri, int *parity_sector);
+/* Observation schedule replacing observe_every: observables (and rho3 blocks
+ * per point) after steps[i] layers, steps increasing in 0..layers, 0 = the
+ * initial state; points = count (count = 0 restores observe_every). */
+int mipt_gb300_batch_set_observation_steps(mipt_gb300_batch *batch, const int *steps, int count);
 /* Run every layer of the prepared batch on the device, asynchronously on
  * `stream` (a cudaStream_t; NULL = default stream). */
 int mipt_gb300_batch_execute(mipt_gb300_batch *batch, void *stream);
@@ -396,6 +421,12 @@ uint64_t mipt_gb300_trajectory_seed(uint64_t master, uint64_t index);
 int mipt_gb300_draw_haar(uint64_t seed, int n_qubits, int periods, double p, int closed, int chunk_bits,
                          int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured, double *uniforms,
                          int *n_uniforms);
+
+/* The free-energy workspace draw of one trajectory on the host (closed ring,
+ * `layers` layers; outputs as mipt_gb300_draw_haar). */
+int mipt_gb300_draw_haar_workspace(uint32_t seed, int n_qubits, int layers, double p, int chunk_bits,
+                                   int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured,
+                                   double *uniforms, int *n_uniforms);
 
 #ifdef __cplusplus
 }

@@ -77,6 +77,12 @@ def lib():
     L.mipt_gb300_batch_destroy.argtypes = [vp]
     L.mipt_gb300_batch_destroy.restype = None
     L.mipt_gb300_batch_prepare_haar.argtypes = [vp, vp, vp, ci, vp]
+    L.mipt_gb300_batch_prepare_haar_workspace.argtypes = [vp, vp, vp, ci]
+    L.mipt_gb300_batch_set_initial_states.argtypes = [vp, vp, ci, ci, ci, vp]
+    L.mipt_gb300_batch_set_initial_state.argtypes = [vp, ci, vp]
+    L.mipt_gb300_batch_set_observation_steps.argtypes = [vp, vp, ci]
+    L.mipt_gb300_draw_initial_state.argtypes = [u64, ci, ci, ci, ci, vp, vp]
+    L.mipt_gb300_draw_haar_workspace.argtypes = [ctypes.c_uint32, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_execute.argtypes = [vp, vp]
     L.mipt_gb300_batch_fetch.argtypes = [vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_fetch_tmi.argtypes = [vp, ci, vp]
@@ -130,6 +136,15 @@ def trajectory_seed(master, index):
     return lib().mipt_gb300_trajectory_seed(master, index)
 
 
+def draw_initial_state(seed, n, kind, fixed_parity=False, fp64=True):
+    """The free-energy protocol's random initial state (complex amplitudes, parity sector)."""
+    ri = np.zeros(2 << n)
+    par = ctypes.c_int()
+    _check(lib().mipt_gb300_draw_initial_state(seed, n, int(kind), int(fixed_parity), int(fp64), _p(ri),
+                                               ctypes.byref(par)))
+    return ri.view(np.complex128), par.value
+
+
 def draw_haar(seed, n, periods, p, closed=True, chunk_bits=16):
     """Host draw of one Haar trajectory (no GPU): the reference's random record."""
     L = 2 * periods
@@ -141,6 +156,19 @@ def draw_haar(seed, n, periods, p, closed=True, chunk_bits=16):
     nu = np.zeros(1, np.int32)
     _check(lib().mipt_gb300_draw_haar(seed, n, periods, p, int(closed), chunk_bits, _p(gpl), _p(bq), _p(bu),
                                       _p(meas), _p(uni), _p(nu)))
+    return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu[0]].copy())
+
+
+def draw_haar_workspace(seed32, n, layers, p, chunk_bits=16):
+    """Host draw of one free-energy trajectory's layers (probed-workspace streams)."""
+    gpl = np.zeros(layers, np.int32)
+    bq = np.zeros((layers, n // 2, 2), np.int32)
+    bu = np.zeros((layers, n // 2, 32))
+    meas = np.zeros(layers, np.uint64)
+    uni = np.zeros(layers * n + 1)
+    nu = np.zeros(1, np.int32)
+    _check(lib().mipt_gb300_draw_haar_workspace(seed32, n, layers, p, chunk_bits, _p(gpl), _p(bq), _p(bu),
+                                                _p(meas), _p(uni), _p(nu)))
     return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu[0]].copy())
 
 
@@ -282,6 +310,32 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+    def prepare_workspace(self, workspace_seeds, p):
+        """Free-energy draw: layers from the probed workspace streams of each 32-bit seed."""
+        seeds = np.ascontiguousarray(workspace_seeds, np.uint32)
+        p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, np.float64), seeds.shape))
+        _check(lib().mipt_gb300_batch_prepare_haar_workspace(self._h, _p(seeds), _p(p), len(seeds)))
+        self.count = len(seeds)
+
+    def set_initial_states(self, seeds, kind, fixed_parity=False):
+        """Random initial states (kind 0 product, 1 Haar) for the next execute; returns parity sectors."""
+        seeds = np.ascontiguousarray(seeds, np.uint64)
+        sectors = np.zeros(len(seeds), np.int32)
+        _check(lib().mipt_gb300_batch_set_initial_states(self._h, _p(seeds), int(kind), int(fixed_parity),
+                                                          len(seeds), _p(sectors)))
+        return sectors
+
+    def set_initial_state(self, index, psi):
+        ri = np.ascontiguousarray(np.asarray(psi, np.complex128)).view(np.float64)
+        _check(lib().mipt_gb300_batch_set_initial_state(self._h, int(index), _p(ri)))
+
+    def set_observation_steps(self, steps):
+        """Observe after each listed number of layers (0 = the initial state)."""
+        steps = np.ascontiguousarray(steps, np.int32)
+        _check(lib().mipt_gb300_batch_set_observation_steps(self._h, _p(steps), len(steps)))
+        self.points = len(steps) if len(steps) else ((self.layers // self.observe_every)
+                                                     if self.observe_every > 0 else 1)
 
     def prepare(self, seeds, p, forced=None):
         seeds = np.ascontiguousarray(seeds, np.uint64)

@@ -19,7 +19,7 @@ LIB = os.path.join(OUT, "libmipt_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 APPS = os.path.join(HERE, "apps")
 APP_TARGETS = [("mipt.cpp", "mipt.exe"), ("sim_tmi.cpp", "sim_tmi.exe"), ("gmn.cpp", "gmn.exe"),
-               ("entropy.cpp", "entropy.exe")]
+               ("entropy.cpp", "entropy.exe"), ("free_energy.cpp", "free_energy.exe")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu", "parity.cu", "gmn.cu", "mlp.cu"]

@@ -10,6 +10,9 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <atomic>
+#include <complex>
+#include <thread>
 #include <tuple>
 #include <mutex>
 #include <cmath>
@@ -785,6 +788,13 @@ struct mipt_gb300_batch
     bool has_forced = false;
     int points = 0;
     int reqs_per_point = 0;
+    // Explicit observation schedule (mipt_gb300_batch_set_observation_steps):
+    // obs_point[t] is the point index observed after t layers (t = 0: the
+    // initial state), -1 where none; empty = the observe_every rule.
+    std::vector<int> obs_point;
+    // Trajectories whose initial state was uploaded for the next execute.
+    std::vector<char> custom_init;
+    bool per_point() const { return !obs_point.empty() || cfg.observe_every > 0; }
     std::vector<EntReq> reqs; // for one point, trajectory index filled per launch
     int col_half_vn = -1, col_half_s2 = -1;
     std::vector<int> tmi_vn, tmi_s2; // 7 request slots (A,B,C,D,AB,AC,BC) per cyclic offset
@@ -886,6 +896,45 @@ int mipt_cuda_rho3_subsystems_complex_host_both_f32(const void *s, int n, const 
 const char *mipt_gb300_version(void) { return "mipt_gb300 0.1 (sm_103a)"; }
 std::uint64_t mipt_gb300_splitmix64(std::uint64_t v) { return mg::splitmix64(v); }
 std::uint64_t mipt_gb300_trajectory_seed(std::uint64_t m, std::uint64_t i) { return mg::trajectory_seed(m, i); }
+
+namespace
+{
+int export_draw(const TrajectoryDraw &d, int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured,
+                double *uniforms, int *n_uniforms)
+{
+    for (int t = 0; t < d.layers; ++t)
+    {
+        if (gates_per_layer) gates_per_layer[t] = d.bond_count[t];
+        if (measured) measured[t] = d.measured[t];
+    }
+    if (bond_q) std::copy(d.bond_q.begin(), d.bond_q.end(), bond_q);
+    if (bond_u)
+        for (std::size_t i = 0; i < d.bond_u.size(); ++i)
+        {
+            bond_u[2 * i] = d.bond_u[i].real();
+            bond_u[2 * i + 1] = d.bond_u[i].imag();
+        }
+    if (uniforms) std::copy(d.uniforms.begin(), d.uniforms.end(), uniforms);
+    if (n_uniforms) *n_uniforms = static_cast<int>(d.uniforms.size());
+    return 0;
+}
+} // namespace
+
+int mipt_gb300_draw_haar_workspace(std::uint32_t seed, int n, int layers, double p, int chunk_bits,
+                                   int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured,
+                                   double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        TrajectoryDraw d;
+        draw_haar_trajectory_workspace(seed, n, layers, p, true, chunk_bits, d);
+        return export_draw(d, gates_per_layer, bond_q, bond_u, measured, uniforms, n_uniforms);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+}
 
 int mipt_gb300_draw_haar(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
                          int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured, double *uniforms,
@@ -1210,7 +1259,7 @@ int set_rho3_subs(mipt_gb300_batch *b, const std::vector<int> &subs)
     if ((e = b->rho3.ensure(C * S * 128 * sizeof(double))) != cudaSuccess) return cuda_fail(e, "rho3");
     if ((e = b->r3scratch.ensure(rho3_scratch_bytes(n, b->capacity, S))) != cudaSuccess)
         return cuda_fail(e, "rho3 scratch");
-    if (b->cfg.observe_every > 0)
+    if (b->per_point())
         if ((e = b->rho3_pts.ensure(static_cast<std::size_t>(b->points) * C * S * 128 * sizeof(double))) !=
             cudaSuccess)
             return cuda_fail(e, "rho3 per point");
@@ -1366,31 +1415,24 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     if ((e = b->h_meas.ensure(C * T * sizeof(LayerMeas))) != cudaSuccess) return cuda_fail(e, "pinned meas");
     if ((e = b->h_forced.ensure(C * T * sizeof(std::uint64_t))) != cudaSuccess) return cuda_fail(e, "pinned forced");
     if ((e = b->h_res.ensure(C * T * sizeof(LayerResult))) != cudaSuccess) return cuda_fail(e, "pinned results");
+    b->custom_init.assign(C, 0);
     *out = b.release();
     return 0;
 }
 
 void mipt_gb300_batch_destroy(mipt_gb300_batch *b) { delete b; }
 
-int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seeds, const double *p, int count,
-                                  const std::uint64_t *forced)
+} // extern "C"
+
+namespace
 {
-    if (!b || !seeds || !p || count <= 0 || count > b->capacity)
-        return fail(MIPT_GB300_E_INVALID, "bad batch prepare arguments");
+// Packs drawn trajectories into the batch's pinned layer tables and uploads
+// them (gates in the state's precision, measured-site chunks with their
+// uniforms, optional forced outcomes).
+int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, const std::uint64_t *forced)
+{
+    const int count = static_cast<int>(draws.size());
     const int n = b->cfg.n_qubits, T = b->T, G = b->G, cb = b->cfg.chunk_bits;
-    std::vector<TrajectoryDraw> draws;
-    try
-    {
-        if (b->lattice)
-            draw_haar_lattice_batch(seeds, p, count, b->cfg.lattice_x, b->cfg.lattice_y, T, cb, draws,
-                                    b->cfg.host_threads);
-        else
-            draw_haar_batch(seeds, p, count, n, b->cfg.periods, b->cfg.closed != 0, cb, draws, b->cfg.host_threads);
-    }
-    catch (const std::exception &e)
-    {
-        return fail(MIPT_GB300_E_INVALID, e.what());
-    }
     b->count = count;
     b->measured.assign(static_cast<std::size_t>(count) * T, 0);
     b->any_meas.assign(T, 0);
@@ -1464,6 +1506,179 @@ int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seed
     b->executed = false;
     return 0;
 }
+} // namespace
+
+extern "C" {
+int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seeds, const double *p, int count,
+                                  const std::uint64_t *forced)
+{
+    if (!b || !seeds || !p || count <= 0 || count > b->capacity)
+        return fail(MIPT_GB300_E_INVALID, "bad batch prepare arguments");
+    std::vector<TrajectoryDraw> draws;
+    try
+    {
+        if (b->lattice)
+            draw_haar_lattice_batch(seeds, p, count, b->cfg.lattice_x, b->cfg.lattice_y, b->T, b->cfg.chunk_bits,
+                                    draws, b->cfg.host_threads);
+        else
+            draw_haar_batch(seeds, p, count, b->cfg.n_qubits, b->cfg.periods, b->cfg.closed != 0,
+                            b->cfg.chunk_bits, draws, b->cfg.host_threads);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    return upload_draws(b, draws, forced);
+}
+
+int mipt_gb300_batch_prepare_haar_workspace(mipt_gb300_batch *b, const std::uint32_t *seeds, const double *p,
+                                            int count)
+{
+    if (!b || !seeds || !p || count <= 0 || count > b->capacity)
+        return fail(MIPT_GB300_E_INVALID, "bad batch prepare arguments");
+    if (b->lattice) return fail(MIPT_GB300_E_INVALID, "the workspace draw is the 1-D brickwork");
+    std::vector<TrajectoryDraw> draws;
+    try
+    {
+        draw_haar_workspace_batch(seeds, p, count, b->cfg.n_qubits, b->T, b->cfg.closed != 0, b->cfg.chunk_bits,
+                                  draws, b->cfg.host_threads);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    return upload_draws(b, draws, nullptr);
+}
+
+int mipt_gb300_batch_set_observation_steps(mipt_gb300_batch *b, const int *steps, int count)
+{
+    if (!b || count < 0 || (count > 0 && !steps)) return fail(MIPT_GB300_E_INVALID, "bad observation schedule");
+    std::vector<int> point;
+    if (count > 0)
+    {
+        point.assign(static_cast<std::size_t>(b->T) + 1, -1);
+        for (int i = 0; i < count; ++i)
+        {
+            if (steps[i] < 0 || steps[i] > b->T || (i > 0 && steps[i] <= steps[i - 1]))
+                return fail(MIPT_GB300_E_INVALID, "observation steps must be increasing within 0..layers");
+            point[static_cast<std::size_t>(steps[i])] = i;
+        }
+    }
+    const int points = count > 0 ? count : (b->cfg.observe_every > 0 ? b->T / b->cfg.observe_every : 1);
+    const std::size_t C = static_cast<std::size_t>(b->capacity);
+    cudaError_t e;
+    if (b->reqs_per_point > 0)
+        if ((e = b->ent.ensure(C * points * b->reqs_per_point * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "entropy outputs");
+    if (b->cfg.rho3 && (count > 0 || b->cfg.observe_every > 0))
+        if ((e = b->rho3_pts.ensure(static_cast<std::size_t>(points) * C * b->rho3_count * 128 * sizeof(double))) !=
+            cudaSuccess)
+            return cuda_fail(e, "rho3 per point");
+    b->obs_point = std::move(point);
+    b->points = points;
+    b->executed = false;
+    return 0;
+}
+
+int mipt_gb300_batch_set_initial_state(mipt_gb300_batch *b, int index, const double *host_ri)
+{
+    if (!b || !host_ri || index < 0 || index >= b->capacity)
+        return fail(MIPT_GB300_E_INVALID, "bad initial-state arguments");
+    const std::size_t dim = b->dim;
+    void *dst = static_cast<char *>(b->states.p) + static_cast<std::size_t>(index) * dim * b->elem;
+    if (b->cfg.fp64)
+        MG_CUDA(cudaMemcpy(dst, host_ri, dim * 16, cudaMemcpyHostToDevice));
+    else
+    {
+        std::vector<float> f(2 * dim);
+        for (std::size_t i = 0; i < 2 * dim; ++i) f[i] = static_cast<float>(host_ri[i]);
+        MG_CUDA(cudaMemcpy(dst, f.data(), dim * 8, cudaMemcpyHostToDevice));
+    }
+    b->custom_init[static_cast<std::size_t>(index)] = 1;
+    return 0;
+}
+
+int mipt_gb300_batch_set_initial_states(mipt_gb300_batch *b, const std::uint64_t *seeds, int kind, int fixed_parity,
+                                        int count, int *parity_sectors)
+{
+    if (!b || !seeds || count <= 0 || count > b->capacity || (kind != 0 && kind != 1))
+        return fail(MIPT_GB300_E_INVALID, "bad initial-state arguments");
+    const int n = b->cfg.n_qubits;
+    const std::size_t dim = b->dim, bytes = dim * b->elem;
+    // Host threads draw into their own staging buffers, bounded to 8 GiB.
+    int threads = b->cfg.host_threads > 0 ? b->cfg.host_threads
+                                          : static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    threads = std::max(1, std::min<int>({threads, count, static_cast<int>(std::max<std::size_t>(1, (8ull << 30) / bytes))}));
+    std::vector<std::vector<char>> stage(static_cast<std::size_t>(threads), std::vector<char>(bytes));
+    std::vector<int> sector(static_cast<std::size_t>(count), -1);
+    for (int first = 0; first < count; first += threads)
+    {
+        const int group = std::min(threads, count - first);
+        std::vector<std::thread> pool;
+        std::atomic<bool> failed{false};
+        std::string what;
+        std::mutex what_mu;
+        for (int k = 0; k < group; ++k)
+            pool.emplace_back([&, k]() {
+                try
+                {
+                    const int i = first + k;
+                    sector[i] = b->cfg.fp64
+                                    ? draw_initial_state<double>(seeds[i], n, kind, fixed_parity != 0,
+                                                                 reinterpret_cast<std::complex<double> *>(stage[k].data()))
+                                    : draw_initial_state<float>(seeds[i], n, kind, fixed_parity != 0,
+                                                                reinterpret_cast<std::complex<float> *>(stage[k].data()));
+                }
+                catch (const std::exception &e)
+                {
+                    std::lock_guard<std::mutex> lock(what_mu);
+                    what = e.what();
+                    failed = true;
+                }
+            });
+        for (auto &th : pool) th.join();
+        if (failed) return fail(MIPT_GB300_E_INVALID, what.c_str());
+        for (int k = 0; k < group; ++k)
+        {
+            MG_CUDA(cudaMemcpy(static_cast<char *>(b->states.p) + static_cast<std::size_t>(first + k) * bytes,
+                               stage[k].data(), bytes, cudaMemcpyHostToDevice));
+            b->custom_init[static_cast<std::size_t>(first + k)] = 1;
+        }
+    }
+    if (parity_sectors) std::copy(sector.begin(), sector.end(), parity_sectors);
+    return 0;
+}
+
+int mipt_gb300_draw_initial_state(std::uint64_t seed, int n_qubits, int kind, int fixed_parity, int fp64,
+                                  double *host_ri, int *parity_sector)
+{
+    if (!host_ri || n_qubits < 1 || n_qubits > 30 || (kind != 0 && kind != 1))
+        return fail(MIPT_GB300_E_INVALID, "bad initial-state arguments");
+    try
+    {
+        const std::size_t dim = std::size_t{1} << n_qubits;
+        int sector;
+        if (fp64)
+            sector = draw_initial_state<double>(seed, n_qubits, kind, fixed_parity != 0,
+                                                reinterpret_cast<std::complex<double> *>(host_ri));
+        else
+        {
+            std::vector<std::complex<float>> f(dim);
+            sector = draw_initial_state<float>(seed, n_qubits, kind, fixed_parity != 0, f.data());
+            for (std::size_t i = 0; i < dim; ++i)
+            {
+                host_ri[2 * i] = f[i].real();
+                host_ri[2 * i + 1] = f[i].imag();
+            }
+        }
+        if (parity_sector) *parity_sector = sector;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+    return 0;
+}
 
 } // extern "C"
 
@@ -1484,9 +1699,22 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     b->next_event = 0;
     {
         Mark m(b, K_OTHER, s);
-        MG_CUDA(launch_init_zero<Real>(states, b->dim, count, s));
+        int custom = 0;
+        for (int i = 0; i < count; ++i) custom += b->custom_init[i] ? 1 : 0;
+        if (custom == 0)
+        {
+            MG_CUDA(launch_init_zero<Real>(states, b->dim, count, s));
+            ++L;
+        }
+        else
+            for (int i = 0; i < count; ++i)
+                if (!b->custom_init[i])
+                {
+                    MG_CUDA(launch_init_zero<Real>(states + static_cast<std::size_t>(i) * b->dim, b->dim, 1, s));
+                    ++L;
+                }
+        std::fill(b->custom_init.begin(), b->custom_init.end(), 0);
     }
-    ++L;
     const std::size_t slots = static_cast<std::size_t>(count) * T;
     k_reset_layers<<<std::min<std::size_t>((slots + 255) / 256, 1024), 256, 0, s>>>(col, res, slots);
     ++L;
@@ -1496,6 +1724,42 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
         const std::size_t ne = static_cast<std::size_t>(count) * b->points * b->reqs_per_point;
         k_fill_double<<<std::min<std::size_t>((ne + 255) / 256, 1024), 256, 0, s>>>(b->ent.as<double>(), ne, NAN);
         ++L;
+    }
+    // Observations of point `point` on the current states (`pending`: the
+    // collapse each trajectory still owes, or null).
+    auto observe = [&](int point, const Collapse *pending) -> int {
+        if (b->reqs_per_point > 0)
+        {
+            std::vector<EntReq> reqs;
+            for (int i = 0; i < count; ++i)
+                for (int r = 0; r < b->reqs_per_point; ++r)
+                {
+                    EntReq q = b->reqs[r];
+                    q.traj = i;
+                    q.out = (i * b->points + point) * b->reqs_per_point + r;
+                    reqs.push_back(q);
+                }
+            Mark m(b, K_OBS, s);
+            const int rc = run_entropies<Real>(states, n, reqs, pending, T, b->ws, s, b->ent.as<double>(), L);
+            if (rc) return rc;
+        }
+        if (b->cfg.rho3)
+        {
+            Mark m(b, K_OBS, s);
+            MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count,
+                                     b->cfg.fermion_trace ? 1 : 0, pending, T,
+                                     b->rho3_pts.as<double>() +
+                                         static_cast<std::size_t>(point) * b->capacity * b->rho3_count * 128,
+                                     b->r3scratch.p, b->r3scratch.bytes, s));
+            L += 2;
+        }
+        return 0;
+    };
+    const bool sched = !b->obs_point.empty();
+    if (sched && b->obs_point[0] >= 0)
+    {
+        const int rc = observe(b->obs_point[0], nullptr);
+        if (rc) return rc;
     }
     const std::size_t gstride = static_cast<std::size_t>(T) * G * 16;
     for (int t = 0; t < T; ++t)
@@ -1533,33 +1797,15 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                 ++L;
             }
         }
-        const bool due = b->cfg.observe_every > 0 ? ((t + 1) % b->cfg.observe_every == 0) : (t == T - 1);
-        if (due && b->reqs_per_point > 0 && b->cfg.observe_every > 0)
+        int point = -1;
+        if (sched)
+            point = b->obs_point[t + 1];
+        else if (b->cfg.observe_every > 0 && (t + 1) % b->cfg.observe_every == 0)
+            point = (t + 1) / b->cfg.observe_every - 1;
+        if (point >= 0)
         {
-            const int point = (t + 1) / b->cfg.observe_every - 1;
-            std::vector<EntReq> reqs;
-            for (int i = 0; i < count; ++i)
-                for (int r = 0; r < b->reqs_per_point; ++r)
-                {
-                    EntReq q = b->reqs[r];
-                    q.traj = i;
-                    q.out = (i * b->points + point) * b->reqs_per_point + r;
-                    reqs.push_back(q);
-                }
-            Mark m(b, K_OBS, s);
-            const int rc = run_entropies<Real>(states, n, reqs, col + t, T, b->ws, s, b->ent.as<double>(), L);
+            const int rc = observe(point, col + t);
             if (rc) return rc;
-        }
-        if (due && b->cfg.rho3 && b->cfg.observe_every > 0)
-        {
-            const int point = (t + 1) / b->cfg.observe_every - 1;
-            Mark m(b, K_OBS, s);
-            MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count, b->cfg.fermion_trace ? 1 : 0,
-                                     col + t, T,
-                                     b->rho3_pts.as<double>() +
-                                         static_cast<std::size_t>(point) * b->capacity * b->rho3_count * 128,
-                                     b->r3scratch.p, b->r3scratch.bytes, s));
-            L += 2;
         }
     }
     // Leave every trajectory in its collapsed, normalised final state.
@@ -1568,7 +1814,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
         MG_CUDA(launch_collapse<Real>(states, b->dim, count, col + (T - 1), T, s));
     }
     ++L;
-    if (b->reqs_per_point > 0 && b->cfg.observe_every == 0)
+    if (b->reqs_per_point > 0 && !b->per_point())
     {
         std::vector<EntReq> reqs;
         for (int i = 0; i < count; ++i)
@@ -1585,6 +1831,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     }
     if (b->cfg.rho3)
     {
+        // The final-state blocks are written in every mode.
         Mark m(b, K_OBS, s);
         MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count, b->cfg.fermion_trace ? 1 : 0,
                                  nullptr, 0, b->rho3.as<double>(), b->r3scratch.p, b->r3scratch.bytes, s));
@@ -1728,8 +1975,8 @@ int mipt_gb300_batch_rho3_subsystem_count(mipt_gb300_batch *b) { return b ? b->r
 int mipt_gb300_batch_fetch_rho3_points(mipt_gb300_batch *b, double *out)
 {
     if (!b || !b->executed || !out) return fail(MIPT_GB300_E_INVALID, "batch not executed or null output");
-    if (!b->cfg.rho3 || b->cfg.observe_every <= 0)
-        return fail(MIPT_GB300_E_INVALID, "rho3 per point needs rho3 and observe_every > 0");
+    if (!b->cfg.rho3 || !b->per_point())
+        return fail(MIPT_GB300_E_INVALID, "rho3 per point needs rho3 and observe_every > 0 or an observation schedule");
     MG_CUDA(cudaDeviceSynchronize());
     const std::size_t P = b->points, S = b->rho3_count, C = b->capacity, per = S * 128;
     for (std::size_t pt = 0; pt < P; ++pt)

@@ -79,18 +79,48 @@ bool csd_is_singular(const C *u)
     return std::sqrt(hi) < tiny || std::sqrt(lo) < tiny || std::sqrt(std::max(0.0, 1.0 - hi)) < tiny ||
            std::sqrt(std::max(0.0, 1.0 - lo)) < tiny;
 }
-} // namespace
 
-void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool closed, int chunk_bits,
-                          TrajectoryDraw &out)
+// Run `fn(i)` for i in [0, count) on up to `threads` host threads.
+template <typename Fn> void parallel_for(int count, int threads, Fn fn, const char *what)
+{
+    if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+    threads = std::min(threads, std::max(1, count));
+    std::atomic<int> next{0};
+    std::atomic<bool> failed{false};
+    auto work = [&]() {
+        for (;;)
+        {
+            const int i = next.fetch_add(1);
+            if (i >= count) return;
+            try
+            {
+                fn(i);
+            }
+            catch (...)
+            {
+                failed = true;
+            }
+        }
+    };
+    if (threads == 1)
+        work();
+    else
+    {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; ++t) pool.emplace_back(work);
+        for (auto &th : pool) th.join();
+    }
+    if (failed) throw std::runtime_error(what);
+}
+
+// The 1-D brickwork layer loop shared by both seedings: layer t's unitaries
+// (bonds from t % 2), its Bernoulli(p) flags from the layer stream, then one
+// measurement uniform per chunk from the measurement stream.
+void draw_haar_layers(std::mt19937 &gates_rng, std::mt19937 &meas_rng, int n, int T, double p, bool closed,
+                      int chunk_bits, TrajectoryDraw &out)
 {
     if (n < 2 || n % 2 != 0 || n > 62) throw std::invalid_argument("Haar brickwork needs even 2 <= n <= 62");
     if (chunk_bits < 1) throw std::invalid_argument("chunk_bits must be positive");
-    std::mt19937 gates_rng, meas_rng;
-    seed_mt(gates_rng, seed);
-    seed_mt(meas_rng, splitmix64(seed ^ 0xa0761d0dull));
-
-    const int T = 2 * periods;
     const int mb = n / 2;
     out.n = n;
     out.layers = T;
@@ -140,6 +170,109 @@ void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool
     }
     out.uniform_offset[T] = static_cast<int>(out.uniforms.size());
 }
+} // namespace
+
+void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool closed, int chunk_bits,
+                          TrajectoryDraw &out)
+{
+    std::mt19937 gates_rng, meas_rng;
+    seed_mt(gates_rng, seed);
+    seed_mt(meas_rng, splitmix64(seed ^ 0xa0761d0dull));
+    draw_haar_layers(gates_rng, meas_rng, n, 2 * periods, p, closed, chunk_bits, out);
+}
+
+void draw_haar_trajectory_workspace(std::uint32_t seed, int n, int layers, double p, bool closed, int chunk_bits,
+                                    TrajectoryDraw &out)
+{
+    std::mt19937 gates_rng(seed), meas_rng(seed ^ 0x9e3779b9u);
+    draw_haar_layers(gates_rng, meas_rng, n, layers, p, closed, chunk_bits, out);
+}
+
+void draw_haar_workspace_batch(const std::uint32_t *seeds, const double *p, int count, int n, int layers,
+                               bool closed, int chunk_bits, std::vector<TrajectoryDraw> &out, int threads)
+{
+    out.resize(count);
+    parallel_for(
+        count, threads,
+        [&](int i) { draw_haar_trajectory_workspace(seeds[i], n, layers, p[i], closed, chunk_bits, out[i]); },
+        "workspace trajectory draw failed");
+}
+
+template <typename Real>
+int draw_initial_state(std::uint64_t seed, int n, int kind, bool fixed_parity, std::complex<Real> *out)
+{
+    if (n < 1 || n > 40) throw std::invalid_argument("initial state needs 1 <= n <= 40");
+    if (kind != 0 && kind != 1) throw std::invalid_argument("initial state kind must be 0 or 1");
+    const std::size_t dim = std::size_t{1} << n;
+    std::fill(out, out + dim, std::complex<Real>(0, 0));
+    std::mt19937_64 rng(seed);
+    if (kind == 0 && fixed_parity)
+    {
+        // A basis product state: n-1 fair bits, the last one fixing the parity.
+        std::bernoulli_distribution bit(0.5);
+        const int sector = bit(rng) ? 1 : 0;
+        std::uint64_t basis = 0;
+        int parity = 0;
+        for (int q = 0; q + 1 < n; ++q)
+        {
+            const int v = bit(rng) ? 1 : 0;
+            parity ^= v;
+            basis |= static_cast<std::uint64_t>(v) << q;
+        }
+        basis |= static_cast<std::uint64_t>(parity ^ sector) << (n - 1);
+        out[basis] = std::complex<Real>(1, 0);
+        return sector;
+    }
+    if (kind == 0)
+    {
+        // Site q's Bloch vector uniform on the sphere (z = cos theta uniform,
+        // phi uniform); the amplitude table doubles per site, each product
+        // rounded to Real as it is stored.
+        std::uniform_real_distribution<double> unit(0.0, 1.0);
+        constexpr double two_pi = 6.283185307179586476925286766559;
+        out[0] = std::complex<Real>(1, 0);
+        std::size_t active = 1;
+        for (int q = 0; q < n; ++q)
+        {
+            const double z = 1.0 - 2.0 * unit(rng);
+            const double theta = std::acos(std::clamp(z, -1.0, 1.0));
+            const double phi = two_pi * unit(rng);
+            const std::complex<double> up(std::cos(0.5 * theta), 0.0);
+            const std::complex<double> down = std::polar(std::sin(0.5 * theta), phi);
+            for (std::size_t i = 0; i < active; ++i)
+            {
+                const std::complex<double> prior(out[i]);
+                out[i] = static_cast<std::complex<Real>>(prior * up);
+                out[i | active] = static_cast<std::complex<Real>>(prior * down);
+            }
+            active <<= 1;
+        }
+        return -1;
+    }
+    // Gaussian amplitudes: two normal draws per kept index (real part first,
+    // as the reference's g++ build evaluates its constructor arguments
+    // right to left -- the imaginary draw is taken first), norm accumulated in
+    // long double, one rounded scale applied in Real.
+    std::normal_distribution<double> normal(0.0, 1.0);
+    std::bernoulli_distribution coin(0.5);
+    const int sector = fixed_parity ? (coin(rng) ? 1 : 0) : -1;
+    long double norm2 = 0.0L;
+    for (std::size_t i = 0; i < dim; ++i)
+    {
+        if (fixed_parity && (__builtin_popcountll(static_cast<unsigned long long>(i)) & 1) != sector) continue;
+        const double im = normal(rng);
+        const double re = normal(rng);
+        const std::complex<double> v(re, im);
+        out[i] = static_cast<std::complex<Real>>(v);
+        norm2 += static_cast<long double>(std::norm(v));
+    }
+    if (!(norm2 > 0.0L)) throw std::runtime_error("random Haar state normalisation vanished");
+    const Real scale = static_cast<Real>(1.0 / std::sqrt(static_cast<double>(norm2)));
+    for (std::size_t i = 0; i < dim; ++i) out[i] *= scale;
+    return sector;
+}
+template int draw_initial_state<float>(std::uint64_t, int, int, bool, std::complex<float> *);
+template int draw_initial_state<double>(std::uint64_t, int, int, bool, std::complex<double> *);
 
 std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour)
 {

@@ -49,6 +49,27 @@ void draw_haar_trajectory(std::uint64_t seed, int n, int periods, double p, bool
 void draw_haar_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, bool closed,
                      int chunk_bits, std::vector<TrajectoryDraw> &out, int threads);
 
+// The same brickwork draw (`layers` layers, layer t starting at bond t % 2)
+// from the streams of the probed circuit workspace that free_energy.exe uses:
+// the layer stream is an mt19937 seeded with the 32-bit `seed` itself, the
+// measurement stream one seeded with seed ^ 0x9e3779b9
+// (cpp/include/mipt/probed.hpp:103-108,196-206).
+void draw_haar_trajectory_workspace(std::uint32_t seed, int n, int layers, double p, bool closed, int chunk_bits,
+                                    TrajectoryDraw &out);
+void draw_haar_workspace_batch(const std::uint32_t *seeds, const double *p, int count, int n, int layers,
+                               bool closed, int chunk_bits, std::vector<TrajectoryDraw> &out, int threads);
+
+// Random initial states of the free-energy protocol
+// (cpp/include/mipt/free_energy.hpp:125-222), drawn from an mt19937_64 seeded
+// with `seed`, amplitudes rounded to Real exactly where the reference stores
+// them. kind 0: product of Haar-random single-site states (with
+// `fixed_parity`: a uniformly random basis state of a random global parity);
+// kind 1: normalised complex Gaussian amplitudes (with `fixed_parity`: only
+// those of a random parity sector). Writes 2^n amplitudes; returns the parity
+// sector (0/1) or -1.
+template <typename Real>
+int draw_initial_state(std::uint64_t seed, int n, int kind, bool fixed_parity, std::complex<Real> *out);
+
 } // namespace mg
 
 namespace mg

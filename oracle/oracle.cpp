@@ -29,6 +29,13 @@
 //                                                cpp/include/mipt/tmi/linalg.hpp:125-141,201-208
 //   * TMI over four contiguous cyclic quarters   cpp/include/mipt/tmi/compute.hpp:186-227
 //   * three-site RDMs on the periodic ring       cpp/include/mipt/rdm.hpp:92-106,149-305
+//   * free-energy protocol                       cpp/apps/free_energy.cpp:454-533
+//     per-trajectory streams: trajectory_seed = splitmix64(master ^ index);
+//     workspace seed = low 32 bits of splitmix64(trajectory_seed ^ "CIRCUITU");
+//     initial-state stream mt19937_64(splitmix64(trajectory_seed ^ "INITIALS"))
+//     workspace layer/measurement streams       cpp/include/mipt/probed.hpp:103-108
+//     random product / Haar initial states       cpp/include/mipt/free_energy.hpp:125-222
+//     half-chain S1 schedule                     cpp/include/mipt/free_energy_resume.hpp:150-166
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -1155,6 +1162,212 @@ double orc_ff_block_entropy(const double *gamma, int N, const int *modes, int m)
 {
     ff::Mat G(gamma, gamma + 4 * N * N);
     return ff::block_entropy(G, N, std::vector<int>(modes, modes + m));
+}
+
+// Free-energy initial state: kind 0 random product, 1 random Haar; with
+// fixed_parity a random global-parity sector. fp32 rounds every stored
+// amplitude to float exactly where an FP32 state stores it. Returns 0; the
+// sector (or -1) in *parity.
+int orc_fe_initial_state(std::uint64_t seed, int n, int kind, int fixed_parity, int fp32, double *out_ri,
+                         int *parity)
+{
+    try
+    {
+        const std::uint64_t dim = 1ull << n;
+        std::mt19937_64 rng(seed);
+        auto store = [fp32](cd v) { return fp32 ? cd(static_cast<float>(v.real()), static_cast<float>(v.imag())) : v; };
+        std::vector<cd> a(dim, cd(0.0, 0.0));
+        int sector = -1;
+        if (kind == 0 && fixed_parity)
+        {
+            std::bernoulli_distribution coin(0.5);
+            sector = coin(rng) ? 1 : 0;
+            std::uint64_t x = 0;
+            int par = 0;
+            for (int q = 0; q < n - 1; ++q)
+                if (coin(rng))
+                {
+                    x |= 1ull << q;
+                    par ^= 1;
+                }
+            if (par != sector) x |= 1ull << (n - 1);
+            a[x] = 1.0;
+        }
+        else if (kind == 0)
+        {
+            std::uniform_real_distribution<double> u01(0.0, 1.0);
+            a[0] = 1.0;
+            for (int q = 0; q < n; ++q)
+            {
+                const double cos_theta = std::clamp(1.0 - 2.0 * u01(rng), -1.0, 1.0);
+                const double half = 0.5 * std::acos(cos_theta);
+                const double phi = 2.0 * 3.14159265358979323846 * u01(rng);
+                const cd c0(std::cos(half), 0.0);
+                const cd c1 = std::polar(std::sin(half), phi);
+                const std::uint64_t m = 1ull << q;
+                for (std::uint64_t x = 0; x < m; ++x)
+                {
+                    const cd v = a[x];
+                    a[x] = store(v * c0);
+                    a[x + m] = store(v * c1);
+                }
+            }
+        }
+        else
+        {
+            std::normal_distribution<double> gauss(0.0, 1.0);
+            if (fixed_parity)
+            {
+                std::bernoulli_distribution coin(0.5);
+                sector = coin(rng) ? 1 : 0;
+            }
+            long double nn = 0.0L;
+            for (std::uint64_t x = 0; x < dim; ++x)
+            {
+                if (fixed_parity && (__builtin_popcountll(x) & 1) != sector) continue;
+                // cd(normal, normal) in the reference: imaginary argument drawn first.
+                const double im = gauss(rng);
+                const double re = gauss(rng);
+                a[x] = store(cd(re, im));
+                nn += static_cast<long double>(re * re + im * im);
+            }
+            const double inv = 1.0 / std::sqrt(static_cast<double>(nn));
+            const double scale = fp32 ? static_cast<double>(static_cast<float>(inv)) : inv;
+            for (auto &v : a) v = store(v * scale);
+        }
+        for (std::uint64_t x = 0; x < dim; ++x)
+        {
+            out_ri[2 * x] = a[x].real();
+            out_ri[2 * x + 1] = a[x].imag();
+        }
+        if (parity) *parity = sector;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Workspace-seeded Haar draw (32-bit seed): gates and measured sites of
+// `layers` layers, plus the measurement uniforms (one per chunk). Layout as
+// orc_haar_draw.
+int orc_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits, int *gates_per_layer, int *gate_q,
+                double *gate_m, int *sites_per_layer, int *sites, double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        std::mt19937 gates(seed), meas(seed ^ 0x9e3779b9u);
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        const int mg = n / 2;
+        int u = 0;
+        for (int t = 0; t < layers; ++t)
+        {
+            Layer L;
+            draw_layer(L, n, t & 1, p, true, gates);
+            gates_per_layer[t] = static_cast<int>(L.q.size() / 2);
+            for (std::size_t g = 0; g < L.q.size() / 2; ++g)
+            {
+                gate_q[(static_cast<std::size_t>(t) * mg + g) * 2] = L.q[2 * g];
+                gate_q[(static_cast<std::size_t>(t) * mg + g) * 2 + 1] = L.q[2 * g + 1];
+                for (int e = 0; e < 16; ++e)
+                {
+                    gate_m[(static_cast<std::size_t>(t) * mg + g) * 32 + 2 * e] = L.m[16 * g + e].real();
+                    gate_m[(static_cast<std::size_t>(t) * mg + g) * 32 + 2 * e + 1] = L.m[16 * g + e].imag();
+                }
+            }
+            sites_per_layer[t] = static_cast<int>(L.sites.size());
+            for (std::size_t k = 0; k < L.sites.size(); ++k) sites[static_cast<std::size_t>(t) * n + k] = L.sites[k];
+            for (std::size_t k = 0; k < L.sites.size(); k += chunk_bits) uniforms[u++] = unif(meas);
+        }
+        *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// One free-energy trajectory of the Haar brickwork on the closed ring:
+// 28n timesteps (4n equilibration + 24n production), each one layer and its
+// joint measurement. surprisal[T], measured[T] (site counts), s_half[T+1]
+// (half-chain S1 in bits on the sampled timesteps, NaN elsewhere).
+int orc_fe_trajectory(std::uint64_t trajectory_seed, int n, double p, int init_kind, int fp32_init,
+                      int chunk_bits, int entropy_max_t, int entropy_stride, double *surprisal, int *measured,
+                      double *s_half, int *parity)
+{
+    try
+    {
+        const int T = 28 * n;
+        const std::uint32_t ws = static_cast<std::uint32_t>(mix64(trajectory_seed ^ 0x4349524355495455ull));
+        const std::uint64_t init_seed = mix64(trajectory_seed ^ 0x494e495449414c53ull);
+        const std::uint64_t dim = 1ull << n;
+        std::vector<double> ri(2 * dim);
+        if (orc_fe_initial_state(init_seed, n, init_kind, 0, fp32_init, ri.data(), parity)) return 1;
+        std::vector<cd> psi(dim);
+        for (std::uint64_t x = 0; x < dim; ++x) psi[x] = cd(ri[2 * x], ri[2 * x + 1]);
+        std::mt19937 gates(ws), meas(ws ^ 0x9e3779b9u);
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        auto sampled = [&](int t) {
+            if (entropy_max_t < 0) return false;
+            if (t == 0) return true;
+            if (t > entropy_max_t) return false;
+            return t % entropy_stride == 0 || t == entropy_max_t;
+        };
+        // The workspace draws every layer before the first one runs; the
+        // layer stream is separate from the measurement stream, so drawing
+        // layer by layer consumes both in the same order.
+        std::vector<Layer> layers(T);
+        for (int t = 0; t < T; ++t) draw_layer(layers[t], n, t & 1, p, true, gates);
+        for (int t = 0; t <= T; ++t) s_half[t] = std::nan("");
+        if (sampled(0)) s_half[0] = subsystem_entropy(psi.data(), n, half_chain(n), 1);
+        for (int t = 0; t < T; ++t)
+        {
+            const Layer &L = layers[t];
+            for (std::size_t g = 0; g < L.q.size() / 2; ++g)
+                apply_bond(psi.data(), n, L.q[2 * g], L.q[2 * g + 1], &L.m[16 * g]);
+            std::vector<double> us;
+            for (std::size_t k = 0; k < L.sites.size(); k += chunk_bits) us.push_back(unif(meas));
+            std::vector<int> oc(L.sites.size(), 0);
+            int used = 0;
+            surprisal[t] = measure_layer(psi.data(), n, L.sites, chunk_bits, us.data(), used, nullptr, oc.data());
+            measured[t] = static_cast<int>(L.sites.size());
+            if (sampled(t + 1)) s_half[t + 1] = subsystem_entropy(psi.data(), n, half_chain(n), 1);
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// Free-energy trajectories master/first..first+count-1 on host threads:
+// F_total (sum of all layer surprisals) per trajectory, no entropies. The
+// timed CPU baseline of the free-energy workload.
+int orc_fe_batch(std::uint64_t master, int first, int count, int n, double p, int init_kind, int chunk_bits,
+                 double *f_total, int threads)
+{
+    int failed = 0;
+#ifdef _OPENMP
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : failed)
+#endif
+    for (int i = 0; i < count; ++i)
+    {
+        const std::uint64_t ts = mix64(master ^ static_cast<std::uint64_t>(first + i));
+        const int T = 28 * n;
+        std::vector<double> sp(T), sh(T + 1);
+        std::vector<int> mc(T);
+        int parity = -1;
+        if (orc_fe_trajectory(ts, n, p, init_kind, 0, chunk_bits, -1, 1, sp.data(), mc.data(), sh.data(), &parity))
+            failed |= 1;
+        double tot = 0.0;
+        for (double v : sp) tot += v;
+        f_total[i] = tot;
+    }
+    return failed;
 }
 
 int orc_max_threads()

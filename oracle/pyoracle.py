@@ -46,6 +46,10 @@ def lib():
     L.orc_run_haar_trajectory.argtypes = [u64, ci, ci, cd, ci, ci, ci, ci, vp, vp, vp, vp, vp]
     L.orc_run_batch.argtypes = [u64, ci, ci, ci, ci, cd, ci, ci, ci, vp, vp, ci]
     L.orc_max_threads.restype = ci
+    L.orc_fe_initial_state.argtypes = [u64, ci, ci, ci, ci, vp, vp]
+    L.orc_fe_draw.argtypes = [ctypes.c_uint32, ci, ci, cd, ci] + [vp] * 7
+    L.orc_fe_trajectory.argtypes = [u64, ci, cd, ci, ci, ci, ci, ci, vp, vp, vp, vp]
+    L.orc_fe_batch.argtypes = [u64, ci, ci, ci, cd, ci, ci, vp, ci]
     _lib = L
     return L
 
@@ -278,3 +282,69 @@ def run_lattice_trajectory(seed, X, Y, layers, p, chunk_bits=16, forced=None, ob
                                     observe_every, _p(states) if points else None, _p(psi)):
         raise RuntimeError("orc_run_lattice_trajectory failed")
     return dict(outcomes=outcomes, surprisal=surprisal, states=states[:points], psi=psi)
+
+
+# ------------------------------------------------------------ free energy
+FE_CIRCUIT_SALT = 0x4349524355495455
+FE_INITIAL_SALT = 0x494E495449414C53
+
+
+def fe_trajectory_seed(master, index):
+    """trajectory_seed = splitmix64(master ^ index) (the free-energy stream)."""
+    return lib().orc_splitmix64((master ^ index) & 0xFFFFFFFFFFFFFFFF)
+
+
+def fe_workspace_seed(trajectory_seed):
+    return lib().orc_splitmix64(trajectory_seed ^ FE_CIRCUIT_SALT) & 0xFFFFFFFF
+
+
+def fe_initial_seed(trajectory_seed):
+    return lib().orc_splitmix64(trajectory_seed ^ FE_INITIAL_SALT)
+
+
+def fe_initial_state(seed, n, kind, fixed_parity=False, fp32=False):
+    ri = np.zeros(2 << n)
+    par = np.zeros(1, np.int32)
+    if lib().orc_fe_initial_state(seed, n, kind, int(fixed_parity), int(fp32), _p(ri), _p(par)):
+        raise RuntimeError("orc_fe_initial_state failed")
+    return ri.view(np.complex128), int(par[0])
+
+
+def fe_draw(seed32, n, layers, p, chunk_bits=16):
+    mg = n // 2
+    gpl = np.zeros(layers, np.int32)
+    gq = np.zeros((layers, mg, 2), np.int32)
+    gm = np.zeros((layers, mg, 32))
+    spl = np.zeros(layers, np.int32)
+    sites = np.full((layers, n), -1, np.int32)
+    uni = np.zeros(layers * n + 1)
+    nu = np.zeros(1, np.int32)
+    if lib().orc_fe_draw(seed32, n, layers, p, chunk_bits, *[_p(a) for a in (gpl, gq, gm, spl, sites, uni, nu)]):
+        raise RuntimeError("orc_fe_draw failed")
+    return dict(gates_per_layer=gpl, gate_q=gq, gate_m=gm, sites_per_layer=spl, sites=sites,
+                uniforms=uni[: nu[0]].copy())
+
+
+def fe_trajectory(trajectory_seed, n, p, init_kind, fp32_init=False, chunk_bits=16, entropy_max_t=None,
+                  entropy_stride=1):
+    """One free-energy trajectory (28n timesteps): surprisal[T], measured counts[T],
+    half-chain S1 bits [T+1] (NaN where not sampled), parity sector."""
+    T = 28 * n
+    if entropy_max_t is None:
+        entropy_max_t = 2 * n
+    sp = np.zeros(T)
+    mc = np.zeros(T, np.int32)
+    sh = np.zeros(T + 1)
+    par = np.zeros(1, np.int32)
+    if lib().orc_fe_trajectory(trajectory_seed, n, p, init_kind, int(fp32_init), chunk_bits, entropy_max_t,
+                               entropy_stride, _p(sp), _p(mc), _p(sh), _p(par)):
+        raise RuntimeError("orc_fe_trajectory failed")
+    return dict(surprisal=sp, measured=mc, s_half=sh, parity=int(par[0]))
+
+
+def fe_batch(master, first, count, n, p, init_kind, chunk_bits=16, threads=0):
+    """F_total of trajectories first..first+count-1 on host threads (CPU baseline)."""
+    out = np.zeros(count)
+    if lib().orc_fe_batch(master, first, count, n, p, init_kind, chunk_bits, _p(out), threads):
+        raise RuntimeError("orc_fe_batch failed")
+    return out

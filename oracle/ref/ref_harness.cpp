@@ -18,7 +18,12 @@
 //   reduced_density_manual_from_state           cpp/include/mipt/tmi/linalg.hpp:1098-1142
 //   entropy_hermitian_inplace (Jacobi path)     cpp/include/mipt/tmi/linalg.hpp:524-583
 //   reduced_density_complex_from_host_statevector cpp/include/mipt/rdm.hpp:149-305
+//   random_product_amplitudes / random_haar_amplitudes
+//                                               cpp/include/mipt/free_energy.hpp:125-222
+//   CircuitWorkspace1D::seed (restated below: the class itself needs a live
+//   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
 #include "mipt/circuits/haar.hpp"
+#include "mipt/free_energy.hpp"
 #include "mipt/cusv/gates.hpp"
 #include "mipt/free_energy_measure.hpp"
 #include "mipt/rdm.hpp"
@@ -202,6 +207,76 @@ int ref_rho3_from_state(const double *psi_ri, int n, const int *subs, int count,
         std::vector<mipt::Subsystem> s(static_cast<std::size_t>(count));
         for (int i = 0; i < count; ++i) s[i] = {subs[3 * i], subs[3 * i + 1], subs[3 * i + 2]};
         mipt::reduced_density_complex_from_host_statevector(psi.data(), n, s, out, fermion != 0);
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// The free-energy protocol's initial state, from the reference's own
+// functions (FP64 amplitudes; this build has no MIPT_CUDAQ_PRECISION=32).
+int ref_fe_initial_state(std::uint64_t seed, int n, int kind, int fixed_parity, double *out_ri, int *parity)
+{
+    try
+    {
+        std::mt19937_64 rng(seed);
+        int sector = -1;
+        const auto amps = kind == 0
+                              ? mipt::free_energy::random_product_amplitudes(n, fixed_parity != 0, sector, rng)
+                              : mipt::free_energy::random_haar_amplitudes(n, fixed_parity != 0, sector, rng);
+        for (std::size_t i = 0; i < amps.size(); ++i)
+        {
+            out_ri[2 * i] = amps[i].real();
+            out_ri[2 * i + 1] = amps[i].imag();
+        }
+        *parity = sector;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// The probed workspace's Haar layers for a 32-bit seed: fill_haar_layer per
+// timestep on the layer stream, uniforms from the measurement stream. Layout
+// as ref_haar_draw.
+int ref_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits, int *gates_per_layer, int *gate_q,
+                double *gate_m, int *sites_per_layer, int *sites, double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        std::mt19937 layer_rng, measure_rng;
+        layer_rng.seed(seed);
+        measure_rng.seed(seed ^ 0x9e3779b9u);
+        const int max_gates = n / 2;
+        int u = 0;
+        for (int l = 0; l < layers; ++l)
+        {
+            mipt::HaarLayer layer;
+            mipt::fill_haar_layer(layer, n, l % 2, p, true, layer_rng);
+            const auto ops = mipt::cusv::build_haar_layer_ops(layer, n);
+            gates_per_layer[l] = static_cast<int>(ops.ops.size());
+            for (std::size_t g = 0; g < ops.ops.size(); ++g)
+            {
+                const auto &op = ops.ops[g];
+                gate_q[(l * max_gates + g) * 2 + 0] = op.targets[0];
+                gate_q[(l * max_gates + g) * 2 + 1] = op.targets[1];
+                for (int e = 0; e < 16; ++e)
+                {
+                    gate_m[(l * max_gates + g) * 32 + 2 * e + 0] = op.matrix.values[e].real();
+                    gate_m[(l * max_gates + g) * 32 + 2 * e + 1] = op.matrix.values[e].imag();
+                }
+            }
+            sites_per_layer[l] = static_cast<int>(ops.measure_sites.size());
+            for (std::size_t s = 0; s < ops.measure_sites.size(); ++s) sites[l * n + s] = ops.measure_sites[s];
+            std::uniform_real_distribution<double> uniform(0.0, 1.0);
+            for (std::size_t b = 0; b < ops.measure_sites.size(); b += static_cast<std::size_t>(chunk_bits))
+                uniforms[u++] = uniform(measure_rng);
+        }
+        *n_uniforms = u;
         return 0;
     }
     catch (...)

@@ -190,6 +190,39 @@ def main():
         out[f"rho3_{k}_ferm"] = np.array([ferm])
         out[f"rho3_{k}_out"] = rho3
 
+    # --- free-energy protocol: initial states and workspace draws -----------
+    lib.ref_fe_initial_state.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp]
+    lib.ref_fe_draw.argtypes = [ctypes.c_uint32, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                ctypes.c_int] + [vp] * 7
+    fe_init = []
+    for k, (seed, n, kind, fixed) in enumerate([(11, 6, 0, 0), (12, 6, 1, 0), (13, 7, 0, 1), (14, 6, 1, 1),
+                                                (2**64 - 3, 10, 0, 0), (99, 10, 1, 0)]):
+        amps = np.zeros(2 << n)
+        par = np.zeros(1, np.int32)
+        assert lib.ref_fe_initial_state(seed, n, kind, fixed, amps.ctypes.data, par.ctypes.data) == 0
+        out[f"feinit{k}_amps"] = amps
+        fe_init.append((seed, n, kind, fixed, par[0]))
+    out["feinit_params"] = np.array(fe_init, np.uint64)
+    FE_DRAWS = [(0x12345678, 6, 12, 0.3, 16), (7, 8, 10, 1.0, 3), (0xFFFFFFFF, 10, 6, 0.1, 16), (1, 4, 8, 0.0, 16)]
+    out["fedraw_params"] = np.array(FE_DRAWS, np.float64)
+    for k, (seed, n, layers, p, chunk) in enumerate(FE_DRAWS):
+        mg = n // 2
+        gpl = np.zeros(layers, np.int32)
+        gq = np.zeros((layers, mg, 2), np.int32)
+        gm = np.zeros((layers, mg, 32))
+        spl = np.zeros(layers, np.int32)
+        sites = np.full((layers, n), -1, np.int32)
+        uni = np.zeros(layers * n + 1)
+        nu = np.zeros(1, np.int32)
+        assert lib.ref_fe_draw(seed, n, layers, p, chunk,
+                               *[a.ctypes.data for a in (gpl, gq, gm, spl, sites, uni, nu)]) == 0
+        out[f"fedraw{k}_gates_per_layer"] = gpl
+        out[f"fedraw{k}_gate_q"] = gq
+        out[f"fedraw{k}_gate_m"] = gm
+        out[f"fedraw{k}_sites_per_layer"] = spl
+        out[f"fedraw{k}_sites"] = sites
+        out[f"fedraw{k}_uniforms"] = uni[: nu[0]].copy()
+
     path = os.path.join(HERE, "ref_fixtures.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.1f} KiB, {len(out)} arrays)")

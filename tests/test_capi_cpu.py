@@ -61,3 +61,30 @@ def test_host_sampler_matches_reference(mg, k):
 def test_bad_arguments_fail_loudly(mg):
     with pytest.raises(mg.MiptError):
         mg.draw_haar(1, 7, 2, 0.2)  # odd chain
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["feinit_params"])))
+def test_initial_state_draw_matches_reference(mg, k):
+    seed, n, kind, fixed, parity = (int(x) for x in GOLD["feinit_params"][k])
+    psi, sector = mg.draw_initial_state(seed, n, kind, bool(fixed), fp64=True)
+    np.testing.assert_array_equal(psi, GOLD[f"feinit{k}_amps"].view(np.complex128))
+    assert sector == (parity if parity < 2**63 else -1)
+    # The FP32 draw rounds where an FP32 state stores: the oracle does the same.
+    from oracle import pyoracle as orc
+    psi32, _ = mg.draw_initial_state(seed, n, kind, bool(fixed), fp64=False)
+    want32, _ = orc.fe_initial_state(seed, n, kind, bool(fixed), fp32=True)
+    np.testing.assert_array_equal(psi32, want32)
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["fedraw_params"])))
+def test_workspace_sampler_matches_reference(mg, k):
+    seed, n, layers, p, chunk = GOLD["fedraw_params"][k]
+    n, layers, chunk = int(n), int(layers), int(chunk)
+    d = mg.draw_haar_workspace(int(seed), n, layers, float(p), chunk)
+    np.testing.assert_array_equal(d["gates_per_layer"], GOLD[f"fedraw{k}_gates_per_layer"])
+    np.testing.assert_array_equal(d["bond_q"], GOLD[f"fedraw{k}_gate_q"])
+    np.testing.assert_allclose(d["bond_u"], GOLD[f"fedraw{k}_gate_m"], rtol=0, atol=1e-12)
+    sites, spl = GOLD[f"fedraw{k}_sites"], GOLD[f"fedraw{k}_sites_per_layer"]
+    for t in range(layers):
+        assert int(d["measured"][t]) == sum(1 << int(s) for s in sites[t, : spl[t]])
+    np.testing.assert_array_equal(d["uniforms"], GOLD[f"fedraw{k}_uniforms"])

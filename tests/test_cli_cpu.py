@@ -211,3 +211,94 @@ def test_entropy_usage_argument_errors_and_checkpoints(exes, tmp_path):
     (tmp_path / "other.csv").write_text("a,b\n1,2\n")
     r = run([ent, "8", "2", "0.1", "2", "1", "other.csv"], tmp_path)
     assert r.returncode == 1 and "different column layout" in r.stderr
+
+
+FE_SAMPLES_HEADER = ("N,p,circ_type,circuit_name,init_state,trajectory,parity_sector,trajectory_seed,"
+                     "equil_timesteps,production_timesteps,total_timesteps,measurements_total,"
+                     "measurements_production,F_total,F_production,production_rate_endpoint,production_slope,"
+                     "free_energy_density_tilde")
+FE_SERIES_HEADER = ("N,p,circ_type,circuit_name,init_state,requested_realizations,completed_realizations,t,"
+                    "t_over_L,phase,F_mean,F_stddev,F_stderr,F_over_tL_mean,F_over_tL_stddev,F_over_tL_stderr,"
+                    "S_half_mean,S_half_stddev,S_half_stderr,S_half_count")
+
+
+def fe_files(n, p, init, requested, completed, master, entropy_max_t=None):
+    """A free-energy checkpoint of `completed` trajectories in the reference's
+    layout (cpp/include/mipt/free_energy_resume.hpp:79-88); values are
+    placeholders, seeds follow splitmix64(master ^ trajectory)."""
+    from oracle import pyoracle as orc
+    T, eq = 28 * n, 4 * n
+    mt = 2 * n if entropy_max_t is None else entropy_max_t
+    name = '"Random Haar Unitary"'
+    rows = [FE_SAMPLES_HEADER]
+    for t in range(completed):
+        ts = orc.fe_trajectory_seed(master, t)
+        rows.append(f"{n},{float(p)!r},1,{name},{init},{t},-1,{ts},{eq},{24 * n},{T},10,8,1.5,1.25,0.1,0.1,0.0125")
+    series = [FE_SERIES_HEADER]
+    for t in range(T + 1):
+        phase = "initial" if t == 0 else ("equilibration" if t <= eq else "production")
+        s_count = completed if (t == 0 or (t <= mt)) else 0
+        s_stat = "0.5,0.1,0.05" if s_count else "nan,nan,nan"
+        f = "0,0,0" if t == 0 else "0.25,0.01,0.005"
+        ftl = "nan,nan,nan" if t == 0 else "0.01,0.001,0.0005"
+        series.append(f"{n},{float(p)!r},1,{name},{init},{requested},{completed},{t},{t / n!r},{phase},"
+                      f"{f},{ftl},{s_stat},{s_count}")
+    return "\n".join(rows) + "\n", "\n".join(series) + "\n"
+
+
+def test_free_energy_usage_argument_errors_and_checkpoints(exes, tmp_path):
+    """free_energy.exe's argument contract (cpp/apps/free_energy.cpp:164-240)
+    and its checkpoint refusals (cpp/apps/free_energy.cpp:254-358,
+    cpp/include/mipt/free_energy_resume.hpp:246-534); every case ends
+    before device work."""
+    fe = os.path.join(os.path.dirname(exes[0]), "free_energy.exe")
+    r = run([fe, "--help"], tmp_path)
+    assert r.returncode == 0 and "Usage:" in r.stdout and "MIPT_FREE_ENERGY_ENTROPY_STRIDE" in r.stdout
+    r = run([fe, "8", "0.1"], tmp_path)
+    assert r.returncode == 2 and "Usage:" in r.stdout
+    for args, msg in [(["8", "0.1", "0", "1", "0"], "realizations must lie in [1,1000000000]."),
+                      (["31", "0.1", "2", "1", "0"], "N must lie in [2,30]"),
+                      (["9", "0.1", "2", "1", "0"], "requires an even N"),
+                      (["8", "1.5", "2", "1", "0"], "p must lie in [0,1]."),
+                      (["8", "0.1", "2", "1", "2"], "init_state must be 0 or 1."),
+                      (["8", "0.1", "2", "2", "0"], "not on the GB300 trajectory path"),
+                      (["8", "0.1", "2", "9", "0"], "circ_type must be one of")]:
+        r = run([fe] + args, tmp_path)
+        assert r.returncode == 1 and "free_energy.exe: " in r.stderr and msg in r.stderr, (args, r.stderr)
+    stem = "free_energy_haar_n_8_p_0.1_init_0_reals_3"
+    samples, series = fe_files(8, 0.1, 0, 3, 3, master=77)
+    (tmp_path / f"{stem}_samples.csv").write_text(samples)
+    (tmp_path / f"{stem}_timeseries.csv").write_text(series)
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 0 and "is already complete (3/3 trajectories). Nothing to do." in r.stdout, r.stderr
+    assert "seed stream recovered" in r.stdout
+    # Only one of the two files: refused.
+    (tmp_path / f"{stem}_timeseries.csv").unlink()
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "Both CSVs are needed to continue a run" in r.stderr
+    # A different entropy schedule than the checkpoint's.
+    (tmp_path / f"{stem}_timeseries.csv").write_text(series)
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path, {"MIPT_FREE_ENERGY_ENTROPY_MAX_T": "5"})
+    assert r.returncode == 1 and "S_half_count=3 at t=6" in r.stderr, r.stderr
+    # An aggregate ahead of the samples file.
+    samples2, _ = fe_files(8, 0.1, 0, 3, 2, master=77)
+    (tmp_path / f"{stem}_samples.csv").write_text(samples2)
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "aggregates 3 trajectories but" in r.stderr
+    # Trajectory indices with a gap.
+    lines = samples.splitlines()
+    del lines[2]
+    (tmp_path / f"{stem}_samples.csv").write_text("\n".join(lines) + "\n")
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "has trajectory=2 where 1 was expected" in r.stderr
+    # Another run's identity and another layout.
+    (tmp_path / f"{stem}_samples.csv").write_text(samples.replace(",0,0,-1,", ",1,0,-1,", 1))
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "was produced with init_state=1" in r.stderr, r.stderr
+    (tmp_path / f"{stem}_samples.csv").write_text("a,b\n1,2\n")
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path)
+    assert r.returncode == 1 and "different column layout" in r.stderr
+    # The recovered master seed wins over MIPT_FREE_ENERGY_SEED.
+    (tmp_path / f"{stem}_samples.csv").write_text(samples)
+    r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path, {"MIPT_FREE_ENERGY_SEED": "5"})
+    assert r.returncode == 0 and "Nothing to do." in r.stdout

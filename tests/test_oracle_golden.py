@@ -123,3 +123,47 @@ def test_page_state_tmi():
     # both deep-circuit and exactly random states sit near the Page value
     assert abs(orc.tmi(psi, 0, 1) - orc.tmi(haar, 0, 1)) < 0.5
     assert orc.tmi(psi, 0, 1) < -1.0
+
+
+# ------------------------------------------------------------ free energy
+@pytest.mark.parametrize("k", range(len(GOLD["feinit_params"])))
+def test_free_energy_initial_state_matches_reference(k):
+    seed, n, kind, fixed, parity = (int(x) for x in GOLD["feinit_params"][k])
+    want = GOLD[f"feinit{k}_amps"].view(np.complex128)
+    psi, sector = orc.fe_initial_state(seed, n, kind, bool(fixed))
+    np.testing.assert_array_equal(psi, want)
+    assert sector == (parity if parity < 2**63 else -1)
+    assert abs(np.linalg.norm(psi) - 1.0) < 1e-12
+    if fixed:
+        # Every amplitude lies in the drawn parity sector.
+        support = np.nonzero(np.abs(psi) > 0)[0]
+        assert all(bin(int(x)).count("1") % 2 == sector for x in support)
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["fedraw_params"])))
+def test_free_energy_workspace_draw_matches_reference(k):
+    seed, n, layers, p, chunk = GOLD["fedraw_params"][k]
+    d = orc.fe_draw(int(seed), int(n), int(layers), float(p), int(chunk))
+    for f in ("gates_per_layer", "gate_q", "sites_per_layer", "sites", "uniforms"):
+        np.testing.assert_array_equal(d[f], GOLD[f"fedraw{k}_{f}"])
+    np.testing.assert_allclose(d["gate_m"], GOLD[f"fedraw{k}_gate_m"], rtol=0, atol=1e-12)
+
+
+def test_free_energy_trajectory_invariants():
+    """Seed derivation, the draw the trajectory runs, the entropy schedule,
+    and the chain rule: a layer's surprisal is -log of its joint outcome
+    probability, zero on layers without measurements."""
+    ts = orc.fe_trajectory_seed(0xC0FFEE, 3)
+    assert ts == orc.lib().orc_splitmix64(0xC0FFEE ^ 3)
+    n = 6
+    r = orc.fe_trajectory(ts, n, 0.3, init_kind=1, entropy_max_t=2 * n, entropy_stride=5)
+    T = 28 * n
+    d = orc.fe_draw(orc.fe_workspace_seed(ts), n, T, 0.3)
+    np.testing.assert_array_equal(r["measured"], d["sites_per_layer"])
+    assert np.all(r["surprisal"] >= 0) and np.all(r["surprisal"][r["measured"] == 0] == 0)
+    sampled = [t for t in range(T + 1) if not np.isnan(r["s_half"][t])]
+    assert sampled == [0, 5, 10, 12]
+    assert 0 <= np.nanmax(r["s_half"]) <= n // 2
+    # Product initial state: zero half-chain entropy at t = 0.
+    r0 = orc.fe_trajectory(ts, n, 0.3, init_kind=0)
+    assert abs(r0["s_half"][0]) < 1e-12
