@@ -471,10 +471,51 @@ def config4():
                              "sample": f"{len(sample)} states, FP64 ADMM oracle (the reference uses MOSEK, absent)"}}
 
 
+def config5():
+    """The free-energy protocol (free_energy.exe's loop): N = 16 periodic Haar
+    brickwork, p = 0.1, random Haar initial states, 28N = 448 timesteps per
+    trajectory, half-chain S_vN at t = 0..2N; 512 trajectories in one batch,
+    FP32 states. Timed end to end through the batch calls the executable makes
+    (initial-state draw and upload, layer draw, all layers, fetch)."""
+    import mipt_gb300 as mg
+    from oracle import pyoracle as orc
+    n, p, count = 16, 0.1, 512
+    T = 28 * n
+    steps = list(range(2 * n + 1))
+    b = mg.Batch(n, T // 2, count, closed=True, fp64=False, observables=mg.OBS_SVN_HALF)
+    b.set_observation_steps(steps)
+    ts = [orc.fe_trajectory_seed(5, i) for i in range(count)]
+    init = [orc.fe_initial_seed(t) for t in ts]
+    ws = [orc.fe_workspace_seed(t) for t in ts]
+
+    def step():
+        b.set_initial_states(init, 1)
+        b.prepare_workspace(ws, p)
+        b.execute()
+        return b.fetch()
+
+    step()
+    b.set_profiling(True)
+    out, dt = _timed(step)
+    stats = b.kernel_stats()
+    want = orc.fe_trajectory(ts[0], n, p, 1, fp32_init=True, entropy_max_t=2 * n)
+    threads = orc.max_threads()
+    _, cdt = _timed(lambda: orc.fe_batch(5, 0, threads, n, p, 1, threads=threads))
+    return {"config": "5: free-energy protocol N=16 periodic Haar, p=0.1, Haar initial states, 448 timesteps, "
+                      "S_vN(half) at t=0..32, 512 trajectories, FP32",
+            "value": count * T / dt, "unit": UNIT, "trajectories_per_s": count / dt,
+            "kernel_ms": {k: v[0] for k, v in stats.items()},
+            "max_abs_dF_vs_oracle_traj0": float(abs(out["surprisal"][0].sum() - want["surprisal"].sum())),
+            "max_abs_dS_vs_oracle_traj0": float(np.max(np.abs(out["obs"][0, :, 0] - want["s_half"][steps]))),
+            "cpu_baseline": {"value": threads * T / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{threads} trajectories, FP64 oracle, one per host thread, "
+                                       "no entropies (the GPU arm includes them)"}}
+
+
 def run_config(k):
     import torch
     torch.cuda.set_device(0)
-    fn = [config0, config1, config2, config3, config4][k]
+    fn = [config0, config1, config2, config3, config4, config5][k]
     line = fn()
     line["data"] = "synthetic"
     print(json.dumps(line), flush=True)
@@ -489,7 +530,7 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tile", type=int, default=0, help="local qubits per pass tile (0 = library default)")
-    ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..4 instead")
+    ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..5 instead")
     args = ap.parse_args()
     if args.config >= 0:
         return run_config(args.config)
