@@ -132,9 +132,12 @@ __global__ void k_scatter(const double *in, const int *idx, int n, double *out, 
 }
 
 // S = -sum lambda log2 lambda over lambda > 1e-15 (fixed-order reduction).
+// Block b: entropy (bits) of the spectrum w[b*d .. b*d + d) into out[b].
 __global__ void k_entropy_from_eigs(const double *w, int d, double *out)
 {
     __shared__ double red[256];
+    w += static_cast<std::size_t>(blockIdx.x) * d;
+    out += blockIdx.x;
     double s = 0.0;
     for (int i = threadIdx.x; i < d; i += blockDim.x)
     {
@@ -166,8 +169,12 @@ struct Workspace
 {
     DevBuf jobs, rho, scratch, vals, idx, eig, work, info, err, rows;
     cusolverDnHandle_t solver = nullptr;
+    cusolverDnParams_t params = nullptr;
+    std::vector<char> host_work;
+    bool batched_eig_failed = false;
     ~Workspace()
     {
+        if (params) cusolverDnDestroyParams(params);
         if (solver) cusolverDnDestroy(solver);
     }
 };
@@ -318,14 +325,42 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
             }
             else
             {
-                // Large spectra: FP64 divide-and-conquer eigensolver (cuSOLVER),
-                // one matrix at a time.
+                // Large spectra: FP64 eigenvalues from cuSOLVER, all matrices of
+                // the group in one batched call; one matrix at a time only if
+                // the batched routine is unavailable.
                 if (!ws.solver)
                 {
                     if (cusolverDnCreate(&ws.solver) != CUSOLVER_STATUS_SUCCESS)
                         return fail(MIPT_GB300_E_INTERNAL, "cusolverDnCreate failed");
                 }
                 cusolverDnSetStream(ws.solver, s);
+                if (!ws.params && cusolverDnCreateParams(&ws.params) != CUSOLVER_STATUS_SUCCESS)
+                    return fail(MIPT_GB300_E_INTERNAL, "cusolverDnCreateParams failed");
+                std::size_t dev_bytes = 0, host_bytes = 0;
+                if (!ws.batched_eig_failed &&
+                    cusolverDnXsyevBatched_bufferSize(ws.solver, ws.params, CUSOLVER_EIG_MODE_NOVECTOR,
+                                                      CUBLAS_FILL_MODE_LOWER, d, CUDA_C_64F, ws.rho.p, d, CUDA_R_64F,
+                                                      ws.eig.p, CUDA_C_64F, &dev_bytes, &host_bytes,
+                                                      nbi) == CUSOLVER_STATUS_SUCCESS)
+                {
+                    MG_CUDA(ws.work.ensure(std::max<std::size_t>(dev_bytes, 16)));
+                    MG_CUDA(ws.eig.ensure(sizeof(double) * d * static_cast<std::size_t>(nbi)));
+                    MG_CUDA(ws.info.ensure(sizeof(int) * static_cast<std::size_t>(nbi)));
+                    ws.host_work.resize(std::max<std::size_t>(host_bytes, 16));
+                    if (cusolverDnXsyevBatched(ws.solver, ws.params, CUSOLVER_EIG_MODE_NOVECTOR,
+                                               CUBLAS_FILL_MODE_LOWER, d, CUDA_C_64F, ws.rho.p, d, CUDA_R_64F,
+                                               ws.eig.p, CUDA_C_64F, ws.work.p, dev_bytes, ws.host_work.data(),
+                                               host_bytes, ws.info.as<int>(), nbi) == CUSOLVER_STATUS_SUCCESS)
+                    {
+                        k_entropy_from_eigs<<<nbi, 256, 0, s>>>(ws.eig.as<double>(), d, ws.vals.as<double>());
+                        launches += 2;
+                        k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi,
+                                                                    d_out, 0);
+                        ++launches;
+                        continue;
+                    }
+                }
+                ws.batched_eig_failed = true;
                 int lwork = 0;
                 if (cusolverDnZheevd_bufferSize(ws.solver, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, d,
                                                 ws.rho.as<cuDoubleComplex>(), d, ws.eig.as<double>(), &lwork) !=

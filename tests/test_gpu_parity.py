@@ -283,3 +283,23 @@ def test_fp32_region_svn_large_state(mg):
     np.testing.assert_array_equal(runs[False][1], runs[True][1])
     assert runs[True][0].max() > 1.0  # entangled regions, not only product states
     np.testing.assert_allclose(runs[False][0], runs[True][0], rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("fp64", [True, False])
+def test_large_spectrum_svn_batched_eigensolver(mg, orc, fp64):
+    """S_vN of 8- and 9-qubit regions (256 x 256 and 512 x 512 spectra, the
+    batched FP64 eigensolver) for several trajectories at once, against the
+    oracle's RDM eigenvalues of the same final states."""
+    n, periods, p = 18, 2, 0.15
+    seeds = [mg.trajectory_seed(31, i) for i in range(3)]
+    b = mg.Batch(n, periods, capacity=len(seeds), fp64=fp64)
+    regions = [list(range(8)), list(range(9)), [0, 2, 4, 6, 8, 10, 12, 14]]
+    for r in regions:
+        b.add_region(r, 1)
+    b.run(seeds, p)
+    got = b.fetch_regions()
+    for i, sd in enumerate(seeds):
+        psi = orc.run_trajectory(int(sd), n, periods, p, closed=True, want_state=True)["psi"]
+        for g, r in enumerate(regions):
+            want = orc.entropy(orc.rdm(psi, r), 1)
+            assert abs(got[i, 0, g] - want) < (1e-10 if fp64 else 1e-5), (i, r, got[i, 0, g], want)
