@@ -211,6 +211,13 @@ typedef struct mipt_gb300_batch_config
                           at most n/4) -- cpp/include/mipt/tmi/compute.hpp:89-113 */
     int lattice_x;     /* lattice_y > 1: 2-D four-colour brickwork on a lattice_x x lattice_y torus */
     int lattice_y;     /* (n_qubits = x * y, qubit = row * x + column; closed is ignored) */
+    int circuit;       /* gate set, the reference's circ_type: 0 or 1 Haar brickwork; 2 FermionRPPU,
+                          4 qRPPU (closed 1-D ring; layers = 2 * periods + 1, the last one the
+                          reference's random extra even layer or an identity layer) --
+                          cpp/include/mipt/circuits/rppu_layer.hpp:167-300 */
+    int split_last;    /* RPPU: measure site n-1 as its own chunk after the others, as the
+                          reference's parity-sector engine does (its default; MIPT_CUSV_PARITY=0
+                          there is split_last = 0) -- cpp/include/mipt/cusv/engine.hpp:415-458 */
 } mipt_gb300_batch_config;
 
 typedef struct mipt_gb300_batch mipt_gb300_batch;
@@ -229,11 +236,12 @@ int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, 
                              int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count);
 void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
 
-/* Draw `count` Haar trajectories (trajectory i from seeds[i] with
- * measurement rate p[i]) on host threads exactly as the reference's
- * HaarCircuit1D draws them (cpp/include/mipt/circuit.hpp:129-140,415-439),
- * and upload gates, measurement sites and uniforms. forced_outcomes
- * (nullable, [count][2*periods] bit masks) replays recorded outcomes. */
+/* Draw `count` trajectories (trajectory i from seeds[i] with measurement
+ * rate p[i]) on host threads exactly as the reference's HaarCircuit1D
+ * (cpp/include/mipt/circuit.hpp:129-140,415-439) -- or, for circuit 2/4, its
+ * RppuCircuit1D / QrppuCircuit1D (circuit.hpp:445-560) -- draws them, and
+ * upload gates, measurement sites and uniforms. forced_outcomes (nullable,
+ * [count][layers] bit masks) replays recorded outcomes. */
 int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *batch, const uint64_t *seeds, const double *p, int count,
                                   const uint64_t *forced_outcomes);
 /* Free-energy protocol (cpp/apps/free_energy.cpp:460-533): the same Haar
@@ -422,6 +430,15 @@ int mipt_gb300_draw_haar(uint64_t seed, int n_qubits, int periods, double p, int
                          int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured, double *uniforms,
                          int *n_uniforms);
 
+/* One RPPU / qRPPU trajectory as the batch draws it (circuit 2 or 4; the
+ * draw is the same, the batch adds the fermionic closure string for 2):
+ * 2*periods + 1 layers in the plan's bond order (odd layers end with the
+ * closure bond (n-1, 0)); a missing extra even layer is identity gates.
+ * workspace = 1: the probed workspace's streams from the low 32 bits of seed,
+ * 2*periods layers and an identity last layer. Outputs as mipt_gb300_draw_haar. */
+int mipt_gb300_draw_rppu(uint64_t seed, int n_qubits, int periods, double p, int chunk_bits, int split_last,
+                         int workspace, int *gates_per_layer, int *bond_q, double *bond_u, uint64_t *measured,
+                         double *uniforms, int *n_uniforms);
 /* The free-energy workspace draw of one trajectory on the host (closed ring,
  * `layers` layers; outputs as mipt_gb300_draw_haar). */
 int mipt_gb300_draw_haar_workspace(uint32_t seed, int n_qubits, int layers, double p, int chunk_bits,

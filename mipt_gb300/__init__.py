@@ -38,7 +38,8 @@ class FFConfig(ctypes.Structure):
 class BatchConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in (
         "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
-        "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles", "lattice_x", "lattice_y")]
+        "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles", "lattice_x", "lattice_y", "circuit",
+        "split_last")]
 
 
 def lib():
@@ -83,6 +84,7 @@ def lib():
     L.mipt_gb300_batch_set_observation_steps.argtypes = [vp, vp, ci]
     L.mipt_gb300_draw_initial_state.argtypes = [u64, ci, ci, ci, ci, vp, vp]
     L.mipt_gb300_draw_haar_workspace.argtypes = [ctypes.c_uint32, ci, ci, cd, ci, vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_draw_rppu.argtypes = [u64, ci, ci, cd, ci, ci, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_execute.argtypes = [vp, vp]
     L.mipt_gb300_batch_fetch.argtypes = [vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_batch_fetch_tmi.argtypes = [vp, ci, vp]
@@ -169,6 +171,20 @@ def draw_haar_workspace(seed32, n, layers, p, chunk_bits=16):
     nu = np.zeros(1, np.int32)
     _check(lib().mipt_gb300_draw_haar_workspace(seed32, n, layers, p, chunk_bits, _p(gpl), _p(bq), _p(bu),
                                                 _p(meas), _p(uni), _p(nu)))
+    return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu[0]].copy())
+
+
+def draw_rppu(seed, n, periods, p, chunk_bits=16, split_last=True, workspace=False):
+    """Host draw of one RPPU / qRPPU trajectory as the batch runs it (2*periods + 1 layers)."""
+    L = 2 * periods + 1
+    gpl = np.zeros(L, np.int32)
+    bq = np.zeros((L, n // 2, 2), np.int32)
+    bu = np.zeros((L, n // 2, 32))
+    meas = np.zeros(L, np.uint64)
+    uni = np.zeros(L * n + L)
+    nu = np.zeros(1, np.int32)
+    _check(lib().mipt_gb300_draw_rppu(seed, n, periods, p, chunk_bits, int(split_last), int(workspace), _p(gpl),
+                                      _p(bq), _p(bu), _p(meas), _p(uni), _p(nu)))
     return dict(gates_per_layer=gpl, bond_q=bq, bond_u=bu, measured=meas, uniforms=uni[: nu[0]].copy())
 
 
@@ -285,16 +301,18 @@ class Batch:
 
     def __init__(self, n, periods, capacity, closed=True, fp64=False, chunk_bits=16, observables=0,
                  observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0, tmi_cycles=0,
-                 lattice=None):
+                 lattice=None, circuit=1, split_last=True):
         lx, ly = lattice if lattice is not None else (0, 0)
         cfg = BatchConfig(n, periods, int(closed), int(fp64), chunk_bits, observables, observe_every, int(rho3),
-                          int(fermion_trace), host_threads, tile_qubits, tmi_cycles, lx, ly)
+                          int(fermion_trace), host_threads, tile_qubits, tmi_cycles, lx, ly, int(circuit),
+                          int(split_last))
         self.regions = 0
         self.tmi_cycles = max(1, tmi_cycles)
         h = ctypes.c_void_p()
         _check(lib().mipt_gb300_batch_create(ctypes.byref(cfg), capacity, ctypes.byref(h)))
         self._h = h
-        self.n, self.periods, self.layers = n, periods, 2 * periods
+        self.n, self.periods = n, periods
+        self.layers = 2 * periods + (1 if circuit in (2, 4) else 0)
         self.observe_every = observe_every
         self.points = (self.layers // observe_every) if observe_every > 0 else 1
         self.rho3 = rho3

@@ -63,15 +63,30 @@ inline void print_circuit_type_help(std::ostream &out, const char *indent)
     for (int i = 0; i < 5; ++i) out << indent << i << " = " << kCircuits[i].help << '\n';
 }
 
-// The GB300 path runs the Haar brickwork; the other gate sets stay with the
-// reference.
+// The GB300 path runs the Haar brickwork and the parity-preserving RPPU /
+// qRPPU gate sets; MMS and RFGS stay with the reference.
+inline bool on_gb300_path(int type) { return type == kHaar || type == 2 || type == 4; }
+
 inline void require_gb300_circuit(int type)
 {
     const CircuitInfo &c = circuit_info(type);
-    if (type != kHaar)
+    if (!on_gb300_path(type))
         throw std::invalid_argument(std::string("circ_type ") + std::to_string(type) + " (" + c.name +
                                     ") is not on the GB300 trajectory path; use circ_type=1 (" +
-                                    kCircuits[kHaar].name + ").");
+                                    kCircuits[kHaar].name + "), 2 (" + kCircuits[2].name + ") or 4 (" +
+                                    kCircuits[4].name + ").");
+}
+
+inline bool env_bool_flag(const char *name, bool fallback);
+
+// Gate set, partial-trace convention and, for the RPPU sets, the measurement
+// chunking of the reference's parity-sector engine (site n-1 on its own;
+// MIPT_CUSV_PARITY=0 selects the plain chunking, as in the reference).
+inline void configure_circuit(mipt_gb300_batch_config &cfg, int type)
+{
+    cfg.circuit = type == kHaar ? 0 : type;
+    cfg.fermion_trace = circuit_info(type).fermionic_trace ? 1 : 0;
+    cfg.split_last = (type == 2 || type == 4) && env_bool_flag("MIPT_CUSV_PARITY", true) ? 1 : 0;
 }
 
 inline void validate_circuit_site_count(int type, int sites, const char *site_name = "n")
@@ -111,6 +126,17 @@ inline bool env_falsey_path(const char *v)
     std::string t(v);
     for (auto &c : t) c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
     return t == "0" || t == "false" || t == "off" || t == "no" || t == "none" || t == "disabled";
+}
+
+inline bool env_bool_flag(const char *name, bool fallback)
+{
+    const char *v = std::getenv(name);
+    if (!v) return fallback;
+    std::string t(v);
+    for (auto &c : t) c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
+    if (t == "1" || t == "true" || t == "yes" || t == "on") return true;
+    if (t == "0" || t == "false" || t == "no" || t == "off") return false;
+    return fallback;
 }
 
 inline long env_long(const char *name, long fallback)

@@ -111,7 +111,8 @@ void write_results(const std::string &path, int n, int periods, double p, int re
         const bool has1 = a.count > 0;
         out += std::to_string(n) + ',' + std::to_string(periods) + ',' + fmt(p) + ',' + std::to_string(requested) +
                ',' + std::to_string(b.count) + ',' + std::to_string(circ_type) + ',' +
-               quote(circuit_info(circ_type).name) + ",0," + std::to_string(kept) + ',' + fmt(x) + ',' +
+               quote(circuit_info(circ_type).name) + ',' + (circuit_info(circ_type).fermionic_trace ? "1" : "0") +
+               ',' + std::to_string(kept) + ',' + fmt(x) + ',' +
                fmt(std::log(x)) + ',' + fmt(has1 ? a.mean : nan) + ',' + fmt(has1 ? a.stddev() : nan) + ',' +
                fmt(has1 ? a.stderr_() : nan) + ',' + fmt(b.mean) + ',' + fmt(b.stddev()) + ',' + fmt(b.stderr_()) +
                ',' + std::to_string(n) + ',' + std::to_string(static_cast<std::uint64_t>(n) * b.count) + '\n';
@@ -349,7 +350,8 @@ int main(int argc, char **argv)
         const std::uint64_t seed = master_seed();
         std::cout << "Running entanglement-entropy chord-length scan: N=" << n << ", periods=" << periods
                   << ", p=" << p << ", realizations=" << realizations << ", circ_type=" << circ_type << " ("
-                  << circuit_info(circ_type).name << "), fermionic_trace=0\n"
+                  << circuit_info(circ_type).name << "), fermionic_trace="
+                  << (circuit_info(circ_type).fermionic_trace ? 1 : 0) << "\n"
                   << "Averaging each L_A over " << n << " contiguous cyclic translations per traj.\n"
                   << "Entropies: S2 for L_A=" << min_kept << ".." << max_block << "; S1 ";
         if (max_s1 < min_kept)
@@ -366,6 +368,7 @@ int main(int argc, char **argv)
         cfg.closed = 1;
         cfg.fp64 = fp64 ? 1 : 0;
         cfg.chunk_bits = 16;
+        configure_circuit(cfg, circ_type);
         Batch batch(cfg, capacity);
         // Regions: (L_A, translation) -> S2 column and, when computed, S1 column.
         std::vector<int> col2(static_cast<std::size_t>((max_block + 1) * n), -1), col1(col2.size(), -1);

@@ -664,15 +664,20 @@ int run(int argc, char **argv)
     cfg.fp64 = fp64 ? 1 : 0;
     cfg.chunk_bits = 16;
     cfg.observables = steps.empty() ? 0 : MIPT_GB300_OBS_SVN_HALF;
+    configure_circuit(cfg, circ_type);
+    cfg.split_last = 0; // the free-energy loop measures the full state (cpp/include/mipt/probed.hpp:589-598)
     Batch batch(cfg, capacity);
+    // RPPU batches carry one more (identity) layer slot after the 28N timesteps.
+    const int slots = total + (cfg.circuit == 2 || cfg.circuit == 4 ? 1 : 0);
+    const bool fixed_parity = circ_type == 2 || circ_type == 3 || circ_type == 4;
     if (!steps.empty())
         check(mipt_gb300_batch_set_observation_steps(batch.get(), steps.data(), static_cast<int>(steps.size())),
               "mipt_gb300_batch_set_observation_steps");
     const int points = steps.empty() ? 1 : static_cast<int>(steps.size());
 
-    std::vector<std::uint64_t> tseed(capacity), init_seed(capacity), measured(static_cast<std::size_t>(capacity) * total);
+    std::vector<std::uint64_t> tseed(capacity), init_seed(capacity), measured(static_cast<std::size_t>(capacity) * slots);
     std::vector<std::uint32_t> wseed(capacity);
-    std::vector<double> prob(capacity, p), surprisal(static_cast<std::size_t>(capacity) * total),
+    std::vector<double> prob(capacity, p), surprisal(static_cast<std::size_t>(capacity) * slots),
         obs(static_cast<std::size_t>(capacity) * points * 4);
     std::vector<int> sector(capacity);
 
@@ -690,7 +695,8 @@ int run(int argc, char **argv)
             wseed[i] = static_cast<std::uint32_t>(splitmix(tseed[i] ^ kCircuitSalt));
             init_seed[i] = splitmix(tseed[i] ^ kInitialSalt);
         }
-        check(mipt_gb300_batch_set_initial_states(batch.get(), init_seed.data(), init_state, 0, count, sector.data()),
+        check(mipt_gb300_batch_set_initial_states(batch.get(), init_seed.data(), init_state, fixed_parity ? 1 : 0,
+                                                  count, sector.data()),
               "mipt_gb300_batch_set_initial_states");
         check(mipt_gb300_batch_prepare_haar_workspace(batch.get(), wseed.data(), prob.data(), count),
               "mipt_gb300_batch_prepare_haar_workspace");
@@ -701,8 +707,8 @@ int run(int argc, char **argv)
         std::string rows;
         for (int i = 0; i < count; ++i)
         {
-            const double *sp = surprisal.data() + static_cast<std::size_t>(i) * total;
-            const std::uint64_t *mm = measured.data() + static_cast<std::size_t>(i) * total;
+            const double *sp = surprisal.data() + static_cast<std::size_t>(i) * slots;
+            const std::uint64_t *mm = measured.data() + static_cast<std::size_t>(i) * slots;
             double cumulative = 0.0, prod_f = 0.0;
             std::uint64_t meas_total = 0, meas_prod = 0;
             LineFit fit;

@@ -98,6 +98,7 @@ void run_1d(int n, int periods, int realizations, int res, double p_min, double 
     cfg.chunk_bits = 16;
     cfg.rho3 = 1;
     cfg.fermion_trace = fermion_trace ? 1 : 0;
+    configure_circuit(cfg, circ_type);
     Batch batch(cfg, capacity);
     const std::uint64_t seed = master_seed();
     std::cout << "GB300 path: " << mipt_gb300_version() << ", " << (fp64 ? "FP64" : "FP32")
@@ -157,7 +158,8 @@ void print_usage(const char *argv0)
     std::cout << "  p_max = maximum measurement rate\n";
     std::cout << "  circ_type:\n";
     print_circuit_type_help(std::cout, "    ");
-    std::cout << "  On the GB300 path circ_type=1 (Haar brickwork) runs; d=2 is not on this path.\n";
+    std::cout << "  On the GB300 path circ_type=1 (Haar brickwork), 2 (FermionRPPU) and 4 (qRPPU) run; d=2 is not on\n"
+                 "  this path.\n";
 }
 
 int run_cli(int argc, char *argv[])

@@ -342,7 +342,7 @@ void run(int n, int periods, int realizations, int res, double p_min, double p_m
     cfg.fp64 = fp64 ? 1 : 0;
     cfg.chunk_bits = 16;
     cfg.observables = order == 2 ? MIPT_GB300_OBS_TMI_S2 : MIPT_GB300_OBS_TMI_VN;
-    cfg.fermion_trace = circuit_info(circ_type).fermionic_trace ? 1 : 0;
+    configure_circuit(cfg, circ_type);
     cfg.tmi_cycles = cycles;
     Batch batch(cfg, capacity);
     const std::uint64_t seed = master_seed();
@@ -409,7 +409,7 @@ void print_usage(const char *argv0)
               << " [n = 10] [periods = 10] [realizations = 10] [resolution = 5] [p_min = 0.0] [p_max = 1.0]"
                  " [circ_type = 0] [all_cycles = 0] [output.csv = auto]\n\nArguments:\n  circ_type:\n";
     print_circuit_type_help(std::cerr, "    ");
-    std::cerr << "  On the GB300 path circ_type=1 (Haar brickwork) runs.\n"
+    std::cerr << "  On the GB300 path circ_type=1 (Haar brickwork), 2 (FermionRPPU) and 4 (qRPPU) run.\n"
               << "  all_cycles = 0 computes the original offset only.\n"
               << "  all_cycles = 1 computes N/4 cyclic offsets; e.g. N=8 gives [0,1]|[2,3]|[4,5]|[6,7] and "
                  "[1,2]|[3,4]|[5,6]|[7,0].\n"

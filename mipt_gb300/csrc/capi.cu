@@ -111,6 +111,29 @@ __global__ void k_fill_double(double *p, std::size_t n, double v)
         p[i] = v;
 }
 
+// The Jordan-Wigner closure string of the fermionic ring, on every state of a
+// batch: amplitudes whose site n-1 is occupied and whose sites 1..n-2 hold an
+// odd number of particles change sign (the reference brackets the closure bond
+// with this diagonal, cpp/include/mipt/cusv/gates.hpp:243-271). One thread per
+// amplitude with bit n-1 set.
+template <typename Real>
+__global__ void k_jw_closure(Cx<Real> *states, int n, int count)
+{
+    const std::uint64_t half = 1ull << (n - 1), mid = half - 2ull;
+    const std::uint64_t total = half * static_cast<std::uint64_t>(count);
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const std::uint64_t traj = i >> (n - 1), x = (i & (half - 1)) | half;
+        if (__popcll(x & mid) & 1)
+        {
+            Cx<Real> &a = states[(traj << n) | x];
+            a.re = -a.re;
+            a.im = -a.im;
+        }
+    }
+}
+
 __global__ void k_reset_layers(Collapse *col, LayerResult *res, std::size_t n)
 {
     for (std::size_t i = blockIdx.x * static_cast<std::size_t>(blockDim.x) + threadIdx.x; i < n;
@@ -971,6 +994,26 @@ int mipt_gb300_draw_haar_workspace(std::uint32_t seed, int n, int layers, double
     }
 }
 
+int mipt_gb300_draw_rppu(std::uint64_t seed, int n, int periods, double p, int chunk_bits, int split_last,
+                         int workspace, int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured,
+                         double *uniforms, int *n_uniforms)
+{
+    try
+    {
+        TrajectoryDraw d;
+        if (workspace)
+            draw_rppu_workspace(static_cast<std::uint32_t>(seed), n, 2 * periods, p, chunk_bits, split_last != 0,
+                                2 * periods + 1, d);
+        else
+            draw_rppu_trajectory(seed, n, periods, p, chunk_bits, split_last != 0, 2 * periods + 1, d);
+        return export_draw(d, gates_per_layer, bond_q, bond_u, measured, uniforms, n_uniforms);
+    }
+    catch (const std::exception &e)
+    {
+        return fail(MIPT_GB300_E_INVALID, e.what());
+    }
+}
+
 int mipt_gb300_draw_haar(std::uint64_t seed, int n, int periods, double p, int closed, int chunk_bits,
                          int *gates_per_layer, int *bond_q, double *bond_u, std::uint64_t *measured, double *uniforms,
                          int *n_uniforms)
@@ -1335,13 +1378,18 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     if ((cfg->observables & (MIPT_GB300_OBS_TMI_VN | MIPT_GB300_OBS_TMI_S2)) && (n % 4) != 0)
         return fail(MIPT_GB300_E_INVALID, "TMI needs n divisible by 4");
     if (cfg->observe_every < 0) return fail(MIPT_GB300_E_INVALID, "observe_every must be >= 0");
+    const bool rppu = cfg->circuit == 2 || cfg->circuit == 4;
+    if (cfg->circuit != 0 && cfg->circuit != 1 && !rppu)
+        return fail(MIPT_GB300_E_INVALID, "circuit must be 0/1 (Haar), 2 (FermionRPPU) or 4 (qRPPU)");
+    if (rppu && (lattice || !cfg->closed))
+        return fail(MIPT_GB300_E_INVALID, "RPPU circuits run on the closed 1-D ring");
     int dev = 0;
     if (cudaGetDeviceCount(&dev) != cudaSuccess || dev == 0) return fail(MIPT_GB300_E_NODEVICE, "no CUDA device");
 
     std::unique_ptr<mipt_gb300_batch> b(new mipt_gb300_batch());
     b->cfg = *cfg;
     b->capacity = capacity;
-    b->T = 2 * cfg->periods;
+    b->T = 2 * cfg->periods + (rppu ? 1 : 0);
     b->G = n / 2;
     b->kmax = cfg->tile_qubits > 0 ? std::min(cfg->tile_qubits, kMaxLocal) : chosen_tile(*cfg, capacity);
     b->cmin = kCoalesceQubits;
@@ -1505,13 +1553,18 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
             const std::uint64_t mask = d.measured[t];
             b->measured[slot] = mask;
             LayerMeas M{};
-            const int m = __builtin_popcountll(mask);
-            M.nchunks = (m + cb - 1) / cb;
+            // Sites in ascending chunks of cb; with split_last, site n-1 forms
+            // a final chunk of its own.
+            const std::uint64_t last = 1ull << (n - 1);
+            const bool alone = d.split_last && (mask & last);
+            const std::uint64_t plain = alone ? (mask & ~last) : mask;
+            const int m = __builtin_popcountll(plain);
+            M.nchunks = (m + cb - 1) / cb + (alone ? 1 : 0);
             if (M.nchunks > kMaxChunks) return fail(MIPT_GB300_E_INVALID, "too many measurement chunks per layer");
-            int site = 0, c = -1, in_chunk = cb;
+            int c = -1, in_chunk = cb;
             for (int q = 0; q < n; ++q)
             {
-                if (!((mask >> q) & 1ull)) continue;
+                if (!((plain >> q) & 1ull)) continue;
                 if (in_chunk == cb)
                 {
                     ++c;
@@ -1519,8 +1572,8 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
                 }
                 M.chunk[c] |= 1ull << q;
                 ++in_chunk;
-                ++site;
             }
+            if (alone) M.chunk[++c] = last;
             for (int cc = 0; cc < M.nchunks; ++cc) M.uniform[cc] = d.uniforms[d.uniform_offset[t] + cc];
             hm[slot] = M;
             hf[slot] = forced ? forced[slot] : 0ull;
@@ -1555,6 +1608,9 @@ int mipt_gb300_batch_prepare_haar(mipt_gb300_batch *b, const std::uint64_t *seed
         if (b->lattice)
             draw_haar_lattice_batch(seeds, p, count, b->cfg.lattice_x, b->cfg.lattice_y, b->T, b->cfg.chunk_bits,
                                     draws, b->cfg.host_threads);
+        else if (b->cfg.circuit == 2 || b->cfg.circuit == 4)
+            draw_rppu_batch(seeds, p, count, b->cfg.n_qubits, b->cfg.periods, b->cfg.chunk_bits,
+                            b->cfg.split_last != 0, b->T, draws, b->cfg.host_threads);
         else
             draw_haar_batch(seeds, p, count, b->cfg.n_qubits, b->cfg.periods, b->cfg.closed != 0,
                             b->cfg.chunk_bits, draws, b->cfg.host_threads);
@@ -1575,8 +1631,12 @@ int mipt_gb300_batch_prepare_haar_workspace(mipt_gb300_batch *b, const std::uint
     std::vector<TrajectoryDraw> draws;
     try
     {
-        draw_haar_workspace_batch(seeds, p, count, b->cfg.n_qubits, b->T, b->cfg.closed != 0, b->cfg.chunk_bits,
-                                  draws, b->cfg.host_threads);
+        if (b->cfg.circuit == 2 || b->cfg.circuit == 4)
+            draw_rppu_workspace_batch(seeds, p, count, b->cfg.n_qubits, 2 * b->cfg.periods, b->cfg.chunk_bits,
+                                      b->cfg.split_last != 0, b->T, draws, b->cfg.host_threads);
+        else
+            draw_haar_workspace_batch(seeds, p, count, b->cfg.n_qubits, b->T, b->cfg.closed != 0,
+                                      b->cfg.chunk_bits, draws, b->cfg.host_threads);
     }
     catch (const std::exception &e)
     {
@@ -1801,6 +1861,17 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     {
         const auto &plan = b->plan[t % b->ncolour];
         const bool fuse = b->any_meas[t] && b->fusable[t];
+        // Fermionic closure: the odd layer's gates run between two JW strings;
+        // every other odd-layer bond lies inside the string and preserves its
+        // parity, so the bracket covers the whole layer.
+        const bool jw = b->cfg.circuit == 2 && (t & 1);
+        auto jw_closure = [&]() {
+            Mark m(b, K_OTHER, s);
+            k_jw_closure<Real><<<std::max(1, std::min(4 * 152, static_cast<int>(((b->dim / 2) * count + 255) / 256))),
+                                 256, 0, s>>>(states, n, count);
+            ++L;
+        };
+        if (jw) jw_closure();
         for (std::size_t pi = 0; pi < plan.size(); ++pi)
         {
             const Collapse *cin = (pi == 0 && t > 0) ? col + (t - 1) : nullptr;
@@ -1811,6 +1882,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                                       b->err.as<int>(), s));
             ++L;
         }
+        if (jw) jw_closure();
         if (b->any_meas[t])
         {
             for (int ci = 0; ci < b->max_chunks[t]; ++ci)

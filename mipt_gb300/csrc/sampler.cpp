@@ -274,6 +274,199 @@ int draw_initial_state(std::uint64_t seed, int n, int kind, bool fixed_parity, s
 template int draw_initial_state<float>(std::uint64_t, int, int, bool, std::complex<float> *);
 template int draw_initial_state<double>(std::uint64_t, int, int, bool, std::complex<double> *);
 
+namespace
+{
+// haar_unitary_2: Gram-Schmidt of a complex Gaussian 2x2 (row-major), each
+// entry's imaginary draw first as the g++-built reference evaluates
+// std::complex<double>(normal(rng), normal(rng)).
+void haar_u2(std::mt19937 &rng, C *q)
+{
+    std::normal_distribution<double> normal(0.0, 1.0);
+    C z[4];
+    for (auto &v : z)
+    {
+        const double im = normal(rng);
+        const double re = normal(rng);
+        v = C(re, im);
+    }
+    C z00 = z[0], z10 = z[2];
+    const C z01 = z[1], z11 = z[3];
+    double n0 = std::sqrt(std::norm(z00) + std::norm(z10));
+    if (n0 == 0.0)
+    {
+        z00 = 1.0;
+        z10 = 0.0;
+        n0 = 1.0;
+    }
+    const C q00 = z00 / n0, q10 = z10 / n0;
+    const C r01 = std::conj(q00) * z01 + std::conj(q10) * z11;
+    C u01 = z01 - q00 * r01, u11 = z11 - q10 * r01;
+    double n1 = std::sqrt(std::norm(u01) + std::norm(u11));
+    if (n1 < 1e-15)
+    {
+        u01 = -std::conj(q10);
+        u11 = std::conj(q00);
+        n1 = std::sqrt(std::norm(u01) + std::norm(u11));
+    }
+    q[0] = q00;
+    q[1] = u01 / n1;
+    q[2] = q10;
+    q[3] = u11 / n1;
+}
+
+// One parity-preserving bond (even block drawn first), as a row-major 4x4
+// with bit 0 = the gate's first qubit; `swapped` stores it for the reversed
+// qubit order.
+void parity_gate(std::mt19937 &rng, C *m, bool swapped)
+{
+    C e[4], o[4], g[16] = {};
+    haar_u2(rng, e);
+    haar_u2(rng, o);
+    g[0] = e[0];
+    g[3] = e[1];
+    g[12] = e[2];
+    g[15] = e[3];
+    g[10] = o[0];
+    g[9] = o[1];
+    g[6] = o[2];
+    g[5] = o[3];
+    auto sw = [swapped](int i) { return swapped ? ((i & 1) << 1) | ((i >> 1) & 1) : i; };
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) m[4 * sw(r) + sw(c)] = g[4 * r + c];
+}
+
+// Layer t of `out` (odd or even) from the layer stream, then its flags and
+// measurement uniforms.
+void rppu_layer(std::mt19937 &gates_rng, std::mt19937 &meas_rng, int n, bool odd, double p, int chunk_bits,
+                bool split_last, int t, TrajectoryDraw &out)
+{
+    const int mb = n / 2;
+    C *u = &out.bond_u[static_cast<std::size_t>(t) * mb * 16];
+    int *q = &out.bond_q[static_cast<std::size_t>(t) * mb * 2];
+    std::bernoulli_distribution flag(p);
+    if (!odd)
+    {
+        for (int j = 0; j < mb; ++j)
+        {
+            parity_gate(gates_rng, u + 16 * j, false);
+            q[2 * j] = 2 * j;
+            q[2 * j + 1] = 2 * j + 1;
+        }
+    }
+    else
+    {
+        // Closure first in the draw, last in the plan's bond order.
+        parity_gate(gates_rng, u + 16 * (mb - 1), true);
+        q[2 * (mb - 1)] = n - 1;
+        q[2 * (mb - 1) + 1] = 0;
+        for (int j = 0; j + 1 < mb; ++j)
+        {
+            parity_gate(gates_rng, u + 16 * j, false);
+            q[2 * j] = 2 * j + 1;
+            q[2 * j + 1] = 2 * j + 2;
+        }
+    }
+    out.bond_count[t] = mb;
+    std::uint64_t mask = 0;
+    if (p >= 1.0)
+        mask = (1ull << n) - 1ull;
+    else if (p > 0.0)
+        for (int s = 0; s < n; ++s)
+            if (flag(gates_rng)) mask |= 1ull << s;
+    out.measured[t] = mask;
+    out.uniform_offset[t] = static_cast<int>(out.uniforms.size());
+    std::uniform_real_distribution<double> unif(0.0, 1.0);
+    const bool last_alone = split_last && ((mask >> (n - 1)) & 1ull);
+    const int plain = __builtin_popcountll(mask) - (last_alone ? 1 : 0);
+    for (int c = 0; c < plain; c += chunk_bits) out.uniforms.push_back(unif(meas_rng));
+    if (last_alone) out.uniforms.push_back(unif(meas_rng));
+}
+
+void rppu_init(TrajectoryDraw &out, int n, int layers_out, bool split_last)
+{
+    if (n < 4 || n % 2 != 0 || n > 62) throw std::invalid_argument("RPPU brickwork needs even 4 <= n <= 62");
+    const int mb = n / 2;
+    out.n = n;
+    out.layers = layers_out;
+    out.max_bonds = mb;
+    out.split_last = split_last;
+    out.bond_count.assign(layers_out, 0);
+    out.bond_q.assign(static_cast<std::size_t>(layers_out) * mb * 2, 0);
+    out.bond_u.assign(static_cast<std::size_t>(layers_out) * mb * 16, C(0.0, 0.0));
+    out.measured.assign(layers_out, 0);
+    out.uniforms.clear();
+    out.uniform_offset.assign(layers_out + 1, 0);
+}
+
+// Identity even layer (no gates drawn, nothing measured) in slot t.
+void identity_layer(TrajectoryDraw &out, int t)
+{
+    const int mb = out.max_bonds;
+    for (int j = 0; j < mb; ++j)
+    {
+        C *u = &out.bond_u[(static_cast<std::size_t>(t) * mb + j) * 16];
+        for (int e = 0; e < 16; ++e) u[e] = (e % 5 == 0) ? C(1.0, 0.0) : C(0.0, 0.0);
+        out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2] = 2 * j;
+        out.bond_q[(static_cast<std::size_t>(t) * mb + j) * 2 + 1] = 2 * j + 1;
+    }
+    out.bond_count[t] = mb;
+    out.measured[t] = 0;
+    out.uniform_offset[t] = static_cast<int>(out.uniforms.size());
+}
+} // namespace
+
+void draw_rppu_trajectory(std::uint64_t seed, int n, int periods, double p, int chunk_bits, bool split_last,
+                          int layers_out, TrajectoryDraw &out)
+{
+    if (layers_out < 2 * periods + 1) throw std::invalid_argument("RPPU draw needs 2*periods + 1 layer slots");
+    if (chunk_bits < 1) throw std::invalid_argument("chunk_bits must be positive");
+    std::mt19937 gates_rng, meas_rng;
+    seed_mt(gates_rng, seed);
+    seed_mt(meas_rng, splitmix64(seed ^ 0xa0761d0dull));
+    rppu_init(out, n, layers_out, split_last);
+    std::bernoulli_distribution extra_even(0.5);
+    const bool extra = extra_even(gates_rng);
+    int t = 0;
+    for (; t < 2 * periods; ++t) rppu_layer(gates_rng, meas_rng, n, (t & 1) != 0, p, chunk_bits, split_last, t, out);
+    if (extra) rppu_layer(gates_rng, meas_rng, n, false, p, chunk_bits, split_last, t++, out);
+    for (; t < layers_out; ++t) identity_layer(out, t);
+    out.uniform_offset[layers_out] = static_cast<int>(out.uniforms.size());
+}
+
+void draw_rppu_workspace(std::uint32_t seed, int n, int layers, double p, int chunk_bits, bool split_last,
+                         int layers_out, TrajectoryDraw &out)
+{
+    if (layers_out < layers) throw std::invalid_argument("too few layer slots");
+    if (chunk_bits < 1) throw std::invalid_argument("chunk_bits must be positive");
+    std::mt19937 gates_rng(seed), meas_rng(seed ^ 0x9e3779b9u);
+    rppu_init(out, n, layers_out, split_last);
+    int t = 0;
+    for (; t < layers; ++t) rppu_layer(gates_rng, meas_rng, n, (t & 1) != 0, p, chunk_bits, split_last, t, out);
+    for (; t < layers_out; ++t) identity_layer(out, t);
+    out.uniform_offset[layers_out] = static_cast<int>(out.uniforms.size());
+}
+
+void draw_rppu_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, int chunk_bits,
+                     bool split_last, int layers_out, std::vector<TrajectoryDraw> &out, int threads)
+{
+    out.resize(count);
+    parallel_for(
+        count, threads,
+        [&](int i) { draw_rppu_trajectory(seeds[i], n, periods, p[i], chunk_bits, split_last, layers_out, out[i]); },
+        "RPPU trajectory draw failed");
+}
+
+void draw_rppu_workspace_batch(const std::uint32_t *seeds, const double *p, int count, int n, int layers,
+                               int chunk_bits, bool split_last, int layers_out, std::vector<TrajectoryDraw> &out,
+                               int threads)
+{
+    out.resize(count);
+    parallel_for(
+        count, threads,
+        [&](int i) { draw_rppu_workspace(seeds[i], n, layers, p[i], chunk_bits, split_last, layers_out, out[i]); },
+        "RPPU workspace draw failed");
+}
+
 std::vector<std::pair<int, int>> lattice_bonds(int X, int Y, int colour)
 {
     if (X < 2 || Y < 1 || colour < 0 || colour > 3) throw std::invalid_argument("bad lattice or colour");

@@ -38,7 +38,33 @@ struct TrajectoryDraw
     std::vector<std::uint64_t> measured;
     std::vector<double> uniforms;
     std::vector<int> uniform_offset; // first uniform of layer t
+    // Site n-1 is measured as its own chunk, after the others (the reference's
+    // parity-sector engine measures it as the parity of the encoded index).
+    bool split_last = false;
 };
+
+// Random parity-preserving (RPPU / qRPPU) brickwork, 1-D closed ring
+// (cpp/include/mipt/circuits/rppu_layer.hpp:51-285). Each bond is
+// U_even (+) U_odd, two haar_unitary_2 draws (even block on |00>,|11>, odd
+// block on |10>,|01>). The odd layer's closure gate is drawn first; it acts on
+// (0, n-1) and is stored in the plan's orientation (n-1, 0) as the last bond.
+// For the fermionic gate set the closure carries the Jordan-Wigner string on
+// sites 1..n-2 (the batch brackets odd layers with that diagonal; the
+// reference's FSWAP-chain form of the closure is the same operator).
+//   draw_rppu_trajectory: Circuit1D streams, 2*periods layers plus, with
+//   probability 1/2 (drawn first), one extra even layer; `layers_out` layers
+//   are written (>= 2*periods + 1), a missing extra layer as identity gates
+//   and no measurements. split_last: the encoded-measurement chunking.
+//   draw_rppu_workspace: the probed workspace's streams, `layers` layers.
+void draw_rppu_trajectory(std::uint64_t seed, int n, int periods, double p, int chunk_bits, bool split_last,
+                          int layers_out, TrajectoryDraw &out);
+void draw_rppu_workspace(std::uint32_t seed, int n, int layers, double p, int chunk_bits, bool split_last,
+                         int layers_out, TrajectoryDraw &out);
+void draw_rppu_batch(const std::uint64_t *seeds, const double *p, int count, int n, int periods, int chunk_bits,
+                     bool split_last, int layers_out, std::vector<TrajectoryDraw> &out, int threads);
+void draw_rppu_workspace_batch(const std::uint32_t *seeds, const double *p, int count, int n, int layers,
+                               int chunk_bits, bool split_last, int layers_out, std::vector<TrajectoryDraw> &out,
+                               int threads);
 
 // Draws a 1-D Haar brickwork trajectory (2*periods layers; odd layers close
 // the ring with bond (n-1, 0) when `closed`).

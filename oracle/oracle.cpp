@@ -36,6 +36,12 @@
 //     workspace layer/measurement streams       cpp/include/mipt/probed.hpp:103-108
 //     random product / Haar initial states       cpp/include/mipt/free_energy.hpp:125-222
 //     half-chain S1 schedule                     cpp/include/mipt/free_energy_resume.hpp:150-166
+//   * RPPU / qRPPU brickwork                     cpp/include/mipt/circuits/rppu_layer.hpp:51-285
+//     (haar_unitary_2 blocks, even block first; random extra even layer drawn
+//     first; closure gate first in the odd layer: FSWAP chain, JW-string or
+//     direct qubit form), ops as cpp/include/mipt/cusv/gates.hpp:229-281
+//     builds them; encoded measurement (site n-1 as its own final chunk)
+//                                                cpp/include/mipt/cusv/engine.hpp:364-458
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -451,11 +457,11 @@ double entropy_from_rdm(const cd *rho, int d, int order)
     return snap(s);
 }
 
-double subsystem_entropy(const cd *psi, int n, const std::vector<int> &kept, int order)
+double subsystem_entropy(const cd *psi, int n, const std::vector<int> &kept, int order, bool fermion = false)
 {
     const int d = 1 << kept.size();
     std::vector<cd> rho(static_cast<std::size_t>(d) * d);
-    rdm(psi, n, kept.data(), static_cast<int>(kept.size()), false, rho.data());
+    rdm(psi, n, kept.data(), static_cast<int>(kept.size()), fermion, rho.data());
     return entropy_from_rdm(rho.data(), d, order);
 }
 
@@ -1293,9 +1299,21 @@ int orc_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits,
 // 28n timesteps (4n equilibration + 24n production), each one layer and its
 // joint measurement. surprisal[T], measured[T] (site counts), s_half[T+1]
 // (half-chain S1 in bits on the sampled timesteps, NaN elsewhere).
+int orc_fe_trajectory_circuit(std::uint64_t trajectory_seed, int n, double p, int circuit, int init_kind,
+                              int fp32_init, int chunk_bits, int entropy_max_t, int entropy_stride, double *surprisal,
+                              int *measured, double *s_half, int *parity);
+
 int orc_fe_trajectory(std::uint64_t trajectory_seed, int n, double p, int init_kind, int fp32_init,
                       int chunk_bits, int entropy_max_t, int entropy_stride, double *surprisal, int *measured,
                       double *s_half, int *parity)
+{
+    return orc_fe_trajectory_circuit(trajectory_seed, n, p, 1, init_kind, fp32_init, chunk_bits, entropy_max_t,
+                                     entropy_stride, surprisal, measured, s_half, parity);
+}
+
+int orc_fe_haar_trajectory(std::uint64_t trajectory_seed, int n, double p, int init_kind, int fp32_init,
+                           int chunk_bits, int entropy_max_t, int entropy_stride, double *surprisal, int *measured,
+                           double *s_half, int *parity)
 {
     try
     {
@@ -1368,6 +1386,295 @@ int orc_fe_batch(std::uint64_t master, int first, int count, int n, double p, in
         f_total[i] = tot;
     }
     return failed;
+}
+
+namespace rp
+{
+// One op of an RPPU layer in application order: kind 0 matrix on (q0, q1)
+// (bit 0 = q0), 1 FSWAP, 2 JW string (sign where bit q1 is set and the
+// sites strictly between q0 and q1 hold odd parity).
+struct Op
+{
+    int kind, q0, q1;
+    std::array<cd, 16> m;
+};
+
+void u2(std::mt19937 &rng, cd *q)
+{
+    std::normal_distribution<double> normal(0.0, 1.0);
+    cd z[4];
+    for (int i = 0; i < 4; ++i)
+    {
+        // cd(normal(rng), normal(rng)) in the reference: imaginary draw first.
+        const double im = normal(rng);
+        const double re = normal(rng);
+        z[i] = cd(re, im);
+    }
+    cd a = z[0], c = z[2];
+    double na = std::sqrt(std::norm(a) + std::norm(c));
+    if (na == 0.0)
+    {
+        a = 1.0;
+        c = 0.0;
+        na = 1.0;
+    }
+    const cd q00 = a / na, q10 = c / na;
+    const cd r = std::conj(q00) * z[1] + std::conj(q10) * z[3];
+    cd b0 = z[1] - q00 * r, b1 = z[3] - q10 * r;
+    double nb = std::sqrt(std::norm(b0) + std::norm(b1));
+    if (nb < 1e-15)
+    {
+        b0 = -std::conj(q10);
+        b1 = std::conj(q00);
+        nb = std::sqrt(std::norm(b0) + std::norm(b1));
+    }
+    q[0] = q00;
+    q[1] = b0 / nb;
+    q[2] = q10;
+    q[3] = b1 / nb;
+}
+
+Op gate(std::mt19937 &rng, int q0, int q1)
+{
+    cd e[4], o[4];
+    u2(rng, e);
+    u2(rng, o);
+    Op g{0, q0, q1, {}};
+    // Even block on basis (0, 3), odd block on basis (2, 1).
+    g.m[0] = e[0];
+    g.m[3] = e[1];
+    g.m[12] = e[2];
+    g.m[15] = e[3];
+    g.m[10] = o[0];
+    g.m[9] = o[1];
+    g.m[6] = o[2];
+    g.m[5] = o[3];
+    return g;
+}
+
+Op fswap(int q0, int q1)
+{
+    Op g{1, q0, q1, {}};
+    g.m[0] = 1.0;
+    g.m[6] = 1.0;
+    g.m[9] = 1.0;
+    g.m[15] = -1.0;
+    return g;
+}
+
+struct Layer
+{
+    std::vector<Op> ops;
+    std::vector<int> sites;
+};
+
+// boundary: 0 FSWAP chain, 1 JW string, 2 direct qubit gate.
+void draw_layer(Layer &L, int n, bool odd, double p, int boundary, std::mt19937 &rng)
+{
+    std::bernoulli_distribution flag(p);
+    L.ops.clear();
+    L.sites.clear();
+    if (!odd)
+        for (int q = 0; q < n; q += 2) L.ops.push_back(gate(rng, q, q + 1));
+    else
+    {
+        if (boundary == 1)
+        {
+            Op s{2, 0, n - 1, {}};
+            L.ops.push_back(s);
+            L.ops.push_back(gate(rng, 0, n - 1));
+            L.ops.push_back(s);
+        }
+        else if (boundary == 2)
+            L.ops.push_back(gate(rng, 0, n - 1));
+        else
+        {
+            for (int k = n - 2; k > 0; --k) L.ops.push_back(fswap(k, k + 1));
+            L.ops.push_back(gate(rng, 0, 1));
+            for (int k = 1; k < n - 1; ++k) L.ops.push_back(fswap(k, k + 1));
+        }
+        for (int q = 1; q < n - 1; q += 2) L.ops.push_back(gate(rng, q, q + 1));
+    }
+    if (p >= 1.0)
+        for (int s = 0; s < n; ++s) L.sites.push_back(s);
+    else if (p > 0.0)
+        for (int s = 0; s < n; ++s)
+            if (flag(rng)) L.sites.push_back(s);
+}
+
+void apply(cd *psi, int n, const Op &op)
+{
+    if (op.kind == 2)
+    {
+        std::uint64_t mid = 0;
+        for (int k = std::min(op.q0, op.q1) + 1; k < std::max(op.q0, op.q1); ++k) mid |= 1ull << k;
+        const std::uint64_t ctl = 1ull << std::max(op.q0, op.q1);
+        for (std::uint64_t x = 0; x < (1ull << n); ++x)
+            if ((x & ctl) && (__builtin_popcountll(x & mid) & 1)) psi[x] = -psi[x];
+        return;
+    }
+    apply_bond(psi, n, op.q0, op.q1, op.m.data());
+}
+} // namespace rp
+
+// RPPU draw in the reference's op order: for each layer, ops[] (kind, q0,
+// q1, 4x4 re/im) and measured sites. Circuit1D streams (workspace = 0: the
+// random extra even layer drawn first) or the probed workspace's (workspace
+// = 1, seed's low 32 bits, `periods` meaning the layer count). Returns the
+// layer count; op_count[layer], ops flattened as [kind, q0, q1] in op_meta
+// and 32 doubles each in op_m; sites_per_layer/sites as orc_haar_draw.
+int orc_rppu_draw(std::uint64_t seed, int n, int periods, double p, int boundary, int workspace, int *op_count,
+                  int *op_meta, double *op_m, int *sites_per_layer, int *sites)
+{
+    try
+    {
+        std::mt19937 gates, meas;
+        int T;
+        bool extra = false;
+        if (workspace)
+        {
+            gates.seed(static_cast<std::uint32_t>(seed));
+            T = periods;
+        }
+        else
+        {
+            seed_pair(seed, gates, meas);
+            std::bernoulli_distribution coin(0.5);
+            extra = coin(gates);
+            T = 2 * periods + (extra ? 1 : 0);
+        }
+        int k = 0;
+        for (int t = 0; t < T; ++t)
+        {
+            rp::Layer L;
+            const bool odd = workspace ? (t % 2) != 0 : (t < 2 * periods && (t & 1));
+            rp::draw_layer(L, n, odd, p, boundary, gates);
+            op_count[t] = static_cast<int>(L.ops.size());
+            for (const auto &op : L.ops)
+            {
+                op_meta[3 * k] = op.kind;
+                op_meta[3 * k + 1] = op.q0;
+                op_meta[3 * k + 2] = op.q1;
+                for (int e = 0; e < 16; ++e)
+                {
+                    op_m[32 * k + 2 * e] = op.m[e].real();
+                    op_m[32 * k + 2 * e + 1] = op.m[e].imag();
+                }
+                ++k;
+            }
+            sites_per_layer[t] = static_cast<int>(L.sites.size());
+            for (std::size_t j = 0; j < L.sites.size(); ++j) sites[static_cast<std::size_t>(t) * n + j] = L.sites[j];
+        }
+        return T;
+    }
+    catch (...)
+    {
+        return -1;
+    }
+}
+
+// One RPPU / qRPPU trajectory on the Circuit1D streams from |0...0>:
+// surprisal[layer] (-ln P), outcomes as orc_run_haar_trajectory's (in the
+// order measured: with `encoded`, site n-1 last), the final state, and the
+// layer count (2*periods or 2*periods + 1) returned.
+int orc_run_rppu_trajectory(std::uint64_t seed, int n, int periods, double p, int boundary, int encoded,
+                            int chunk_bits, double *surprisal, int *outcomes, double *final_psi_ri)
+{
+    try
+    {
+        std::mt19937 gates, meas;
+        seed_pair(seed, gates, meas);
+        std::bernoulli_distribution coin(0.5);
+        const bool extra = coin(gates);
+        const int T = 2 * periods + (extra ? 1 : 0);
+        const std::uint64_t dim = 1ull << n;
+        std::vector<cd> psi(dim, cd(0.0, 0.0));
+        psi[0] = 1.0;
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        for (int t = 0; t < T; ++t)
+        {
+            rp::Layer L;
+            rp::draw_layer(L, n, t < 2 * periods && (t & 1), p, boundary, gates);
+            for (const auto &op : L.ops) rp::apply(psi.data(), n, op);
+            // Encoded measurement: sites below n-1 in chunks, then n-1 alone.
+            std::vector<int> plain, last;
+            for (int s : L.sites) (encoded && s == n - 1 ? last : plain).push_back(s);
+            std::vector<double> us;
+            for (std::size_t j = 0; j < plain.size(); j += chunk_bits) us.push_back(unif(meas));
+            if (!last.empty()) us.push_back(unif(meas));
+            std::vector<int> oc(L.sites.size(), 0);
+            int used = 0;
+            double sp = measure_layer(psi.data(), n, plain, chunk_bits, us.data(), used, nullptr, oc.data());
+            if (!last.empty()) sp += measure_layer(psi.data(), n, last, 1, us.data(), used, nullptr, oc.data() + plain.size());
+            surprisal[t] = sp;
+            if (outcomes)
+            {
+                for (int s = 0; s < n; ++s) outcomes[static_cast<std::size_t>(t) * n + s] = -1;
+                for (std::size_t s = 0; s < oc.size(); ++s) outcomes[static_cast<std::size_t>(t) * n + s] = oc[s];
+            }
+        }
+        if (final_psi_ri) std::memcpy(final_psi_ri, psi.data(), dim * sizeof(cd));
+        return T;
+    }
+    catch (...)
+    {
+        return -1;
+    }
+}
+
+// The free-energy trajectory for any gate set on this path: circuit 1 Haar
+// (orc_fe_haar_trajectory), 2 FermionRPPU (JW closure, fermionic S1), 4
+// qRPPU; the parity-preserving sets start from a fixed-parity initial state
+// (cpp/include/mipt/free_energy.hpp:224-248) and draw their layers with
+// fill_rppu_layer on the workspace stream (cpp/include/mipt/probed.hpp:208-224).
+int orc_fe_trajectory_circuit(std::uint64_t trajectory_seed, int n, double p, int circuit, int init_kind,
+                              int fp32_init, int chunk_bits, int entropy_max_t, int entropy_stride, double *surprisal,
+                              int *measured, double *s_half, int *parity)
+{
+    if (circuit == 1 || circuit == 0)
+        return orc_fe_haar_trajectory(trajectory_seed, n, p, init_kind, fp32_init, chunk_bits, entropy_max_t,
+                                      entropy_stride, surprisal, measured, s_half, parity);
+    try
+    {
+        const int T = 28 * n;
+        const bool fermion = circuit == 2;
+        const std::uint32_t ws = static_cast<std::uint32_t>(mix64(trajectory_seed ^ 0x4349524355495455ull));
+        const std::uint64_t init_seed = mix64(trajectory_seed ^ 0x494e495449414c53ull);
+        const std::uint64_t dim = 1ull << n;
+        std::vector<double> ri(2 * dim);
+        if (orc_fe_initial_state(init_seed, n, init_kind, 1, fp32_init, ri.data(), parity)) return 1;
+        std::vector<cd> psi(dim);
+        for (std::uint64_t x = 0; x < dim; ++x) psi[x] = cd(ri[2 * x], ri[2 * x + 1]);
+        std::mt19937 gates(ws), meas(ws ^ 0x9e3779b9u);
+        std::uniform_real_distribution<double> unif(0.0, 1.0);
+        auto sampled = [&](int t) {
+            if (entropy_max_t < 0) return false;
+            if (t == 0) return true;
+            if (t > entropy_max_t) return false;
+            return t % entropy_stride == 0 || t == entropy_max_t;
+        };
+        std::vector<rp::Layer> layers(T);
+        for (int t = 0; t < T; ++t) rp::draw_layer(layers[t], n, (t % 2) != 0, p, fermion ? 1 : 2, gates);
+        for (int t = 0; t <= T; ++t) s_half[t] = std::nan("");
+        if (sampled(0)) s_half[0] = subsystem_entropy(psi.data(), n, half_chain(n), 1, fermion);
+        for (int t = 0; t < T; ++t)
+        {
+            const rp::Layer &L = layers[t];
+            for (const auto &op : L.ops) rp::apply(psi.data(), n, op);
+            std::vector<double> us;
+            for (std::size_t k = 0; k < L.sites.size(); k += chunk_bits) us.push_back(unif(meas));
+            std::vector<int> oc(L.sites.size(), 0);
+            int used = 0;
+            surprisal[t] = measure_layer(psi.data(), n, L.sites, chunk_bits, us.data(), used, nullptr, oc.data());
+            measured[t] = static_cast<int>(L.sites.size());
+            if (sampled(t + 1)) s_half[t + 1] = subsystem_entropy(psi.data(), n, half_chain(n), 1, fermion);
+        }
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
 }
 
 int orc_max_threads()

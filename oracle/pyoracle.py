@@ -50,6 +50,9 @@ def lib():
     L.orc_fe_draw.argtypes = [ctypes.c_uint32, ci, ci, cd, ci] + [vp] * 7
     L.orc_fe_trajectory.argtypes = [u64, ci, cd, ci, ci, ci, ci, ci, vp, vp, vp, vp]
     L.orc_fe_batch.argtypes = [u64, ci, ci, ci, cd, ci, ci, vp, ci]
+    L.orc_rppu_draw.argtypes = [u64, ci, ci, cd, ci, ci] + [vp] * 5
+    L.orc_fe_trajectory_circuit.argtypes = [u64, ci, cd, ci, ci, ci, ci, ci, ci, vp, vp, vp, vp]
+    L.orc_run_rppu_trajectory.argtypes = [u64, ci, ci, cd, ci, ci, ci, vp, vp, vp]
     _lib = L
     return L
 
@@ -326,9 +329,10 @@ def fe_draw(seed32, n, layers, p, chunk_bits=16):
 
 
 def fe_trajectory(trajectory_seed, n, p, init_kind, fp32_init=False, chunk_bits=16, entropy_max_t=None,
-                  entropy_stride=1):
-    """One free-energy trajectory (28n timesteps): surprisal[T], measured counts[T],
-    half-chain S1 bits [T+1] (NaN where not sampled), parity sector."""
+                  entropy_stride=1, circuit=1):
+    """One free-energy trajectory (28n timesteps) of gate set `circuit` (1 Haar,
+    2 FermionRPPU, 4 qRPPU): surprisal[T], measured counts[T], half-chain S1
+    bits [T+1] (NaN where not sampled), parity sector."""
     T = 28 * n
     if entropy_max_t is None:
         entropy_max_t = 2 * n
@@ -336,8 +340,8 @@ def fe_trajectory(trajectory_seed, n, p, init_kind, fp32_init=False, chunk_bits=
     mc = np.zeros(T, np.int32)
     sh = np.zeros(T + 1)
     par = np.zeros(1, np.int32)
-    if lib().orc_fe_trajectory(trajectory_seed, n, p, init_kind, int(fp32_init), chunk_bits, entropy_max_t,
-                               entropy_stride, _p(sp), _p(mc), _p(sh), _p(par)):
+    if lib().orc_fe_trajectory_circuit(trajectory_seed, n, p, circuit, init_kind, int(fp32_init), chunk_bits,
+                                       entropy_max_t, entropy_stride, _p(sp), _p(mc), _p(sh), _p(par)):
         raise RuntimeError("orc_fe_trajectory failed")
     return dict(surprisal=sp, measured=mc, s_half=sh, parity=int(par[0]))
 
@@ -348,3 +352,37 @@ def fe_batch(master, first, count, n, p, init_kind, chunk_bits=16, threads=0):
     if lib().orc_fe_batch(master, first, count, n, p, init_kind, chunk_bits, _p(out), threads):
         raise RuntimeError("orc_fe_batch failed")
     return out
+
+
+# ------------------------------------------------------------ RPPU / qRPPU
+RPPU_FSWAP, RPPU_JW, RPPU_QUBIT = 0, 1, 2
+
+
+def rppu_draw(seed, n, periods, p, boundary, workspace=False):
+    """Ops of each layer in application order: (kinds[k], q0[k], q1[k],
+    matrices[k] 4x4 complex), ops per layer, sites per layer, sites."""
+    T = periods if workspace else 2 * periods + 1
+    oc = np.zeros(T, np.int32)
+    meta = np.zeros((T * 4 * n, 3), np.int32)
+    m = np.zeros((T * 4 * n, 32))
+    spl = np.zeros(T, np.int32)
+    sites = np.full((T, n), -1, np.int32)
+    t = lib().orc_rppu_draw(seed, n, periods, p, boundary, int(workspace), _p(oc), _p(meta), _p(m), _p(spl),
+                            _p(sites))
+    if t < 0:
+        raise RuntimeError("orc_rppu_draw failed")
+    k = int(oc[:t].sum())
+    return dict(layers=t, ops_per_layer=oc[:t], meta=meta[:k], m=m[:k], sites_per_layer=spl[:t], sites=sites[:t])
+
+
+def run_rppu_trajectory(seed, n, periods, p, boundary, encoded=True, chunk_bits=16):
+    """One RPPU trajectory from |0...0> on the Circuit1D streams."""
+    T = 2 * periods + 1
+    sp = np.zeros(T)
+    oc = np.full((T, n), -1, np.int32)
+    psi = np.zeros(1 << n, np.complex128)
+    t = lib().orc_run_rppu_trajectory(seed, n, periods, p, boundary, int(encoded), chunk_bits, _p(sp), _p(oc),
+                                      _p(psi))
+    if t < 0:
+        raise RuntimeError("orc_run_rppu_trajectory failed")
+    return dict(layers=t, surprisal=sp[:t], outcomes=oc[:t], psi=psi)

@@ -22,7 +22,11 @@
 //                                               cpp/include/mipt/free_energy.hpp:125-222
 //   CircuitWorkspace1D::seed (restated below: the class itself needs a live
 //   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
+//   build_rppu_layers_with_boundary / fill_rppu_layer, build_rppu_layer_ops
+//                                               cpp/include/mipt/circuits/rppu_layer.hpp:167-285,
+//                                               cpp/include/mipt/cusv/gates.hpp:219-281
 #include "mipt/circuits/haar.hpp"
+#include "mipt/circuits/rppu_layer.hpp"
 #include "mipt/free_energy.hpp"
 #include "mipt/cusv/gates.hpp"
 #include "mipt/free_energy_measure.hpp"
@@ -282,6 +286,73 @@ int ref_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits,
     catch (...)
     {
         return 1;
+    }
+}
+
+// RPPU layers as the reference's engine receives them: per layer the ops of
+// build_rppu_layer_ops in order -- op_meta [kind, q0, q1] with kind 0 a 4x4
+// matrix on (q0, q1) (bit 0 = q0) and kind 2 a JW string (q0 = the site below
+// the string, q1 = its control) -- and the measured sites. boundary: 0 FSWAP
+// chain, 1 JW string, 2 direct qubit gate (qRPPU). workspace = 0: Circuit1D
+// streams and build_rppu_layers_with_boundary (periods, random extra layer);
+// workspace = 1: fill_rppu_layer per timestep on mt19937(seed), `periods`
+// meaning the layer count. Returns the layer count.
+int ref_rppu_draw(std::uint64_t seed, int n, int periods, double p, int boundary, int workspace, int *op_count,
+                  int *op_meta, double *op_m, int *sites_per_layer, int *sites)
+{
+    try
+    {
+        const auto mode = static_cast<mipt::RppuBoundaryMode>(boundary);
+        std::vector<mipt::RppuLayer> layers;
+        if (workspace)
+        {
+            std::mt19937 rng;
+            rng.seed(static_cast<std::uint32_t>(seed));
+            layers.resize(static_cast<std::size_t>(periods));
+            for (int t = 0; t < periods; ++t) mipt::fill_rppu_layer(layers[t], n, (t % 2) != 0, p, true, rng, mode);
+        }
+        else
+        {
+            std::mt19937 layer_rng, measure_rng;
+            seed_streams(seed, layer_rng, measure_rng);
+            mipt::build_rppu_layers_with_boundary(layers, n, periods, p, true, layer_rng, mode);
+        }
+        int k = 0;
+        for (std::size_t l = 0; l < layers.size(); ++l)
+        {
+            const auto ops = mipt::cusv::build_rppu_layer_ops(layers[l], n);
+            op_count[l] = static_cast<int>(ops.ops.size());
+            for (const auto &op : ops.ops)
+            {
+                if (op.kind == mipt::cusv::OpKind::JwString)
+                {
+                    int lo = 0;
+                    while (!((op.string_mask >> (lo + 1)) & 1ull)) ++lo;
+                    op_meta[3 * k] = 2;
+                    op_meta[3 * k + 1] = lo;
+                    op_meta[3 * k + 2] = op.string_control;
+                }
+                else
+                {
+                    op_meta[3 * k] = 0;
+                    op_meta[3 * k + 1] = op.targets[0];
+                    op_meta[3 * k + 2] = op.targets[1];
+                    for (int e = 0; e < 16; ++e)
+                    {
+                        op_m[32 * k + 2 * e] = op.matrix.values[e].real();
+                        op_m[32 * k + 2 * e + 1] = op.matrix.values[e].imag();
+                    }
+                }
+                ++k;
+            }
+            sites_per_layer[l] = static_cast<int>(ops.measure_sites.size());
+            for (std::size_t j = 0; j < ops.measure_sites.size(); ++j) sites[l * n + j] = ops.measure_sites[j];
+        }
+        return static_cast<int>(layers.size());
+    }
+    catch (...)
+    {
+        return -1;
     }
 }
 

@@ -223,6 +223,31 @@ def main():
         out[f"fedraw{k}_sites"] = sites
         out[f"fedraw{k}_uniforms"] = uni[: nu[0]].copy()
 
+    # --- RPPU / qRPPU layer draws (ops as the engine receives them) -----------
+    lib.ref_rppu_draw.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_int] + [vp] * 5
+    lib.ref_rppu_draw.restype = ctypes.c_int
+    # (seed, n, periods-or-layers, p, boundary 0 FSWAP / 1 JW / 2 qubit, workspace)
+    RPPU_DRAWS = [(3, 6, 3, 0.3, 1, 0), (4, 8, 2, 0.5, 0, 0), (5, 10, 2, 1.0, 2, 0), (6, 4, 4, 0.0, 1, 0),
+                  (0xABCDEF12, 6, 7, 0.25, 1, 1), (77, 8, 5, 0.4, 2, 1)]
+    out["rppu_params"] = np.array(RPPU_DRAWS, np.float64)
+    for k, (seed, n, periods, p, boundary, ws) in enumerate(RPPU_DRAWS):
+        T = periods if ws else 2 * periods + 1
+        oc = np.zeros(T, np.int32)
+        meta = np.zeros((T * 4 * n, 3), np.int32)
+        m = np.zeros((T * 4 * n, 32))
+        spl = np.zeros(T, np.int32)
+        sites = np.full((T, n), -1, np.int32)
+        t = lib.ref_rppu_draw(seed, n, periods, p, boundary, ws,
+                              *[a.ctypes.data for a in (oc, meta, m, spl, sites)])
+        assert t > 0
+        kk = int(oc[:t].sum())
+        out[f"rppu{k}_ops_per_layer"] = oc[:t].copy()
+        out[f"rppu{k}_meta"] = meta[:kk].copy()
+        out[f"rppu{k}_m"] = m[:kk].copy()
+        out[f"rppu{k}_sites_per_layer"] = spl[:t].copy()
+        out[f"rppu{k}_sites"] = sites[:t].copy()
+
     path = os.path.join(HERE, "ref_fixtures.npz")
     np.savez_compressed(path, **out)
     print(f"wrote {path} ({os.path.getsize(path) / 1024:.1f} KiB, {len(out)} arrays)")

@@ -88,3 +88,39 @@ def test_workspace_sampler_matches_reference(mg, k):
     for t in range(layers):
         assert int(d["measured"][t]) == sum(1 << int(s) for s in sites[t, : spl[t]])
     np.testing.assert_array_equal(d["uniforms"], GOLD[f"fedraw{k}_uniforms"])
+
+
+@pytest.mark.parametrize("seed,n,workspace", [(3, 6, False), (4, 8, False), (11, 10, False), (0x1234, 8, True)])
+def test_rppu_sampler_matches_oracle(mg, seed, n, workspace):
+    """The batch's RPPU draw against the oracle's (itself pinned to the
+    reference): the same bonds and matrices in the plan's order (closure bond
+    last, stored for the qubit order (n-1, 0)), the same measured sites, an
+    identity extra layer when none was drawn, and one uniform per chunk with
+    site n-1 measured alone."""
+    from oracle import pyoracle as orc
+    periods, p, cb = 3, 0.45, 3
+    d = mg.draw_rppu(seed, n, periods, p, chunk_bits=cb, split_last=True, workspace=workspace)
+    o = orc.rppu_draw(seed, n, 2 * periods if workspace else periods, p, orc.RPPU_QUBIT, workspace)
+    swap = [0, 2, 1, 3]
+    k = 0
+    n_uniforms = 0
+    for t in range(2 * periods + 1):
+        bonds = {tuple(int(x) for x in d["bond_q"][t, j]): d["bond_u"][t, j].view(np.complex128).reshape(4, 4)
+                 for j in range(n // 2)}
+        if t >= o["layers"]:
+            assert all(np.array_equal(m, np.eye(4)) for m in bonds.values()) and int(d["measured"][t]) == 0
+            continue
+        for _ in range(o["ops_per_layer"][t]):
+            kind, q0, q1 = (int(x) for x in o["meta"][k])
+            m = o["m"][k].view(np.complex128).reshape(4, 4)
+            k += 1
+            if (q0, q1) == (0, n - 1):
+                got = bonds[(n - 1, 0)][np.ix_(swap, swap)]
+            else:
+                got = bonds[(q0, q1)]
+            np.testing.assert_array_equal(got, m)
+        sites = o["sites"][t, : o["sites_per_layer"][t]]
+        assert int(d["measured"][t]) == sum(1 << int(s) for s in sites)
+        plain = len(sites) - (1 if n - 1 in sites else 0)
+        n_uniforms += -(-plain // cb) + (1 if n - 1 in sites else 0)
+    assert len(d["uniforms"]) == n_uniforms

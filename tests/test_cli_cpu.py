@@ -261,7 +261,7 @@ def test_free_energy_usage_argument_errors_and_checkpoints(exes, tmp_path):
                       (["9", "0.1", "2", "1", "0"], "requires an even N"),
                       (["8", "1.5", "2", "1", "0"], "p must lie in [0,1]."),
                       (["8", "0.1", "2", "1", "2"], "init_state must be 0 or 1."),
-                      (["8", "0.1", "2", "2", "0"], "not on the GB300 trajectory path"),
+                      (["8", "0.1", "2", "3", "0"], "not on the GB300 trajectory path"),
                       (["8", "0.1", "2", "9", "0"], "circ_type must be one of")]:
         r = run([fe] + args, tmp_path)
         assert r.returncode == 1 and "free_energy.exe: " in r.stderr and msg in r.stderr, (args, r.stderr)

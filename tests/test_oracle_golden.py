@@ -167,3 +167,39 @@ def test_free_energy_trajectory_invariants():
     # Product initial state: zero half-chain entropy at t = 0.
     r0 = orc.fe_trajectory(ts, n, 0.3, init_kind=0)
     assert abs(r0["s_half"][0]) < 1e-12
+
+
+# ------------------------------------------------------------ RPPU / qRPPU
+@pytest.mark.parametrize("k", range(len(GOLD["rppu_params"])))
+def test_rppu_draw_matches_reference(k):
+    """Layer ops as the reference's engine receives them: gate order, targets,
+    matrices (the reference rebuilds each block from its U3 parameters: 1e-12),
+    FSWAP chains, JW strings, measured sites and the random extra even layer."""
+    seed, n, periods, p, boundary, ws = GOLD["rppu_params"][k]
+    d = orc.rppu_draw(int(seed), int(n), int(periods), float(p), int(boundary), bool(ws))
+    np.testing.assert_array_equal(d["ops_per_layer"], GOLD[f"rppu{k}_ops_per_layer"])
+    meta = d["meta"].copy()
+    meta[meta[:, 0] == 1, 0] = 0  # an FSWAP reaches the engine as a matrix op
+    np.testing.assert_array_equal(meta, GOLD[f"rppu{k}_meta"])
+    mat = meta[:, 0] == 0
+    np.testing.assert_allclose(d["m"][mat], GOLD[f"rppu{k}_m"][mat], rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(d["sites_per_layer"], GOLD[f"rppu{k}_sites_per_layer"])
+    np.testing.assert_array_equal(d["sites"], GOLD[f"rppu{k}_sites"])
+
+
+def test_rppu_closure_forms_agree_and_keep_parity():
+    """The FSWAP-chain and JW-string closures are the same operator (identical
+    trajectories); parity-preserving circuits keep the odd sector at exactly
+    zero; the qubit closure is a different circuit."""
+    n = 8
+    odd = np.array([bin(i).count("1") % 2 for i in range(1 << n)]) == 1
+    for seed in range(4):
+        a = orc.run_rppu_trajectory(seed, n, 4, 0.3, orc.RPPU_FSWAP)
+        b = orc.run_rppu_trajectory(seed, n, 4, 0.3, orc.RPPU_JW)
+        c = orc.run_rppu_trajectory(seed, n, 4, 0.3, orc.RPPU_QUBIT)
+        np.testing.assert_allclose(a["psi"], b["psi"], rtol=0, atol=1e-13)
+        np.testing.assert_array_equal(a["outcomes"], b["outcomes"])
+        assert np.all(b["psi"][odd] == 0) and np.all(c["psi"][odd] == 0)
+        assert abs(np.linalg.norm(b["psi"]) - 1) < 1e-12
+        assert a["layers"] in (8, 9)
+    assert np.abs(c["psi"] - b["psi"]).max() > 1e-3
