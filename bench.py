@@ -512,10 +512,44 @@ def config5():
                                        "no entropies (the GPU arm includes them)"}}
 
 
+def config6():
+    """The headline's shape on the parity-preserving gate sets: L = 24 closed
+    ring, 32 trajectories, 24 periods (48 layers plus the reference's random
+    extra even layer), p cycled over 16 values, final half-chain S_2, FP32;
+    FermionRPPU (fermionic closure folded into the closure gate, fermionic
+    partial trace) and qRPPU."""
+    import mipt_gb300 as mg
+    from oracle import pyoracle as orc
+    n, periods, count = 24, 24, 32
+    seeds = np.array([mg.trajectory_seed(6, i) for i in range(count)], np.uint64)
+    ps = P_GRID[np.arange(count) % 16]
+    out = {"config": "6: RPPU/qRPPU L=24 closed ring, 32 trajectories x (48 + extra) layers, final S_2(half), FP32",
+           "unit": UNIT}
+    for circuit, name in ((2, "fermion_rppu"), (4, "qrppu")):
+        b = mg.Batch(n, periods, count, fp64=False, observables=mg.OBS_S2_HALF, fermion_trace=circuit == 2,
+                     circuit=circuit)
+        b.run(seeds, ps)
+        b.set_profiling(True)
+        r, dt = _timed(lambda: b.run(seeds, ps))
+        layers = count * 2 * periods  # the extra even layers are not counted
+        stats = b.kernel_stats()
+        out[name] = {"value": layers / dt, "trajectory_layers": layers, "seconds": dt,
+                     "kernel_ms": {k: v[0] for k, v in stats.items()}}
+        b.close()
+    threads = orc.max_threads()
+    sample = [int(s) for s in seeds[:threads]]
+    _, cdt = _oracle_pool(lambda sd: orc.run_rppu_trajectory(sd, n, 1, 0.2, orc.RPPU_JW), sample, threads)
+    out["value"] = out["fermion_rppu"]["value"]
+    out["cpu_baseline"] = {"value": len(sample) * 2 / cdt, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": f"{len(sample)} FermionRPPU trajectories of 2 layers (+ extra), FP64 oracle, "
+                                     "one per host thread, no final entropy"}
+    return out
+
+
 def run_config(k):
     import torch
     torch.cuda.set_device(0)
-    fn = [config0, config1, config2, config3, config4, config5][k]
+    fn = [config0, config1, config2, config3, config4, config5, config6][k]
     line = fn()
     line["data"] = "synthetic"
     print(json.dumps(line), flush=True)
@@ -530,7 +564,7 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tile", type=int, default=0, help="local qubits per pass tile (0 = library default)")
-    ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..5 instead")
+    ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..6 instead")
     args = ap.parse_args()
     if args.config >= 0:
         return run_config(args.config)

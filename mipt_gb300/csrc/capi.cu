@@ -852,6 +852,11 @@ struct mipt_gb300_batch
     std::vector<int> obs_point;
     // Trajectories whose initial state was uploaded for the next execute.
     std::vector<char> custom_init;
+    // Global parity sector of each trajectory's initial state (-1: not a
+    // parity eigenstate), and the sector the FermionRPPU closure gates were
+    // folded for at upload (-1: not folded, the closure string runs as two
+    // diagonal passes).
+    std::vector<int> sector, folded;
     bool per_point() const { return !obs_point.empty() || cfg.observe_every > 0; }
     std::vector<EntReq> reqs; // for one point, trajectory index filled per launch
     int col_half_vn = -1, col_half_s2 = -1;
@@ -1499,6 +1504,8 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     if ((e = b->h_forced.ensure(C * T * sizeof(std::uint64_t))) != cudaSuccess) return cuda_fail(e, "pinned forced");
     if ((e = b->h_res.ensure(C * T * sizeof(LayerResult))) != cudaSuccess) return cuda_fail(e, "pinned results");
     b->custom_init.assign(C, 0);
+    b->sector.assign(C, 0);
+    b->folded.assign(C, -1);
     *out = b.release();
     return 0;
 }
@@ -1527,11 +1534,30 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
     for (int i = 0; i < count; ++i)
     {
         const TrajectoryDraw &d = draws[i];
+        // FermionRPPU: within a parity sector the closure's JW string is a
+        // diagonal on the closure bond itself -- (-1)^(n_hi * (n_lo + n_hi)) in
+        // the even sector, (-1)^(n_hi * n_lo) in the odd one -- so it folds into
+        // the closure gate (cpp/include/mipt/cusv/parity.hpp:38-45 makes the
+        // same reduction for the even sector).
+        const int fold = b->cfg.circuit == 2 ? b->sector[i] : -1;
+        b->folded[i] = fold;
+        std::vector<std::complex<double>> folded_layer;
         for (int t = 0; t < T; ++t)
         {
             const std::size_t slot = static_cast<std::size_t>(i) * T + t;
             // Gates: the draw's bond list matches the planned brickwork order.
             const std::complex<double> *src = &d.bond_u[static_cast<std::size_t>(t) * G * 16];
+            if (fold >= 0 && (t & 1))
+            {
+                // The closure bond is the layer's last, stored for (n-1, 0):
+                // index j = n_{n-1} + 2 n_0.
+                folded_layer.assign(src, src + static_cast<std::size_t>(G) * 16);
+                const double dg[4] = {1.0, fold == 0 ? -1.0 : 1.0, 1.0, fold == 0 ? 1.0 : -1.0};
+                std::complex<double> *u = folded_layer.data() + static_cast<std::size_t>(G - 1) * 16;
+                for (int r = 0; r < 4; ++r)
+                    for (int c = 0; c < 4; ++c) u[4 * r + c] *= dg[r] * dg[c];
+                src = folded_layer.data();
+            }
             if (b->cfg.fp64)
             {
                 double *dst = b->h_gates.as<double>() + slot * G * 32;
@@ -1690,6 +1716,7 @@ int mipt_gb300_batch_set_initial_state(mipt_gb300_batch *b, int index, const dou
         MG_CUDA(cudaMemcpy(dst, f.data(), dim * 8, cudaMemcpyHostToDevice));
     }
     b->custom_init[static_cast<std::size_t>(index)] = 1;
+    b->sector[static_cast<std::size_t>(index)] = -1;
     return 0;
 }
 
@@ -1738,6 +1765,7 @@ int mipt_gb300_batch_set_initial_states(mipt_gb300_batch *b, const std::uint64_t
             MG_CUDA(cudaMemcpy(static_cast<char *>(b->states.p) + static_cast<std::size_t>(first + k) * bytes,
                                stage[k].data(), bytes, cudaMemcpyHostToDevice));
             b->custom_init[static_cast<std::size_t>(first + k)] = 1;
+            b->sector[static_cast<std::size_t>(first + k)] = sector[first + k];
         }
     }
     if (parity_sectors) std::copy(sector.begin(), sector.end(), parity_sectors);
@@ -1810,6 +1838,20 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                 }
         std::fill(b->custom_init.begin(), b->custom_init.end(), 0);
     }
+    // FermionRPPU: closure strings not folded at upload run as diagonal passes
+    // on those trajectories; a fold for another sector than the state's is an
+    // ordering error of the caller.
+    std::vector<int> unfolded;
+    if (b->cfg.circuit == 2)
+        for (int i = 0; i < count; ++i)
+        {
+            if (b->folded[i] < 0)
+                unfolded.push_back(i);
+            else if (b->folded[i] != b->sector[i])
+                return fail(MIPT_GB300_E_INVALID,
+                            "FermionRPPU: set the initial states before mipt_gb300_batch_prepare_haar*");
+        }
+    std::fill(b->sector.begin(), b->sector.end(), 0);
     const std::size_t slots = static_cast<std::size_t>(count) * T;
     k_reset_layers<<<std::min<std::size_t>((slots + 255) / 256, 1024), 256, 0, s>>>(col, res, slots);
     ++L;
@@ -1864,12 +1906,16 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
         // Fermionic closure: the odd layer's gates run between two JW strings;
         // every other odd-layer bond lies inside the string and preserves its
         // parity, so the bracket covers the whole layer.
-        const bool jw = b->cfg.circuit == 2 && (t & 1);
+        const bool jw = !unfolded.empty() && (t & 1);
         auto jw_closure = [&]() {
             Mark m(b, K_OTHER, s);
-            k_jw_closure<Real><<<std::max(1, std::min(4 * 152, static_cast<int>(((b->dim / 2) * count + 255) / 256))),
-                                 256, 0, s>>>(states, n, count);
-            ++L;
+            const int grid = static_cast<int>(std::min<std::uint64_t>(4 * 152, (b->dim / 2 + 255) / 256));
+            for (int i : unfolded)
+            {
+                k_jw_closure<Real><<<std::max(1, grid), 256, 0, s>>>(states + static_cast<std::size_t>(i) * b->dim,
+                                                                      n, 1);
+                ++L;
+            }
         };
         if (jw) jw_closure();
         for (std::size_t pi = 0; pi < plan.size(); ++pi)

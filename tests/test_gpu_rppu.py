@@ -123,3 +123,38 @@ def test_mipt_exe_rppu_rho3_matches_oracle(mg, orc, tmp_path, circuit):
         psi = orc.run_rppu_trajectory(int(sd), n, periods, ps[pi], boundary, encoded=True)["psi"]
         want = orc.rho3(psi, subs, circuit == 2).reshape(n, 8, 8, 2)
         np.testing.assert_allclose(rec["rho"][k], want[..., 0] + 1j * want[..., 1], rtol=0, atol=1e-10)
+
+
+def test_fermion_closure_fold_matches_string_passes(mg, orc):
+    """FermionRPPU's closure string folded into the closure gate (parity sector
+    known from the initial-state draw) against the same trajectories run with
+    the string as two diagonal passes (the same amplitudes uploaded raw, sector
+    unknown); and the caller-ordering check."""
+    n, periods, p, count = 10, 3, 0.3, 4
+    ts = [orc.fe_trajectory_seed(5, i) for i in range(count)]
+    init = [orc.fe_initial_seed(t) for t in ts]
+    ws = [orc.fe_workspace_seed(t) for t in ts]
+    runs = []
+    for raw in (False, True):
+        b = mg.Batch(n, periods, count, fp64=True, observables=mg.OBS_SVN_HALF, fermion_trace=True, circuit=2,
+                     split_last=False)
+        if raw:
+            for i, sd in enumerate(init):
+                psi, _ = mg.draw_initial_state(sd, n, 1, fixed_parity=True, fp64=True)
+                b.set_initial_state(i, psi)
+        else:
+            sectors = b.set_initial_states(init, 1, fixed_parity=True)
+            assert set(sectors) <= {0, 1}
+        b.prepare_workspace(ws, p)
+        b.execute()
+        runs.append(b.fetch())
+    np.testing.assert_array_equal(runs[0]["outcomes"], runs[1]["outcomes"])
+    np.testing.assert_allclose(runs[0]["surprisal"], runs[1]["surprisal"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(runs[0]["obs"], runs[1]["obs"], rtol=0, atol=1e-12)
+    # Initial states set after the closure gates were folded for |0...0>.
+    b = mg.Batch(n, periods, count, fp64=True, circuit=2)
+    b.prepare_workspace(ws, p)
+    sectors = b.set_initial_states(init, 1, fixed_parity=True)
+    if any(s == 1 for s in sectors):
+        with pytest.raises(mg.MiptError):
+            b.execute()
