@@ -842,6 +842,9 @@ struct mipt_gb300_batch
     PinnedBuf h_gates, h_meas, h_forced, h_res;
     std::vector<std::uint64_t> measured;
     std::vector<char> any_meas, fusable;
+    // [layer][chunk]: every trajectory's chunk lies outside the histogram tile
+    // (one total per tile, streamed without shared-memory staging).
+    std::vector<char> direct_hist;
     std::vector<int> max_chunks;
     bool has_forced = false;
     int points = 0;
@@ -1294,10 +1297,10 @@ int mipt_gb300_engine_measure_layer(mipt_gb300_engine *e, const int *sites, int 
     {
         if (e->fp64)
             MG_CUDA(launch_hist<double>(static_cast<const Cx<double> *>(e->data()), 1, e->n, kmax, kCoalesceQubits, c,
-                                        e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), 0));
+                                        e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), false, 0));
         else
             MG_CUDA(launch_hist<float>(static_cast<const Cx<float> *>(e->data()), 1, e->n, kmax, kCoalesceQubits, c,
-                                       e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), 0));
+                                       e->col.as<Collapse>(), 1, e->meas.as<LayerMeas>(), 1, e->part.as<double>(), false, 0));
         MG_CUDA(launch_measure(1, e->n, nullptr, kmax, kCoalesceQubits, c, e->meas.as<LayerMeas>(), 1,
                                e->part.as<double>(), e->bins.as<double>(), kHistScratch, d_forced, 1,
                                e->col.as<Collapse>(), 1,
@@ -1527,6 +1530,7 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
     b->measured.assign(static_cast<std::size_t>(count) * T, 0);
     b->any_meas.assign(T, 0);
     b->fusable.assign(T, 1);
+    b->direct_hist.assign(static_cast<std::size_t>(T) * kMaxChunks, 1);
     b->max_chunks.assign(T, 0);
     b->has_forced = forced != nullptr;
     LayerMeas *hm = b->h_meas.as<LayerMeas>();
@@ -1600,7 +1604,14 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
                 ++in_chunk;
             }
             if (alone) M.chunk[++c] = last;
-            for (int cc = 0; cc < M.nchunks; ++cc) M.uniform[cc] = d.uniforms[d.uniform_offset[t] + cc];
+            for (int cc = 0; cc < M.nchunks; ++cc)
+            {
+                M.uniform[cc] = d.uniforms[d.uniform_offset[t] + cc];
+                PassGeom hg{};
+                histogram_geometry(n, b->kmax, b->cmin, M.chunk[cc], hg);
+                for (int li = 0; li < hg.k; ++li)
+                    if ((M.chunk[cc] >> hg.pos[li]) & 1ull) b->direct_hist[static_cast<std::size_t>(t) * kMaxChunks + cc] = 0;
+            }
             hm[slot] = M;
             hf[slot] = forced ? forced[slot] : 0ull;
             if (M.nchunks > 0)
@@ -1938,7 +1949,8 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                 {
                     Mark m(b, K_HIST, s);
                     MG_CUDA(launch_hist<Real>(states, count, n, b->kmax, b->cmin, ci, col + t, T, meas + t, T,
-                                              b->part.as<double>(), s));
+                                              b->part.as<double>(),
+                                              b->direct_hist[static_cast<std::size_t>(t) * kMaxChunks + ci] != 0, s));
                     ++L;
                 }
                 Mark m(b, K_MEASURE, s);

@@ -1022,7 +1022,8 @@ template <typename Real>
 __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restrict__ states, int n, int kmax, int cmin,
                                                        int ci, const Collapse *__restrict__ col_in,
                                                        std::size_t col_stride, const LayerMeas *__restrict__ meas,
-                                                       std::size_t meas_stride, double *__restrict__ partials)
+                                                       std::size_t meas_stride, double *__restrict__ partials,
+                                                       int direct)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ PassGeom g;
@@ -1034,7 +1035,7 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
     if (threadIdx.x == 0) histogram_geometry(n, kmax, cmin, chunk, g);
     __syncthreads();
     Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
-    std::uint32_t *seg = reinterpret_cast<std::uint32_t *>(smem_raw + (sizeof(Cx<Real>) << g.k));
+    std::uint32_t *seg = reinterpret_cast<std::uint32_t *>(direct ? smem_raw : smem_raw + (sizeof(Cx<Real>) << g.k));
     const std::uint64_t tix = blockIdx.x;
     const std::uint64_t dim = 1ull << n;
     const Cx<Real> *psi = states + static_cast<std::size_t>(b) * dim;
@@ -1046,13 +1047,42 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
     const bool has_col = col_in != nullptr;
     if (has_col) cl = col_in[b * col_stride];
     __syncthreads();
-    load_tile(tile, psi, g, base, seg, cl, has_col);
-    __syncthreads();
     int lm[kMaxLocal + 1];
     int m_loc = 0;
     for (int i = 0; i < g.k; ++i)
         if ((chunk >> g.pos[i]) & 1ull) lm[m_loc++] = i;
     double *part = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << m_loc);
+    if (direct)
+    {
+        // Every measured site is outside the tile (the host checked), so the
+        // tile contributes one total: stream it from global memory in the
+        // order tile_histogram sums a one-bin tile (thread t takes local
+        // indices t, t + T, ...; then the same shuffle and warp tree), without
+        // staging it in shared memory.
+        const std::uint64_t nloc = 1ull << g.k, cmask = (1ull << g.c) - 1ull;
+        const Real scale = static_cast<Real>(cl.scale);
+        Acc<Real> acc;
+        for (std::uint64_t r = threadIdx.x; r < nloc; r += blockDim.x)
+        {
+            const std::uint64_t gidx = base | seg[r >> g.c] | (r & cmask);
+            Cx<Real> v = psi[gidx];
+            if (has_col) v = collapse_value(v, gidx, cl, scale);
+            acc.add(norm2(v));
+        }
+        double v = acc.value();
+        for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off, 32);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            double t = 0.0;
+            for (int w = 0; w < static_cast<int>(blockDim.x) / 32; ++w) t += red[w];
+            part[0] = t;
+        }
+        return;
+    }
+    load_tile(tile, psi, g, base, seg, cl, has_col);
+    __syncthreads();
     tile_histogram(tile, g.k, lm, m_loc, part, red);
 }
 
@@ -1979,15 +2009,17 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
                         const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
-                        std::size_t meas_stride, double *partials, cudaStream_t s)
+                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s)
 {
     const int k = std::min(kmax, n);
-    const std::size_t smem = pass_smem<Real>(k);
+    // Direct (all measured sites outside the tile): only the segment table.
+    const std::size_t smem = direct ? (sizeof(std::uint32_t) << std::max(0, k - std::min(cmin, k)))
+                                    : pass_smem<Real>(k);
     cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_hist<Real>), smem);
     if (e != cudaSuccess) return e;
     dim3 grid(1u << (n - k), batch);
     k_hist<Real><<<grid, kPassThreads, smem, s>>>(states, n, kmax, cmin, chunk_index, collapse_in, collapse_stride,
-                                                  meas, meas_stride, partials);
+                                                  meas, meas_stride, partials, direct ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -2021,7 +2053,7 @@ cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, cons
                                         const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
                                         int, int *, cudaStream_t);                                               \
     template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
-                                        const LayerMeas *, std::size_t, double *, cudaStream_t);                 \
+                                        const LayerMeas *, std::size_t, double *, bool, cudaStream_t);           \
     template cudaError_t launch_collapse<R>(Cx<R> *, std::uint64_t, int, const Collapse *, std::size_t,          \
                                             cudaStream_t);
 MG_INSTANTIATE(float)

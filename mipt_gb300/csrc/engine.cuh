@@ -136,7 +136,7 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
                         const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
-                        std::size_t meas_stride, double *partials, cudaStream_t s);
+                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s);
 
 // Samples (or replays) the outcome of chunk `chunk_index` from the partial
 // histograms, writes the combined collapse of the layer and the outcome.
