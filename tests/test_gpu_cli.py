@@ -167,3 +167,34 @@ def test_entropy_exe_resumes_its_checkpoint(tmp_path):
     run([exe] + base + ["2", "1", "s1cap.csv"], tmp_path, True, {"MIPT_ENTROPY_S1_MAX_LA": "2"})
     _, c = _entropy_rows(tmp_path / "s1cap.csv")
     assert np.isfinite(c[0]["S1_mean"]) and all(np.isnan(row["S1_mean"]) for row in c[1:])
+
+
+@pytest.mark.parametrize("circuit", [2, 4])
+def test_sim_tmi_exe_rppu_matches_oracle(exes, orc, tmp_path, circuit):
+    """sim_tmi.exe on the parity-preserving gate sets: TMI of the cyclic
+    quarters from fermionic (circ_type 2) or qubit (4) partial traces of the
+    oracle's RPPU trajectories."""
+    _, tmi = exes
+    n, periods, R, res = 8, 2, 3, 2
+    run([tmi, str(n), str(periods), str(R), str(res), "0.1", "0.3", str(circuit), "1", "out.csv"], tmp_path, True)
+    rows = [tuple(float(x) for x in line.split(",")) for line in (tmp_path / "out.csv").read_text().splitlines()[1:]]
+    cycles, q = n // 4, n // 4
+    assert len(rows) == R * res * cycles
+    ps = np.linspace(0.1, 0.3, res)
+    fermion = circuit == 2
+    boundary = orc.RPPU_JW if fermion else orc.RPPU_QUBIT
+
+    def S(psi, modes):
+        return orc.entropy(orc.rdm(psi, [m % n for m in modes], fermion), 1)
+
+    i = 0
+    for pi in range(res):
+        for r in range(R):
+            seed = orc.trajectory_seed(SEED, pi * R + r)
+            psi = orc.run_rppu_trajectory(int(seed), n, periods, ps[pi], boundary, encoded=True)["psi"]
+            for c in range(cycles):
+                A, B, C, D = ([c + j * q + k for k in range(q)] for j in range(4))
+                want = S(psi, A) + S(psi, B) + S(psi, C) + S(psi, D) - S(psi, A + B) - S(psi, A + C) - S(psi, B + C)
+                p, got = rows[i]
+                i += 1
+                assert abs(got - want) < 1e-10, (pi, r, c, got, want)
