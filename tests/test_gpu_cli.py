@@ -144,6 +144,33 @@ def test_entropy_exe_matches_oracle(orc, tmp_path):
             assert abs(row[name + "_stderr"] - v.std(ddof=1) / np.sqrt(R)) < 1e-9, (kept, name)
 
 
+def test_entropy_exe_fermion_rppu_matches_oracle(orc, tmp_path):
+    """entropy.exe with circ_type 2: the cyclic-block entropies of FermionRPPU
+    trajectories from fermionic partial traces, and fermionic_trace = 1."""
+    exe = os.path.join(ROOT, "mipt_gb300", "_build", "entropy.exe")
+    n, periods, p, R = 8, 2, 0.3, 3
+    run([exe, str(n), str(periods), str(p), str(R), "2", "e.csv"], tmp_path, True, {"MIPT_GB300_BATCH": "2"})
+    _, rows = _entropy_rows(tmp_path / "e.csv")
+    per = {k: ([], []) for k in range(2, n // 2 + 1)}
+    for r in range(R):
+        psi = orc.run_rppu_trajectory(int(orc.trajectory_seed(SEED, r)), n, periods, p, orc.RPPU_JW)["psi"]
+        for kept in per:
+            s1 = s2 = 0.0
+            for c in range(n):
+                rho = orc.rdm(psi, [(c + j) % n for j in range(kept)], True)
+                w = np.linalg.eigvalsh(rho)
+                w = w[w > 1e-15]
+                s1 += -np.sum(w * np.log(w)) / n
+                s2 += -np.log(np.sum(np.abs(rho) ** 2)) / n
+            per[kept][0].append(s1)
+            per[kept][1].append(s2)
+    for row in rows:
+        kept = int(row["L_A"])
+        assert row["circ_type"] == 2 and row["fermionic_trace"] == 1
+        for name, vals in (("S1", per[kept][0]), ("S2", per[kept][1])):
+            assert abs(row[name + "_mean"] - np.mean(vals)) < 1e-9, (kept, name)
+
+
 def test_entropy_exe_resumes_its_checkpoint(tmp_path):
     """A 2-trajectory checkpoint re-labelled as part of a 5-trajectory run and
     resumed gives the same file as an uninterrupted 5-trajectory run (up to
