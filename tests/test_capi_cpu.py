@@ -124,3 +124,14 @@ def test_rppu_sampler_matches_oracle(mg, seed, n, workspace):
         plain = len(sites) - (1 if n - 1 in sites else 0)
         n_uniforms += -(-plain // cb) + (1 if n - 1 in sites else 0)
     assert len(d["uniforms"]) == n_uniforms
+
+
+def test_batch_rejects_unsupported_circuits_before_device_work(mg):
+    """Gate-set checks of mipt_gb300_batch_create come before any device call:
+    MMS / RFGS, and RPPU off the closed 1-D ring, fail with an invalid-argument
+    status on any machine."""
+    for kwargs, msg in [(dict(circuit=3), "circuit must be"), (dict(circuit=2, closed=False), "closed 1-D ring"),
+                        (dict(circuit=4, lattice=(2, 4)), "closed 1-D ring")]:
+        with pytest.raises(mg.MiptError) as e:
+            mg.Batch(8, 2, 1, **kwargs)
+        assert msg in str(e.value), (kwargs, str(e.value))
