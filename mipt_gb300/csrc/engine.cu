@@ -1062,12 +1062,36 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
         const std::uint64_t nloc = 1ull << g.k, cmask = (1ull << g.c) - 1ull;
         const Real scale = static_cast<Real>(cl.scale);
         Acc<Real> acc;
-        for (std::uint64_t r = threadIdx.x; r < nloc; r += blockDim.x)
+        // Four loads in flight per thread, added in the same order as one at
+        // a time; tiles that are not a multiple of four block-widths take the
+        // plain loop.
+        const std::uint64_t T4 = 4ull * blockDim.x;
+        if (nloc % T4 != 0)
+            for (std::uint64_t r = threadIdx.x; r < nloc; r += blockDim.x)
+            {
+                const std::uint64_t gidx = base | seg[r >> g.c] | (r & cmask);
+                Cx<Real> v = psi[gidx];
+                if (has_col) v = collapse_value(v, gidx, cl, scale);
+                acc.add(norm2(v));
+            }
+        else
+        for (std::uint64_t r0 = threadIdx.x; r0 < nloc; r0 += T4)
         {
-            const std::uint64_t gidx = base | seg[r >> g.c] | (r & cmask);
-            Cx<Real> v = psi[gidx];
-            if (has_col) v = collapse_value(v, gidx, cl, scale);
-            acc.add(norm2(v));
+            Cx<Real> v[4];
+            std::uint64_t gi[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                const std::uint64_t r = r0 + static_cast<std::uint64_t>(u) * blockDim.x;
+                gi[u] = base | seg[r >> g.c] | (r & cmask);
+                v[u] = psi[gi[u]];
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                if (has_col) v[u] = collapse_value(v[u], gi[u], cl, scale);
+                acc.add(norm2(v[u]));
+            }
         }
         double v = acc.value();
         for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off, 32);
