@@ -294,9 +294,10 @@ def run_gb300(args):
     return 0
 
 
-# ------------------------------------------------- the other BASELINE configs
+# ------------------------------------------------- the other workload configurations
 # `--config N` measures configuration N of the workload list (0: plain FP64
-# chain, 1: free fermions, 2: mixed-length batch, 3: 2-D lattice, 4: GMN) and
+# chain, 1: free fermions, 2: mixed-length batch, 3: 2-D lattice, 4: GMN,
+# 5: free-energy protocol, 6: RPPU / qRPPU gate sets) and
 # prints one JSON line for it; the default run (no --config) is the headline
 # L = 24 metric above.
 def _timed(fn):

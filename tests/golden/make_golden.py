@@ -21,7 +21,7 @@ LIB = os.path.join(ROOT, "oracle", "_ref", "libmipt_ref.so")
 
 # (seed, n, periods, p, closed, chunk_bits): covers open and closed chains,
 # p = 0 and p = 1 (the sampler's two short-cuts), chunk splitting, and the
-# BASELINE-scale chain lengths.
+# the chain lengths of the measured workloads.
 DRAWS = [
     (0, 12, 12, 0.2, 0, 16),
     (1, 12, 3, 0.2, 1, 16),
