@@ -302,3 +302,18 @@ def test_free_energy_usage_argument_errors_and_checkpoints(exes, tmp_path):
     (tmp_path / f"{stem}_samples.csv").write_text(samples)
     r = run([fe, "8", "0.1", "3", "1", "0"], tmp_path, {"MIPT_FREE_ENERGY_SEED": "5"})
     assert r.returncode == 0 and "Nothing to do." in r.stdout
+
+
+def test_rppu_circuit_types_pass_argument_checks(exes, tmp_path):
+    """circ_type 2 (FermionRPPU) and 4 (qRPPU) are on the GB300 path: the
+    executables accept them up to device work (here: no device) and keep the
+    reference's even-N rule for them (cpp/include/mipt/types.hpp:174-185)."""
+    mipt, tmi = exes
+    fe = os.path.join(os.path.dirname(mipt), "free_energy.exe")
+    for ct in ("2", "4"):
+        r = run([mipt, "1", "9", "2", "1", "1", "0.1", "0.2", ct], tmp_path)
+        assert r.returncode == 1 and "requires an even n" in r.stderr, r.stderr
+        r = run([fe, "9", "0.1", "2", ct, "0"], tmp_path)
+        assert r.returncode == 1 and "requires an even N" in r.stderr, r.stderr
+        r = run([mipt, "1", "8", "2", "1", "1", "0.1", "0.2", ct], tmp_path)
+        assert "not on the GB300 trajectory path" not in r.stderr
