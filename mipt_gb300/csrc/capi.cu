@@ -2050,7 +2050,7 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
         MG_CUDA(cudaMemcpy(&err, b->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) return fail(MIPT_GB300_E_INTERNAL, "tensor-core Gram pipeline wait timed out");
     }
-    const int count = b->count, T = b->T, n = b->cfg.n_qubits;
+    const int count = b->count, T = b->T;
     if (measured) std::copy(b->measured.begin(), b->measured.end(), measured);
     if (outcomes || surprisal)
     {
