@@ -57,6 +57,23 @@ def seeds_for(rank, batch, step=0):
     return np.array([mg.trajectory_seed(0, base + i) for i in range(batch)], np.uint64)
 
 
+def max_over_ranks(value, dist, device):
+    """The slowest rank's figure (the whole job ends with it); the value itself
+    on one rank (dist None)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(batch, layers, world, steps, seconds):
+    """Trajectory-layers per second over all ranks: every rank runs `batch`
+    trajectories of `layers` layers per step (weak scaling)."""
+    return batch * layers * world * steps / seconds
+
+
 def p_for(batch):
     return np.array([P_GRID[i % len(P_GRID)] for i in range(batch)])
 
@@ -205,12 +222,8 @@ def run_gb300(args):
     stats = batch.kernel_stats()  # last step, per launch category
     launches = batch.launches * args.steps
     batch.set_profiling(False)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    units = B * T * world * args.steps
-    value = units / (ms / 1000.0)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = whole_job_rate(B, T, world, args.steps, ms / 1000.0)
 
     # ------------------------------------------------------------ e2e
     for _ in range(1):
@@ -222,11 +235,8 @@ def run_gb300(args):
     for s in range(args.steps):
         batch.run(seeds_for(rank, B, s + 1), ps)
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = B * T * world * args.steps / e2e_s
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_value = whole_job_rate(B, T, world, args.steps, e2e_s)
     h2d = B * T * (N_QUBITS // 2) * 16 * 8 + B * T * 136  # FP32 gates + measurement records
     d2h = B * T * 88 + B * 4 * 8
 
