@@ -22,12 +22,15 @@
 //                                               cpp/include/mipt/free_energy.hpp:125-222
 //   CircuitWorkspace1D::seed (restated below: the class itself needs a live
 //   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
+//   free_energy.exe's checkpoint readers (scan_samples, load_timeseries)
+//                                               cpp/include/mipt/free_energy_resume.hpp:246-534
 //   build_rppu_layers_with_boundary / fill_rppu_layer, build_rppu_layer_ops
 //                                               cpp/include/mipt/circuits/rppu_layer.hpp:167-285,
 //                                               cpp/include/mipt/cusv/gates.hpp:219-281
 #include "mipt/circuits/haar.hpp"
 #include "mipt/circuits/rppu_layer.hpp"
 #include "mipt/free_energy.hpp"
+#include "mipt/free_energy_resume.hpp"
 #include "mipt/cusv/gates.hpp"
 #include "mipt/free_energy_measure.hpp"
 #include "mipt/rdm.hpp"
@@ -35,6 +38,7 @@
 #include "mipt/types.hpp"
 
 #include <complex>
+#include <cstdio>
 #include <cstdint>
 #include <cstring>
 #include <random>
@@ -285,6 +289,41 @@ int ref_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits,
     }
     catch (...)
     {
+        return 1;
+    }
+}
+
+// free_energy.exe's resume decision for the two CSVs at `samples_path` /
+// `series_path`: out[0] completed samples rows, out[1] time-series aggregate
+// count, out[2] valid bytes of the samples file; *master the recovered master
+// seed (has_master in out[3]). Returns 0, or 1 when the reference refuses the
+// checkpoint (its message in `message`, up to `message_len` bytes).
+int ref_fe_resume(const char *samples_path, const char *series_path, int n, double p, int circ_type, int init_state,
+                  long requested, int record, int max_t, int stride, long *out, std::uint64_t *master, char *message,
+                  int message_len)
+{
+    namespace r = mipt::free_energy::resume;
+    try
+    {
+        r::RunIdentity id;
+        id.n = n;
+        id.p = p;
+        id.circ_type = circ_type;
+        id.init_state = init_state;
+        id.requested_realizations = requested;
+        const auto samples = r::scan_samples(samples_path, r::kSamplesHeader, id);
+        const auto series = r::load_timeseries(series_path, r::kTimeseriesHeader, id, 28 * n, record != 0, max_t,
+                                               stride);
+        out[0] = samples.completed;
+        out[1] = series.completed;
+        out[2] = static_cast<long>(samples.valid_bytes);
+        out[3] = samples.has_master_seed ? 1 : 0;
+        *master = samples.master_seed;
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        std::snprintf(message, static_cast<std::size_t>(message_len), "%s", e.what());
         return 1;
     }
 }

@@ -61,6 +61,50 @@ def xorshift_state(n, seed):
     return psi / np.linalg.norm(psi)
 
 
+def fe_checkpoint_cases(lib):
+    """free_energy.exe checkpoint pairs (samples CSV, time-series CSV, run
+    parameters) in the reference's layout: a clean one, a killed flush, a
+    lagging aggregate, and three the reference refuses."""
+    sm = lib.ref_splitmix64
+    H_S = ("N,p,circ_type,circuit_name,init_state,trajectory,parity_sector,trajectory_seed,equil_timesteps,"
+           "production_timesteps,total_timesteps,measurements_total,measurements_production,F_total,F_production,"
+           "production_rate_endpoint,production_slope,free_energy_density_tilde")
+    H_T = ("N,p,circ_type,circuit_name,init_state,requested_realizations,completed_realizations,t,t_over_L,phase,"
+           "F_mean,F_stddev,F_stderr,F_over_tL_mean,F_over_tL_stddev,F_over_tL_stderr,S_half_mean,S_half_stddev,"
+           "S_half_stderr,S_half_count")
+    name = '"Random Haar Unitary"'
+
+    def samples(n, p, init, master, count, skip=None):
+        rows = [H_S]
+        for t in range(count):
+            if t == skip:
+                continue
+            ts = sm((master ^ t) & 0xFFFFFFFFFFFFFFFF)
+            rows.append(f"{n},{p!r},1,{name},{init},{t},-1,{ts},{4 * n},{24 * n},{28 * n},10,8,1.5,1.25,0.1,0.1,0.0125")
+        return "\n".join(rows) + "\n"
+
+    def series(n, p, init, requested, completed, max_t):
+        rows = [H_T]
+        for t in range(28 * n + 1):
+            phase = "initial" if t == 0 else ("equilibration" if t <= 4 * n else "production")
+            sc = completed if t <= max_t else 0
+            st = "0.5,0.1,0.05" if sc else "nan,nan,nan"
+            f = "0,0,0" if t == 0 else "0.25,0.01,0.005"
+            ftl = "nan,nan,nan" if t == 0 else "0.01,0.001,0.0005"
+            rows.append(f"{n},{p!r},1,{name},{init},{requested},{completed},{t},{t / n!r},{phase},{f},{ftl},{st},{sc}")
+        return "\n".join(rows) + "\n"
+
+    n, p, R = 6, 0.2, 6
+    return [
+        (samples(n, p, 0, 991, 3), series(n, p, 0, R, 3, 12), (n, p, 0, R, 12, 1)),
+        (samples(n, p, 0, 5, 4) + f"{n},0.2,1,\"Ran", series(n, p, 0, R, 4, 12), (n, p, 0, R, 12, 1)),
+        (samples(n, p, 1, 2**64 - 7, 3), series(n, p, 1, R, 2, 12), (n, p, 1, R, 12, 1)),
+        (samples(n, p, 0, 42, 3, skip=1), series(n, p, 0, R, 2, 12), (n, p, 0, R, 12, 1)),
+        (samples(n, p, 0, 42, 3), series(n, p, 0, R, 3, 12), (n, p, 0, R, 7, 1)),
+        (samples(n, p, 1, 42, 3), series(n, p, 1, R, 3, 12), (n, p, 0, R, 12, 1)),
+    ]
+
+
 def main():
     if not os.path.exists(LIB):
         subprocess.check_call([os.path.join(ROOT, "oracle", "ref", "build_ref.sh")])
@@ -247,6 +291,33 @@ def main():
         out[f"rppu{k}_m"] = m[:kk].copy()
         out[f"rppu{k}_sites_per_layer"] = spl[:t].copy()
         out[f"rppu{k}_sites"] = sites[:t].copy()
+
+    # --- free_energy.exe checkpoints through the reference's own readers ----
+    lib.ref_fe_resume.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
+                                  ctypes.c_char_p, ctypes.c_int]
+    import tempfile
+    cases = fe_checkpoint_cases(lib)
+    rows = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (samples, series, prm) in enumerate(cases):
+            sp, tp = os.path.join(tmp, f"s{k}.csv"), os.path.join(tmp, f"t{k}.csv")
+            with open(sp, "w") as f:
+                f.write(samples)
+            with open(tp, "w") as f:
+                f.write(series)
+            res = np.zeros(4, np.int64)
+            master = np.zeros(1, np.uint64)
+            msg = ctypes.create_string_buffer(1024)
+            n, p, init, R, max_t, stride = prm
+            rc = lib.ref_fe_resume(sp.encode(), tp.encode(), n, p, 1, init, R, 1, max_t, stride,
+                                   res.ctypes.data, master.ctypes.data, msg, 1024)
+            out[f"feck{k}_samples"] = np.array(samples)
+            out[f"feck{k}_series"] = np.array(series)
+            out[f"feck{k}_message"] = np.array(msg.value.decode())
+            rows.append([n, p, init, R, max_t, stride, rc, *res.tolist(), float(master[0])])
+            out[f"feck{k}_master"] = master.copy()
+    out["feck_params"] = np.array(rows, np.float64)
 
     path = os.path.join(HERE, "ref_fixtures.npz")
     np.savez_compressed(path, **out)

@@ -317,3 +317,43 @@ def test_rppu_circuit_types_pass_argument_checks(exes, tmp_path):
         assert r.returncode == 1 and "requires an even N" in r.stderr, r.stderr
         r = run([mipt, "1", "8", "2", "1", "1", "0.1", "0.2", ct], tmp_path)
         assert "not on the GB300 trajectory path" not in r.stderr
+
+
+GOLD = np.load(os.path.join(ROOT, "tests", "golden", "ref_fixtures.npz"))
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["feck_params"])))
+def test_free_energy_resume_matches_reference_reader(exes, tmp_path, k):
+    """free_energy.exe reads six checkpoints exactly as the reference's own
+    readers (scan_samples / load_timeseries, recorded in the fixtures) do:
+    completed rows, aggregate lag, trimmed tail and recovered master seed, or
+    the same refusal text. With no device visible the accepted runs stop at
+    batch creation, after the resume report."""
+    n, p, init, R, max_t, stride, rc, completed, agg, valid, has_master, _ = GOLD["feck_params"][k]
+    n, init, R, completed, agg, valid = int(n), int(init), int(R), int(completed), int(agg), int(valid)
+    master = int(GOLD[f"feck{k}_master"][0])
+    samples, series = str(GOLD[f"feck{k}_samples"]), str(GOLD[f"feck{k}_series"])
+    stem = f"free_energy_haar_n_{n}_p_{p:g}_init_{init}_reals_{R}"
+    sp, tp = tmp_path / f"{stem}_samples.csv", tmp_path / f"{stem}_timeseries.csv"
+    sp.write_text(samples)
+    tp.write_text(series)
+    fe = os.path.join(os.path.dirname(exes[0]), "free_energy.exe")
+    env = {"CUDA_VISIBLE_DEVICES": "", "MIPT_FREE_ENERGY_ENTROPY_MAX_T": str(int(max_t)),
+           "MIPT_FREE_ENERGY_ENTROPY_STRIDE": str(int(stride))}
+    r = run([fe, str(n), str(p), str(R), "1", str(init)], tmp_path, env)
+    if int(rc) != 0:
+        msg = str(GOLD[f"feck{k}_message"])
+        import re
+        msg = re.sub(r"\S*/s\d+\.csv", sp.name, msg)
+        msg = re.sub(r"\S*/t\d+\.csv", tp.name, msg)
+        assert r.returncode == 1 and msg in r.stderr, (msg, r.stderr)
+        return
+    assert f"Resuming from {sp.name}: {completed}/{R} trajectories already recorded, seed stream recovered." \
+        in r.stdout, r.stdout + r.stderr
+    assert f"seed={master}\n" in r.stdout
+    if agg != completed:
+        assert f"The time-series aggregate holds {agg} trajectories against the samples file's {completed}" in r.stdout
+    if valid < len(samples.encode()):
+        assert f"Dropping {len(samples.encode()) - valid} bytes of an unterminated trailing row" in r.stdout
+        assert len(sp.read_bytes()) == valid
+    assert r.returncode == 1 and "free_energy.exe: " in r.stderr and "Resume refused" not in r.stderr
