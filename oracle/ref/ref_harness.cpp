@@ -22,6 +22,7 @@
 //                                               cpp/include/mipt/free_energy.hpp:125-222
 //   CircuitWorkspace1D::seed (restated below: the class itself needs a live
 //   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
+//   DensityMatrixWriter (rho3.bin version 2)   cpp/include/mipt/density.hpp:134-251
 //   free_energy.exe's checkpoint readers (scan_samples, load_timeseries)
 //                                               cpp/include/mipt/free_energy_resume.hpp:246-534
 //   build_rppu_layers_with_boundary / fill_rppu_layer, build_rppu_layer_ops
@@ -29,6 +30,7 @@
 //                                               cpp/include/mipt/cusv/gates.hpp:219-281
 #include "mipt/circuits/haar.hpp"
 #include "mipt/circuits/rppu_layer.hpp"
+#include "mipt/density.hpp"
 #include "mipt/free_energy.hpp"
 #include "mipt/free_energy_resume.hpp"
 #include "mipt/cusv/gates.hpp"
@@ -285,6 +287,44 @@ int ref_fe_draw(std::uint32_t seed, int n, int layers, double p, int chunk_bits,
                 uniforms[u++] = uniform(measure_rng);
         }
         *n_uniforms = u;
+        return 0;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+// A rho3.bin written by the reference's DensityMatrixWriter: dims = spatial
+// dimension, total qubits, kept qubits, periods, realizations, resolution,
+// grid_x, grid_y, subsystem count; records[i] = (p_index, realization) with
+// probability ps[i] and payload[i * values ...].
+int ref_rho3_write(const char *path, const std::uint32_t *dims, std::uint64_t record_count, double p_min,
+                   double p_max, const std::uint32_t *subsystem_qubits, const std::uint32_t *p_index,
+                   const std::uint32_t *realization, const double *ps, const double *payload)
+{
+    try
+    {
+        mipt::io::DensityFileMetadata m;
+        m.spatial_dimension = dims[0];
+        m.total_qubits = dims[1];
+        m.kept_qubits = dims[2];
+        m.matrix_dimension = 1u << dims[2];
+        m.periods = dims[3];
+        m.realizations = dims[4];
+        m.resolution = dims[5];
+        m.grid_x = dims[6];
+        m.grid_y = dims[7];
+        m.subsystem_count = dims[8];
+        m.record_count = record_count;
+        m.p_min = p_min;
+        m.p_max = p_max;
+        m.subsystem_qubits.assign(subsystem_qubits, subsystem_qubits + dims[8] * dims[2]);
+        mipt::io::DensityMatrixWriter w(path, m);
+        const std::size_t values = mipt::io::payload_value_count(m);
+        for (std::uint64_t i = 0; i < record_count; ++i)
+            w.write_record(p_index[i], realization[i], ps[i], payload + i * values, values);
+        w.close();
         return 0;
     }
     catch (...)

@@ -292,6 +292,33 @@ def main():
         out[f"rppu{k}_sites_per_layer"] = spl[:t].copy()
         out[f"rppu{k}_sites"] = sites[:t].copy()
 
+    # --- rho3.bin files written by the reference's DensityMatrixWriter -------
+    lib.ref_rho3_write.argtypes = [ctypes.c_char_p, vp, ctypes.c_uint64, ctypes.c_double, ctypes.c_double] + [vp] * 5
+    import tempfile
+    rng = np.random.default_rng(31)
+    # (spatial, total, kept, periods, realizations, resolution, grid_x, grid_y, subsystems), records
+    RHO3_FILES = [((1, 5, 3, 4, 1, 2, 5, 1, 5), 2), ((2, 6, 3, 3, 2, 1, 2, 3, 4), 3), ((1, 4, 2, 1, 1, 1, 4, 1, 2), 1)]
+    for k, (dims, nrec) in enumerate(RHO3_FILES):
+        dims_a = np.array(dims, np.uint32)
+        S, K = dims[8], dims[2]
+        subs = np.concatenate([rng.permutation(dims[1])[:K] for _ in range(S)]).astype(np.uint32)
+        pidx = rng.integers(0, 3, size=nrec).astype(np.uint32)
+        real = rng.integers(0, 9, size=nrec).astype(np.uint32)
+        ps = rng.uniform(0, 1, size=nrec)
+        payload = rng.standard_normal(nrec * S * 2 * (1 << K) ** 2)
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "rho3.bin")
+            assert lib.ref_rho3_write(path.encode(), dims_a.ctypes.data, nrec, 0.125, 0.875, subs.ctypes.data,
+                                      pidx.ctypes.data, real.ctypes.data, ps.ctypes.data, payload.ctypes.data) == 0
+            with open(path, "rb") as f:
+                out[f"rho3file{k}_bytes"] = np.frombuffer(f.read(), np.uint8).copy()
+        out[f"rho3file{k}_dims"] = dims_a
+        out[f"rho3file{k}_subs"] = subs
+        out[f"rho3file{k}_pidx"] = pidx
+        out[f"rho3file{k}_real"] = real
+        out[f"rho3file{k}_p"] = ps
+        out[f"rho3file{k}_payload"] = payload
+
     # --- free_energy.exe checkpoints through the reference's own readers ----
     lib.ref_fe_resume.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                                   ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, vp,
@@ -314,7 +341,7 @@ def main():
                                    res.ctypes.data, master.ctypes.data, msg, 1024)
             out[f"feck{k}_samples"] = np.array(samples)
             out[f"feck{k}_series"] = np.array(series)
-            out[f"feck{k}_message"] = np.array(msg.value.decode())
+            out[f"feck{k}_message"] = np.array(msg.value.decode().replace(tmp + os.sep, ""))
             rows.append([n, p, init, R, max_t, stride, rc, *res.tolist(), float(master[0])])
             out[f"feck{k}_master"] = master.copy()
     out["feck_params"] = np.array(rows, np.float64)

@@ -342,10 +342,7 @@ def test_free_energy_resume_matches_reference_reader(exes, tmp_path, k):
            "MIPT_FREE_ENERGY_ENTROPY_STRIDE": str(int(stride))}
     r = run([fe, str(n), str(p), str(R), "1", str(init)], tmp_path, env)
     if int(rc) != 0:
-        msg = str(GOLD[f"feck{k}_message"])
-        import re
-        msg = re.sub(r"\S*/s\d+\.csv", sp.name, msg)
-        msg = re.sub(r"\S*/t\d+\.csv", tp.name, msg)
+        msg = str(GOLD[f"feck{k}_message"]).replace(f"s{k}.csv", sp.name).replace(f"t{k}.csv", tp.name)
         assert r.returncode == 1 and msg in r.stderr, (msg, r.stderr)
         return
     assert f"Resuming from {sp.name}: {completed}/{R} trajectories already recorded, seed stream recovered." \
@@ -357,3 +354,60 @@ def test_free_energy_resume_matches_reference_reader(exes, tmp_path, k):
         assert f"Dropping {len(samples.encode()) - valid} bytes of an unterminated trailing row" in r.stdout
         assert len(sp.read_bytes()) == valid
     assert r.returncode == 1 and "free_energy.exe: " in r.stderr and "Resume refused" not in r.stderr
+
+
+@pytest.fixture(scope="module")
+def rho3_io(tmp_path_factory):
+    exe = tmp_path_factory.mktemp("rho3io") / "rho3_io"
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "include"), "-I",
+                        os.path.join(ROOT, "mipt_gb300", "apps"), os.path.join(ROOT, "tests", "golden", "rho3_io.cpp"),
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return str(exe)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_rho3_bin_matches_reference_writer(rho3_io, tmp_path, k):
+    """rho3.bin files the reference's DensityMatrixWriter wrote
+    (cpp/include/mipt/density.hpp:134-251): the executables' C++ writer
+    reproduces them byte for byte from the same content, their C++ reader and
+    mipt_gb300.rho3file read back exactly that content."""
+    want = GOLD[f"rho3file{k}_bytes"].tobytes()
+    dims = [int(x) for x in GOLD[f"rho3file{k}_dims"]]
+    subs, pidx, real = GOLD[f"rho3file{k}_subs"], GOLD[f"rho3file{k}_pidx"], GOLD[f"rho3file{k}_real"]
+    ps, payload = GOLD[f"rho3file{k}_p"], GOLD[f"rho3file{k}_payload"]
+    nrec = len(ps)
+    per = payload.size // nrec
+    spec = [" ".join(str(x) for x in dims + [nrec]), (0.125).hex(), (0.875).hex(), " ".join(str(int(q)) for q in subs)]
+    for r in range(nrec):
+        spec.append(f"{int(pidx[r])} {int(real[r])} {float(ps[r]).hex()} " +
+                    " ".join(float(v).hex() for v in payload[r * per:(r + 1) * per]))
+    (tmp_path / "spec.txt").write_text("\n".join(spec) + "\n")
+    r = subprocess.run([rho3_io, "write", str(tmp_path / "ours.bin"), str(tmp_path / "spec.txt")], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "ours.bin").read_bytes() == want
+    (tmp_path / "ref.bin").write_bytes(want)
+    r = subprocess.run([rho3_io, "read", str(tmp_path / "ref.bin")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    head = lines[0].split()
+    assert [int(x) for x in head[:10]] == dims[:9] + [nrec]
+    assert float.fromhex(head[10]) == 0.125 and float.fromhex(head[11]) == 0.875
+    assert [int(x) for x in lines[1].split()] == [int(q) for q in subs]
+    for r_, line in enumerate(lines[2:]):
+        cells = line.split()
+        assert int(cells[0]) == pidx[r_] and int(cells[1]) == real[r_] and float.fromhex(cells[2]) == ps[r_]
+        assert np.array_equal(np.array([float.fromhex(c) for c in cells[3:]]), payload[r_ * per:(r_ + 1) * per])
+    meta, rec = rho3file.read(tmp_path / "ref.bin")
+    assert meta["spatial_dimension"] == dims[0] and meta["grid_y"] == dims[7] and meta["record_count"] == nrec
+    assert np.array_equal(meta["subsystem_qubits"].ravel(), subs)
+    D = 1 << dims[2]
+    np.testing.assert_array_equal(rec["rho"].reshape(nrec, -1),
+                                  payload.reshape(nrec, -1, 2)[..., 0] + 1j * payload.reshape(nrec, -1, 2)[..., 1])
+    assert rec["rho"].shape == (nrec, dims[8], D, D)
+    rho = payload.reshape(nrec, dims[8], D, D, 2)
+    rho3file.write(tmp_path / "py.bin", rho[..., 0] + 1j * rho[..., 1], ps, pidx, real, total_qubits=dims[1],
+                   periods=dims[3], realizations=dims[4], resolution=dims[5], p_min=0.125, p_max=0.875,
+                   subsystem_qubits=subs, spatial_dimension=dims[0], grid_x=dims[6], grid_y=dims[7])
+    assert (tmp_path / "py.bin").read_bytes() == want
