@@ -23,6 +23,7 @@
 //   CircuitWorkspace1D::seed (restated below: the class itself needs a live
 //   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
 //   DensityMatrixWriter (rho3.bin version 2)   cpp/include/mipt/density.hpp:134-251
+//   entropy.exe's checkpoint reader            cpp/include/mipt/entropy_resume.hpp:102-246
 //   free_energy.exe's checkpoint readers (scan_samples, load_timeseries)
 //                                               cpp/include/mipt/free_energy_resume.hpp:246-534
 //   build_rppu_layers_with_boundary / fill_rppu_layer, build_rppu_layer_ops
@@ -31,6 +32,7 @@
 #include "mipt/circuits/haar.hpp"
 #include "mipt/circuits/rppu_layer.hpp"
 #include "mipt/density.hpp"
+#include "mipt/entropy_resume.hpp"
 #include "mipt/free_energy.hpp"
 #include "mipt/free_energy_resume.hpp"
 #include "mipt/cusv/gates.hpp"
@@ -329,6 +331,30 @@ int ref_rho3_write(const char *path, const std::uint32_t *dims, std::uint64_t re
     }
     catch (...)
     {
+        return 1;
+    }
+}
+
+// entropy.exe's resume decision for the CSV at `path`: *completed, or 1 with
+// the refusal text when the reference refuses it.
+int ref_entropy_resume(const char *path, int n, int periods, double p, long requested, int circ_type,
+                       int max_s1_block, long *completed, char *message, int message_len)
+{
+    namespace r = mipt::entropy::resume;
+    try
+    {
+        r::RunIdentity id;
+        id.n = n;
+        id.periods = periods;
+        id.p = p;
+        id.requested_realizations = requested;
+        id.circ_type = circ_type;
+        *completed = r::load(path, id, max_s1_block).completed;
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        std::snprintf(message, static_cast<std::size_t>(message_len), "%s", e.what());
         return 1;
     }
 }

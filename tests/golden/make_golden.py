@@ -61,6 +61,43 @@ def xorshift_state(n, seed):
     return psi / np.linalg.norm(psi)
 
 
+def entropy_checkpoint_cases():
+    """entropy.exe result CSVs (its checkpoint) in the reference's layout, with
+    the run each is resumed by: (text, n, periods, p, requested, circ_type,
+    largest S1 block of the run)."""
+    head = ("N,periods,p,requested_realizations,completed_realizations,circ_type,circuit_name,fermionic_trace,L_A,"
+            "x,ln_x,S1_mean,S1_stddev,S1_stderr,S2_mean,S2_stddev,S2_stderr,subsystems_per_realization,"
+            "total_subsystems")
+    legacy = ("N,periods,p,requested_realizations,completed_realizations,circ_type,circuit_name,fermionic_trace,L_A,"
+              "x,ln_x,S2_mean,S2_stddev,S2_stderr,subsystems_per_realization,total_subsystems")
+
+    def rows(n, periods, p, requested, done, s1_upto, edit=None, old=False):
+        out = [legacy if old else head]
+        for kept in range(2, n // 2 + 1):
+            x = float((n / np.pi) * np.sin(np.pi * kept / n))
+            sd = 0.25
+            se = float(sd / np.sqrt(done)) if done > 1 else 0.0
+            if edit == kept:
+                se *= 1.5
+            s1 = f"{0.5 * kept!r},{sd!r},{se!r}" if kept <= s1_upto else "nan,nan,nan"
+            s2 = f"{0.4 * kept!r},{sd!r},{se!r}"
+            mid = s2 if old else f"{s1},{s2}"
+            out.append(f'{n},{periods},{p!r},{requested},{done},1,"Random Haar Unitary",0,{kept},{x!r},'
+                       f'{float(np.log(x))!r},{mid},{n},{n * done}')
+        return "\n".join(out) + "\n"
+
+    return [
+        (rows(8, 2, 0.1, 5, 2, 4), 8, 2, 0.1, 5, 1, 4),
+        (rows(8, 2, 0.1, 5, 5, 4), 8, 2, 0.1, 5, 1, 4),
+        (rows(8, 2, 0.1, 5, 2, 4), 8, 2, 0.1, 5, 1, 3),
+        (rows(8, 2, 0.1, 5, 3, 4, edit=3), 8, 2, 0.1, 5, 1, 4),
+        (rows(8, 2, 0.1, 5, 2, 4, old=True), 8, 2, 0.1, 5, 1, 4),
+        (rows(8, 2, 0.1, 5, 2, 4), 10, 2, 0.1, 5, 1, 5),
+        (rows(8, 2, 0.1, 5, 2, 4), 8, 2, 0.2, 5, 1, 4),
+        (rows(8, 2, 0.1, 5, 2, 2), 8, 2, 0.1, 5, 1, 2),
+    ]
+
+
 def fe_checkpoint_cases(lib):
     """free_energy.exe checkpoint pairs (samples CSV, time-series CSV, run
     parameters) in the reference's layout: a clean one, a killed flush, a
@@ -318,6 +355,24 @@ def main():
         out[f"rho3file{k}_real"] = real
         out[f"rho3file{k}_p"] = ps
         out[f"rho3file{k}_payload"] = payload
+
+    # --- entropy.exe checkpoints through the reference's own reader ----------
+    lib.ref_entropy_resume.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_long,
+                                       ctypes.c_int, ctypes.c_int, vp, ctypes.c_char_p, ctypes.c_int]
+    rows_e = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (text, n, periods, p, requested, circ, s1max) in enumerate(entropy_checkpoint_cases()):
+            path = os.path.join(tmp, f"e{k}.csv")
+            with open(path, "w") as f:
+                f.write(text)
+            done = np.zeros(1, np.int64)
+            msg = ctypes.create_string_buffer(1024)
+            rc = lib.ref_entropy_resume(path.encode(), n, periods, p, requested, circ, s1max, done.ctypes.data, msg,
+                                        1024)
+            out[f"entck{k}_text"] = np.array(text)
+            out[f"entck{k}_message"] = np.array(msg.value.decode().replace(tmp + os.sep, ""))
+            rows_e.append([n, periods, p, requested, circ, s1max, rc, int(done[0])])
+    out["entck_params"] = np.array(rows_e, np.float64)
 
     # --- free_energy.exe checkpoints through the reference's own readers ----
     lib.ref_fe_resume.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ctypes.c_int,

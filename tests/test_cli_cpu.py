@@ -411,3 +411,23 @@ def test_rho3_bin_matches_reference_writer(rho3_io, tmp_path, k):
                    periods=dims[3], realizations=dims[4], resolution=dims[5], p_min=0.125, p_max=0.875,
                    subsystem_qubits=subs, spatial_dimension=dims[0], grid_x=dims[6], grid_y=dims[7])
     assert (tmp_path / "py.bin").read_bytes() == want
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["entck_params"])))
+def test_entropy_resume_matches_reference_reader(exes, tmp_path, k):
+    """entropy.exe decides on eight checkpoints as the reference's own reader
+    (cpp/include/mipt/entropy_resume.hpp:102-246, recorded in the fixtures)
+    does: resume from the same completed count, finish, or refuse."""
+    n, periods, p, requested, circ, s1max, rc, done = GOLD["entck_params"][k]
+    n, periods, requested, circ, s1max, done = int(n), int(periods), int(requested), int(circ), int(s1max), int(done)
+    (tmp_path / "e.csv").write_text(str(GOLD[f"entck{k}_text"]))
+    ent = os.path.join(os.path.dirname(exes[0]), "entropy.exe")
+    env = {"CUDA_VISIBLE_DEVICES": "", "MIPT_ENTROPY_S1_MAX_LA": "0" if s1max >= n // 2 else str(s1max)}
+    r = run([ent, str(n), str(periods), repr(float(p)), str(requested), str(circ), "e.csv"], tmp_path, env)
+    if int(rc) != 0:
+        assert r.returncode == 1 and "Resume refused: e.csv" in r.stderr, (str(GOLD[f"entck{k}_message"]), r.stderr)
+    elif done == requested:
+        assert r.returncode == 0 and "e.csv is already complete. Nothing to do." in r.stdout, r.stdout + r.stderr
+    else:
+        assert f"Resuming from e.csv: {done}/{requested}" in r.stdout, r.stdout + r.stderr
+        assert "Resume refused" not in r.stderr
