@@ -170,7 +170,7 @@ struct Checkpoint
     int start_realization = 0;
 };
 
-[[noreturn]] void refuse(const std::string &why) { throw std::runtime_error("cannot resume: " + why); }
+[[noreturn]] void refuse(const std::string &why) { throw std::runtime_error("Resume refused: " + why); }
 
 Checkpoint load_checkpoint(const std::string &path, const std::string &expected_name, int realizations, int cycles,
                            const std::vector<std::string> &p_texts)
@@ -227,11 +227,13 @@ Checkpoint load_checkpoint(const std::string &path, const std::string &expected_
         {
             if (in_group != per_p)
                 refuse(path + " switches away from p=" + p_texts[group] + " after " + std::to_string(in_group) +
-                       " rows, but a complete p group holds realizations*cycles = " + std::to_string(per_p) + ".");
+                       " rows, but a complete p group holds realizations*cycles = " + std::to_string(per_p) +
+                       ". The file does not match this run's arguments.");
             ++group;
             if (group >= p_texts.size() || pt != p_texts[group])
                 refuse(path + " carries p=" + std::string(pt) + " where this run's grid expects " +
-                       (group < p_texts.size() ? p_texts[group] : std::string("no further values")) + ".");
+                       (group < p_texts.size() ? p_texts[group] : std::string("no further values")) +
+                       ". The file was produced with different p arguments.");
             in_group = 0;
         }
         ++in_group;

@@ -24,6 +24,7 @@
 //   CUDA-Q runtime)                             cpp/include/mipt/probed.hpp:103-108
 //   DensityMatrixWriter (rho3.bin version 2)   cpp/include/mipt/density.hpp:134-251
 //   entropy.exe's checkpoint reader            cpp/include/mipt/entropy_resume.hpp:102-246
+//   sim_tmi.exe's checkpoint reader            cpp/include/mipt/tmi/resume.hpp:188-330
 //   free_energy.exe's checkpoint readers (scan_samples, load_timeseries)
 //                                               cpp/include/mipt/free_energy_resume.hpp:246-534
 //   build_rppu_layers_with_boundary / fill_rppu_layer, build_rppu_layer_ops
@@ -33,6 +34,7 @@
 #include "mipt/circuits/rppu_layer.hpp"
 #include "mipt/density.hpp"
 #include "mipt/entropy_resume.hpp"
+#include "mipt/tmi/resume.hpp"
 #include "mipt/free_energy.hpp"
 #include "mipt/free_energy_resume.hpp"
 #include "mipt/cusv/gates.hpp"
@@ -331,6 +333,32 @@ int ref_rho3_write(const char *path, const std::uint32_t *dims, std::uint64_t re
     }
     catch (...)
     {
+        return 1;
+    }
+}
+
+// sim_tmi.exe's resume decision: out = loaded, name_verified, rows,
+// dropped_rows, kept_bytes, start_p_index, start_realization; or 1 with the
+// refusal text.
+int ref_tmi_resume(const char *output_path, const char *expected_name, int realizations, int cycles,
+                   const char *const *p_texts, int p_count, long *out, char *message, int message_len)
+{
+    try
+    {
+        std::vector<std::string> texts(p_texts, p_texts + p_count);
+        const auto ck = mipt::tmi::resume::load(output_path, expected_name, realizations, cycles, texts);
+        out[0] = ck.loaded ? 1 : 0;
+        out[1] = ck.name_verified ? 1 : 0;
+        out[2] = static_cast<long>(ck.rows);
+        out[3] = static_cast<long>(ck.dropped_rows);
+        out[4] = static_cast<long>(ck.kept_bytes);
+        out[5] = static_cast<long>(ck.start_p_index);
+        out[6] = ck.start_realization;
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        std::snprintf(message, static_cast<std::size_t>(message_len), "%s", e.what());
         return 1;
     }
 }

@@ -98,6 +98,34 @@ def entropy_checkpoint_cases():
     ]
 
 
+def tmi_checkpoint_cases():
+    """sim_tmi.exe `p,tmi` CSVs with the run resuming them: (file name, text,
+    n, realizations, resolution, p_min, p_max, all_cycles). The file names
+    follow the generated csv/tmi/<tag>/ naming or deliberately not."""
+    def p_text(v):
+        return format(float(v), ".17g")
+
+    def body(ps, per_p, extra=(), header="p,tmi"):
+        lines = [header]
+        for pv, count in zip(ps, per_p):
+            lines += [f"{p_text(pv)},{0.01 * i!r}" for i in range(count)]
+        lines += list(extra)
+        return "\n".join(lines) + "\n"
+
+    ps = np.linspace(0.1, 0.3, 2)
+    nm = "tmi_haar_n_8_real_3_0.1_0.3_res_2.csv"
+    nmc = "tmi_haarc_n_8_real_3_0.1_0.3_res_2.csv"
+    return [
+        (nm, body(ps, [3, 3]), 8, 3, 2, 0.1, 0.3, 0),
+        (nm, body(ps, [3, 1]), 8, 3, 2, 0.1, 0.3, 0),
+        (nmc, body(ps, [6, 3]), 8, 3, 2, 0.1, 0.3, 1),
+        (nm, body(ps, [3], extra=[f"{p_text(0.25)},0.5"]), 8, 3, 2, 0.1, 0.3, 0),
+        (nm, body(ps, [2], header="p,TMI"), 8, 3, 2, 0.1, 0.3, 0),
+        ("tmi_haar_n_12_real_3_0.1_0.3_res_2.csv", body(ps, [1]), 8, 3, 2, 0.1, 0.3, 0),
+        ("my_tmi.csv", body(ps, [3, 2]), 8, 3, 2, 0.1, 0.3, 0),
+    ]
+
+
 def fe_checkpoint_cases(lib):
     """free_energy.exe checkpoint pairs (samples CSV, time-series CSV, run
     parameters) in the reference's layout: a clean one, a killed flush, a
@@ -355,6 +383,30 @@ def main():
         out[f"rho3file{k}_real"] = real
         out[f"rho3file{k}_p"] = ps
         out[f"rho3file{k}_payload"] = payload
+
+    # --- sim_tmi.exe checkpoints through the reference's own reader ----------
+    lib.ref_tmi_resume.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
+                                   vp, ctypes.c_char_p, ctypes.c_int]
+    rows_t = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for k, (name, text, n, R, res, pmin, pmax, allc) in enumerate(tmi_checkpoint_cases()):
+            path = os.path.join(tmp, name)
+            with open(path, "w") as f:
+                f.write(text)
+            cycles = n // 4 if allc else 1
+            tag = "haarc" if allc else "haar"
+            expected = f"csv/tmi/{tag}/tmi_{tag}_n_{n}_real_{R}_{pmin:g}_{pmax:g}_res_{res}.csv"
+            texts = [format(float(v), ".17g").encode() for v in np.linspace(pmin, pmax, res)]
+            arr = (ctypes.c_char_p * len(texts))(*texts)
+            res_out = np.zeros(7, np.int64)
+            msg = ctypes.create_string_buffer(1024)
+            rc = lib.ref_tmi_resume(path.encode(), expected.encode(), R, cycles, ctypes.cast(arr, vp), len(texts),
+                                    res_out.ctypes.data, msg, 1024)
+            out[f"tmick{k}_name"] = np.array(name)
+            out[f"tmick{k}_text"] = np.array(text)
+            out[f"tmick{k}_message"] = np.array(msg.value.decode().replace(tmp + os.sep, ""))
+            rows_t.append([n, R, res, pmin, pmax, allc, rc, *res_out.tolist()])
+    out["tmick_params"] = np.array(rows_t, np.float64)
 
     # --- entropy.exe checkpoints through the reference's own reader ----------
     lib.ref_entropy_resume.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_long,

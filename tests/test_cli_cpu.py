@@ -431,3 +431,36 @@ def test_entropy_resume_matches_reference_reader(exes, tmp_path, k):
     else:
         assert f"Resuming from e.csv: {done}/{requested}" in r.stdout, r.stdout + r.stderr
         assert "Resume refused" not in r.stderr
+
+
+@pytest.mark.parametrize("k", range(len(GOLD["tmick_params"])))
+def test_sim_tmi_resume_matches_reference_reader(exes, tmp_path, k):
+    """sim_tmi.exe reads seven `p,tmi` checkpoints as the reference's own
+    reader (cpp/include/mipt/tmi/resume.hpp:188-330, recorded in the
+    fixtures) does: rows kept, partial circuit dropped, file truncated to the
+    same byte, the same restart point and name check, or the same refusal."""
+    n, R, res, pmin, pmax, allc, rc, loaded, verified, rows, dropped, kept, sp_, sr = GOLD["tmick_params"][k]
+    n, R, res, allc = int(n), int(R), int(res), int(allc)
+    name = str(GOLD[f"tmick{k}_name"])
+    text = str(GOLD[f"tmick{k}_text"])
+    path = tmp_path / name
+    path.write_text(text)
+    _, tmi = exes
+    r = run([tmi, str(n), "2", str(R), str(res), repr(float(pmin)), repr(float(pmax)), "1", str(allc), str(path)],
+            tmp_path, {"CUDA_VISIBLE_DEVICES": ""})
+    if int(rc) != 0:
+        msg = str(GOLD[f"tmick{k}_message"]).replace(name, str(path), 1)
+        assert r.returncode == 1 and msg in r.stderr, (msg, r.stderr)
+        return
+    total = res * R * (n // 4 if allc else 1)
+    if int(rows) >= total:
+        assert r.returncode == 0 and f"already holds all {total} TMI row(s)" in r.stderr, r.stderr
+        assert path.read_text() == text
+        return
+    line = f"RESUMED from {path}: {int(rows)} TMI row(s) already recorded"
+    if int(dropped) > 0:
+        line += f"; dropped {int(dropped)} row(s) of a partially written circuit"
+    assert line + "." in r.stderr, r.stderr
+    assert f"realization {int(sr)}/{R}." in r.stderr and f"Continuing at p[{int(sp_)}]=" in r.stderr
+    assert ("does not follow the generated naming convention" in r.stderr) == (not int(verified))
+    assert len(path.read_bytes()) == int(kept)
