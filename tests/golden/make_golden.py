@@ -2,9 +2,12 @@
 
 Runs in the development container only: it loads oracle/_ref/libmipt_ref.so,
 which oracle/ref/build_ref.sh compiles from the reference checkout's headers
-(the reference's samplers, bond-matrix builders, measurement primitive,
-reduced-density and entropy code). The fixtures it writes are what the CPU
-oracle and the product are pinned to on machines without the reference.
+(the reference's samplers -- Haar, probed-workspace and RPPU/qRPPU layer draws
+and the free-energy initial states --, bond-matrix builders, measurement
+primitive, reduced-density and entropy code, the rho3.bin writer and the
+checkpoint readers of free_energy.exe, entropy.exe and sim_tmi.exe). The
+fixtures it writes are what the CPU oracle and the product are pinned to on
+machines without the reference.
 
     python tests/golden/make_golden.py
 """
