@@ -62,11 +62,12 @@ int mipt_cuda_renyi2_f32(const void *device_state_vector, int n_qubits, const in
 
 /* mipt_cuda_renyi2_f32 without any device allocation. No reference
  * counterpart. Scratch is a static 512 KiB array per device, so
- * kept_count <= 14; larger requests return MIPT_GB300_E_INVALID. The first
- * call on a device (with that device current) looks up the array's address
- * once and should come before any stream capture. The array is shared by all
- * calls on a device: calls that overlap on the GPU race, so callers serialise
- * them. */
+ * kept_count <= 14; larger requests return MIPT_GB300_E_INVALID. Every call
+ * (with the caller's device current) looks up the array's address in the
+ * current context. No call may be made during a stream capture: each call
+ * copies synchronously and clears on the legacy default stream. The array is
+ * shared by all calls on a device: calls that overlap on the GPU race, so
+ * callers serialise them. */
 int mipt_gb300_renyi2_f32_noalloc(const void *device_state_vector, int n_qubits, const int *host_kept_modes,
                                   int kept_count, int fermion_trace, double *entropy_out);
 

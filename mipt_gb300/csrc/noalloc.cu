@@ -11,10 +11,16 @@
 //     purity 8 B, tile partials 8 * 32,896 B at n_kept = 14; n_kept = 15
 //     would need 1,050,624 B). Larger requests are rejected with
 //     MIPT_GB300_E_INVALID before any device work.
-//   - Set-up: the first call on a device, with that device current, looks up
-//     the array's device address once (cudaGetSymbolAddress) and keeps it in
-//     a per-device table. That first call should come before any stream
-//     capture on the device.
+//   - Set-up: every call, with the caller's device current, looks up the
+//     array's device address (cudaGetSymbolAddress) and checks the return
+//     code before any launch. The lookup is cheap next to the call's copies,
+//     and it never hands out an address cached from an earlier context (a
+//     device reset, or another context on the same ordinal, reloads the
+//     module at a possibly different address).
+//   - No call may be made while a stream capture is active on the device:
+//     the job record and the purity travel by synchronous cudaMemcpy and the
+//     purity slot is cleared on the legacy default stream, which the CUDA
+//     runtime forbids during capture (it would invalidate the capture).
 //   - Nothing in the array needs to start at zero: every word a kernel reads
 //     is written earlier in the same call (job record by the host copy, tile
 //     partials by the Gram kernel, purity by the row sum). The purity slot is
@@ -28,7 +34,6 @@
 
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -58,27 +63,14 @@ static_assert(kTileOffset + sizeof(double) * tiles_of(kMaxKept + 1) > kScratchBy
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 256;
-std::mutex g_table_mu;
-void *g_table[kMaxDevices] = {};
-
-// Device address of the static scratch on the current device, looked up on
-// the first call for that device.
+// Device address of the static scratch in the current context, looked up on
+// every call.
 int scratch_address(unsigned char **out)
 {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return api_cuda_fail(e, "cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices) return api_fail(MIPT_GB300_E_INVALID, "device ordinal beyond 255");
-    std::lock_guard<std::mutex> lock(g_table_mu);
-    if (!g_table[dev])
-    {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return api_cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
-        g_table[dev] = p;
-    }
-    *out = static_cast<unsigned char *>(g_table[dev]);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return api_cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+    *out = static_cast<unsigned char *>(p);
     return 0;
 }
 } // namespace

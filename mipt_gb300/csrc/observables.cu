@@ -779,8 +779,14 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
     if (sizeof(double) * static_cast<std::size_t>(tiles) * njobs > scratch_bytes) return cudaErrorInvalidValue;
     const std::uint64_t E = 1ull << (n - k);
     dim3 grid(tiles, 1, njobs);
-    k_gram<float, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
-                                                        static_cast<double *>(scratch));
+    // From n = 20 the products run in FP32 runs of 64 into FP64 totals, as in
+    // gram_rho; below that every product is summed in FP64.
+    if (n >= 20)
+        k_gram<float, double, true><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
+                                                                  static_cast<double *>(scratch));
+    else
+        k_gram<float, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
+                                                            static_cast<double *>(scratch));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);

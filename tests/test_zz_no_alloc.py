@@ -1,12 +1,16 @@
 """Allocation-free FP32 Renyi-2 (mipt_gb300_renyi2_f32_noalloc) against the
-allocating entry point (mipt_cuda_renyi2_f32), both through the C ABI.
+allocating entry point (mipt_cuda_renyi2_f32), both through the C ABI, and
+against the CPU FP64 oracle (the state's reduced density matrix and its
+Renyi-2 entropy, computed on the host from the same amplitudes).
 
 Tolerance: 1e-5 bits, the FP32 path's entropy bound. Each case calls the
 allocation-free entry point twice in a row; both results must agree with
-the allocating entry point, and with each other exactly (every reduction
-runs in a fixed order). The file name sorts last so that the module also
-runs after every other test in the same process; it needs no state from
-them and passes alone in a fresh process.
+the allocating entry point and the oracle, and with each other exactly
+(every reduction runs in a fixed order). Free device memory is read around
+the second and third calls: after the first call has loaded the kernels,
+a call changes it by nothing. The file name sorts last so that the module
+also runs after every other test in the same process; it needs no state
+from them and passes alone in a fresh process.
 """
 import ctypes
 
@@ -63,15 +67,48 @@ CASES = [
 ]
 
 
+def oracle_renyi2(psi, kept, ferm):
+    from oracle import pyoracle as orc
+    # The device state holds FP32 amplitudes: the oracle reads the same ones.
+    psi32 = psi.astype(np.complex64).astype(np.complex128)
+    return orc.entropy(orc.rdm(psi32, kept, ferm), 2)
+
+
+def free_device_bytes():
+    free = ctypes.c_size_t()
+    total = ctypes.c_size_t()
+    rt = ctypes.CDLL("libcudart.so.13")
+    rt.cudaMemGetInfo.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
 @pytest.mark.parametrize("n,kept,ferm", CASES)
 def test_noalloc_matches_allocating_entry_point(mg, n, kept, ferm):
-    e = fp32_state(mg, random_state(n, 1000 + n))
+    psi = random_state(n, 1000 + n)
+    e = fp32_state(mg, psi)
     want = mg.renyi2(e.data, n, kept, ferm, False)
     first = noalloc(mg, e.data, n, kept, ferm)
     second = noalloc(mg, e.data, n, kept, ferm)
     assert abs(first - want) < TOL, (first, want)
     assert abs(second - want) < TOL, (second, want)
     assert first == second
+    if n <= 20:
+        ref = oracle_renyi2(psi, kept, ferm)
+        assert abs(first - ref) < TOL, (first, ref)
+
+
+def test_noalloc_changes_no_device_memory(mg):
+    """After the first call, calls leave the device's free memory unchanged."""
+    n, kept = 18, list(range(3, 17))
+    e = fp32_state(mg, random_state(n, 99))
+    noalloc(mg, e.data, n, kept, False)  # first call: kernels load here
+    before = free_device_bytes()
+    a = noalloc(mg, e.data, n, kept, False)
+    b = noalloc(mg, e.data, n, [1, 4, 9], True)
+    after = free_device_bytes()
+    assert before == after, (before, after)
+    assert np.isfinite(a) and np.isfinite(b)
 
 
 def test_noalloc_interleaved_sizes(mg):
