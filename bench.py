@@ -200,6 +200,27 @@ def run_gb300(args):
                      tile_qubits=args.tile)
     seeds = seeds_for(rank, B)
     ps = p_for(B)
+    # |dS| against the CPU FP64 oracle: trajectories 0 and 9 of the batch run
+    # free (48 layers) on host threads while the GPU is timed.
+    oracle_idx = [i for i in (0, 9) if i < B] if (rank == 0 and not args.kernels_only) else []
+    oracle_res = {}
+
+    def oracle_leg(i):
+        from oracle import pyoracle as orc
+        r = orc.run_trajectory(int(seeds[i]), N_QUBITS, PERIODS, float(ps[i]), True, 16, want_state=True)
+        m = r["psi"].reshape(-1, 1 << (N_QUBITS // 2))
+        g = m.conj().T @ m
+        d = orc.haar_draw(int(seeds[i]), N_QUBITS, PERIODS, float(ps[i]), True, 16)
+        oc = np.zeros(T, np.uint64)
+        for t in range(T):
+            for j, q in enumerate(d["sites"][t, : d["sites_per_layer"][t]]):
+                if r["outcomes"][t, j]:
+                    oc[t] |= np.uint64(1) << np.uint64(int(q))
+        oracle_res[i] = (-np.log2(float(np.sum(np.abs(g) ** 2))), oc)
+
+    oracle_threads = [threading.Thread(target=oracle_leg, args=(i,), daemon=True) for i in oracle_idx]
+    for th in oracle_threads:
+        th.start()
 
     # ---------------------------------------------------------- value
     batch.prepare(seeds, ps)
@@ -224,6 +245,12 @@ def run_gb300(args):
     batch.set_profiling(False)
     ms = max_over_ranks(ms, dist, "cuda")
     value = whole_job_rate(B, T, world, args.steps, ms / 1000.0)
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"kernels_only": True, "value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
+                              "kernel_ms_per_step": {k: v[0] for k, v in stats.items()}}), flush=True)
+        batch.close()
+        return 0
 
     # ------------------------------------------------------------ e2e
     for _ in range(1):
@@ -272,17 +299,58 @@ def run_gb300(args):
                 "tensor_pipe_source": "ncu sm__pipe_tensor_cycles_active, 2-trajectory capture of the same kernel "
                                       "(profiles/k_gram_tc_L24_halfcut_batch2.md)"}
 
-        # Plain FP64 per-trajectory path on the same GPU, one trajectory.
+        # Plain FP64 per-trajectory path on the same GPU, one trajectory:
+        # device time (CUDA events around the execute, as for `value`) and
+        # end to end (host sampling, upload, run, fetch).
         plain = mg.Batch(N_QUBITS, PERIODS, capacity=1, fp64=True, observables=mg.OBS_S2_HALF)
         plain.run(seeds[:1], ps[:1])
+        plain.prepare(seeds[:1], ps[:1])
         torch.cuda.synchronize()
+        start.record()
+        plain.execute()
+        stop.record()
+        torch.cuda.synchronize()
+        plain_dev_s = start.elapsed_time(stop) / 1000.0
+        pr = plain.fetch()
         t0 = time.perf_counter()
-        pr = plain.run(seeds[:1], ps[:1])
-        plain_s = time.perf_counter() - t0
-        plain_value = T / plain_s
-        same = bool(np.array_equal(pr["outcomes"][0], out["outcomes"][0]))
-        ds = abs(float(pr["obs"][0, 0, 1]) - float(out["obs"][0, 0, 1]))
+        plain.run(seeds[:1], ps[:1])
+        plain_e2e_s = time.perf_counter() - t0
+        plain_value = T / plain_dev_s
         plain.close()
+
+        # Per-layer observables: the half-chain S_2 after every layer (one
+        # step, device time), with the share of the Gram.
+        per_layer = None
+        if args.per_layer:
+            pl = mg.Batch(N_QUBITS, PERIODS, capacity=B, fp64=False, observables=mg.OBS_S2_HALF, observe_every=1,
+                          tile_qubits=args.tile)
+            pl.run(seeds, ps)
+            pl.prepare(seeds, ps)
+            pl.set_profiling(True)
+            torch.cuda.synchronize()
+            start.record()
+            pl.execute()
+            stop.record()
+            torch.cuda.synchronize()
+            pl_ms = start.elapsed_time(stop)
+            pl_out = pl.fetch()
+            pl_stats = pl.kernel_stats()
+            pl.set_profiling(False)
+            t0 = time.perf_counter()
+            pl.run(seeds_for(rank, B, 99), ps)
+            pl_e2e = time.perf_counter() - t0
+            per_layer = {"value": whole_job_rate(B, T, world, 1, pl_ms / 1000.0), "unit": UNIT,
+                         "observables": "half-chain Renyi-2 entropy after every layer",
+                         "ms_per_step": pl_ms, "kernel_ms_per_step": {k: v[0] for k, v in pl_stats.items()},
+                         "gram_share": pl_stats["observables"][0] / pl_ms,
+                         "e2e": {"value": whole_job_rate(B, T, world, 1, pl_e2e), "unit": UNIT},
+                         "same_final_S2_as_headline": bool(abs(pl_out["obs"][0, -1, 1] - out["obs"][0, 0, 1]) < 1e-9)}
+            pl.close()
+
+        for th in oracle_threads:
+            th.join()
+        ds_vals = [abs(oracle_res[i][0] - float(out["obs"][i, 0, 1])) for i in oracle_idx if i in oracle_res]
+        same = all(np.array_equal(oracle_res[i][1], out["outcomes"][i]) for i in oracle_idx if i in oracle_res)
 
         cpu = cpu_sample(1) if world == 1 else None
         line = {
@@ -292,10 +360,18 @@ def run_gb300(args):
             "config": workload_config(B), "roofline": roofline, "gram": gram, "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clocks.summary(),
-            "plain_fp64": {"value": plain_value, "unit": UNIT, "path": "FP64 state, one trajectory per launch sequence",
-                           "speedup_batched_fp32": value / plain_value},
-            "dS": {"max_abs": ds, "same_outcomes": same, "observable": "final half-chain S_2, trajectory 0"},
+            "plain_fp64": {"value": plain_value, "unit": UNIT,
+                           "path": "FP64 state, one trajectory per launch sequence, device time",
+                           "e2e": {"value": T / plain_e2e_s, "unit": UNIT},
+                           "speedup_batched_fp32": value / plain_value,
+                           "same_final_S2_as_batched": bool(abs(pr["obs"][0, 0, 1] - out["obs"][0, 0, 1]) < 1e-5)},
+            "dS": {"max_abs": max(ds_vals) if ds_vals else None, "same_outcomes": bool(same),
+                   "reference": "CPU FP64 oracle, free running",
+                   "observable": f"final half-chain S_2 of trajectories {oracle_idx} (p = "
+                                 f"{[round(float(ps[i]), 3) for i in oracle_idx]}), 48 layers"},
         }
+        if per_layer is not None:
+            line["per_layer_observables"] = per_layer
         print(json.dumps(line), flush=True)
     batch.close()
     if dist:
@@ -352,23 +428,30 @@ def config0():
 
 def config1():
     """Free-fermion covariance, N = 128, depth 256, 500 trajectories per p in
-    {0.1, 0.2, 0.3}; entropies of every block [0, l) and TMI of the quarters."""
+    {0.1, 0.2, 0.3}; entropies of every block [0, l) and TMI of the quarters.
+    The configuration's plain method is FP64 Gamma (`value`); the FP32
+    evolution (FP64 denominators, re-purification, eigensolves) is reported
+    beside it."""
     import mipt_gb300 as mg
     from oracle import pyoracle as orc
     N, depth, per_p = 128, 256, 500
     ps = np.repeat([0.1, 0.2, 0.3], per_p)
     seeds = np.array([mg.trajectory_seed(1, i) for i in range(len(ps))], np.uint64)
     blocks = list(range(1, N + 1))
-    mg.ff_run(seeds[:8], ps[:8], N, depth, blocks=blocks)
-    out, dt = _timed(lambda: mg.ff_run(seeds, ps, N, depth, blocks=blocks))
     ref = orc.ff_trajectory(int(seeds[0]), N, depth, float(ps[0]), True, 64, blocks=blocks, want_gamma=False)
-    ds = float(np.max(np.abs(out["s_blocks"][0] - ref["s_blocks"])))
+    res = {}
+    for fp64 in (True, False):
+        mg.ff_run(seeds[:8], ps[:8], N, depth, blocks=blocks, fp64=fp64)
+        out, dt = _timed(lambda: mg.ff_run(seeds, ps, N, depth, blocks=blocks, fp64=fp64))
+        res[fp64] = {"value": len(ps) * depth / dt, "seconds": dt,
+                     "max_abs_dS_vs_oracle_traj0": float(np.max(np.abs(out["s_blocks"][0] - ref["s_blocks"]))),
+                     "same_outcomes_traj0": bool(np.array_equal(out["outcomes"][0], ref["outcomes"]))}
     threads = orc.max_threads()
     sample = list(range(threads))
     _, cdt = _oracle_pool(lambda i: orc.ff_trajectory(int(seeds[i]), N, depth, float(ps[i]), True, 64,
                                                        blocks=blocks, want_gamma=False), sample, threads)
     return {"config": "1: free fermions N=128 (256 Majoranas), depth 256, 1500 trajectories, all prefix blocks + TMI",
-            "value": len(ps) * depth / dt, "unit": UNIT, "max_abs_dS_vs_oracle_traj0": ds,
+            "value": res[True]["value"], "unit": UNIT, "dtype": "f64", "fp64": res[True], "fp32": res[False],
             "cpu_baseline": {"value": len(sample) * depth / cdt, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{len(sample)} trajectories, FP64 oracle"}}
 
@@ -376,7 +459,10 @@ def config1():
 def config2():
     """4096 trajectories, L uniform on {16, 18, 20, 22}, p from 16 values in
     [0.05, 0.35], periodic, depth 2L, FP32; per-layer half-chain S_2 and (L a
-    multiple of 4) TMI of the quarters from S_2. Each length runs as one batch."""
+    multiple of 4) TMI of the quarters from S_2. The four lengths run as the
+    branches of one CUDA graph (one launch per step). The configuration's
+    per-layer half-chain S_vN (FP64 eigensolves of 256..2048-row spectra) is
+    timed on a bounded sample beside it."""
     import mipt_gb300 as mg
     rng = np.random.default_rng(2)
     total = 4096
@@ -388,10 +474,44 @@ def config2():
         idx = np.nonzero(Ls == L)[0]
         obs = mg.OBS_S2_HALF | (mg.OBS_TMI_S2 if L % 4 == 0 else 0)
         groups.append((L, idx, mg.Batch(L, L, capacity=len(idx), fp64=False, observables=obs, observe_every=1)))
-    for L, idx, b in groups:
-        b.run(seeds[idx[:8]], ps[idx[:8]])
-    _, dt = _timed(lambda: [b.run(seeds[idx], ps[idx]) for L, idx, b in groups])
+    graph = mg.BatchGroup([b for _, _, b in groups])
+
+    def step():
+        for L, idx, b in groups:
+            b.prepare(seeds[idx], ps[idx])
+        graph.execute()
+        return [b.fetch() for _, _, b in groups]
+
+    step()  # normal execute + capture
+    step()
+    _, dt = _timed(step)
     units = int(sum(2 * L * len(idx) for L, idx, b in groups))
+    graph.close()
+    for _, _, b in groups:
+        b.close()
+    # Per-layer half-chain S_vN on a sample: the first 16 trajectories of the
+    # two shorter lengths, one graph, FP64 eigensolves (256 and 512 rows; one
+    # CTA per spectrum, so the 1024- and 2048-row spectra of L = 20 and 22 take
+    # about 1 s and 8 s per layer at any batch size and are left out).
+    svn_groups = []
+    for L in (16, 18):
+        idx = np.nonzero(Ls == L)[0][:16]
+        svn_groups.append((L, idx, mg.Batch(L, L, capacity=len(idx), fp64=False, observables=mg.OBS_SVN_HALF,
+                                            observe_every=1)))
+    sg = mg.BatchGroup([b for _, _, b in svn_groups])
+
+    def svn_step():
+        for L, idx, b in svn_groups:
+            b.prepare(seeds[idx], ps[idx])
+        sg.execute()
+        return [b.fetch() for _, _, b in svn_groups]
+
+    svn_step()
+    _, svn_dt = _timed(svn_step)
+    svn_units = int(sum(2 * L * len(idx) for L, idx, b in svn_groups))
+    sg.close()
+    for _, _, b in svn_groups:
+        b.close()
     # plain FP64 per-trajectory arm on a sample
     plain_units, plain_t = 0, 0.0
     for L in (16, 22):
@@ -404,7 +524,10 @@ def config2():
         plain_t += t
         pb.close()
     return {"config": "2: 4096 trajectories, L uniform on {16,18,20,22}, depth 2L, FP32, per-layer S_2 (+TMI_S2 for L%4==0)",
-            "value": units / dt, "unit": UNIT, "trajectory_layers": units,
+            "value": units / dt, "unit": UNIT, "trajectory_layers": units, "execution": "one CUDA graph, 4 branches",
+            "per_layer_svn_sample": {"value": svn_units / svn_dt, "unit": UNIT, "trajectory_layers": svn_units,
+                                     "sample": "16 trajectories each of L = 16 and 18, half-chain S_vN after every "
+                                               "layer (FP64 eigensolver, 256 and 512 rows)"},
             "plain_fp64_per_trajectory": {"value": plain_units / plain_t, "unit": UNIT,
                                           "sample": "one L=16 and one L=22 trajectory"},
             "speedup_vs_plain_fp64": (units / dt) / (plain_units / plain_t)}
@@ -576,6 +699,10 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tile", type=int, default=0, help="local qubits per pass tile (0 = library default)")
     ap.add_argument("--config", type=int, default=-1, help="measure workload configuration 0..6 instead")
+    ap.add_argument("--per-layer", dest="per_layer", type=int, default=1,
+                    help="also time the workload with the half-chain S_2 after every layer (1 = on)")
+    ap.add_argument("--kernels-only", dest="kernels_only", action="store_true",
+                    help="time the batched device run only (for profiler captures)")
     args = ap.parse_args()
     if args.config >= 0:
         return run_config(args.config)

@@ -237,6 +237,15 @@ int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, 
                              int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count);
 void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
 
+/* Test hook for the bounded device waits (no reference counterpart; the
+ * reference's failure contract is its status ladder, cpp/src/cuda/tmi_cuda_svd.cu:203-215).
+ * The next `count` FP32 pass launches that load tiles by TMA do not issue the
+ * first tile load of their first CTA. That CTA's wait for the tile gives up
+ * after well under a second, it returns without leaving a copy in flight,
+ * and the batch's fetch reports MIPT_GB300_E_INTERNAL ("tile load wait timed
+ * out"). The device stays usable: the next execute runs normally. */
+int mipt_gb300_test_withhold_tile_loads(int count);
+
 /* Draw `count` trajectories (trajectory i from seeds[i] with measurement
  * rate p[i]) on host threads exactly as the reference's HaarCircuit1D
  * (cpp/include/mipt/circuit.hpp:129-140,415-439) -- or, for circuit 2/4, its
@@ -273,6 +282,25 @@ int mipt_gb300_batch_set_observation_steps(mipt_gb300_batch *batch, const int *s
 /* Run every layer of the prepared batch on the device, asynchronously on
  * `stream` (a cudaStream_t; NULL = default stream). */
 int mipt_gb300_batch_execute(mipt_gb300_batch *batch, void *stream);
+/* mipt_gb300_batch_execute through a CUDA graph (no reference counterpart;
+ * the reference runs trajectories one at a time,
+ * cpp/include/mipt/tmi/runner.hpp:269-378). The first call, and any call
+ * after the batch's structure changed (trajectory count, which layers measure
+ * and in how many chunks, forced outcomes, observation schedule, regions),
+ * runs a normal execute and then captures a second one on a private stream;
+ * later calls replay the captured graph with one launch. Batches whose initial
+ * states were uploaded, or with profiling on, run a normal execute. */
+int mipt_gb300_batch_execute_graph(mipt_gb300_batch *batch, void *stream);
+
+/* Several batches (for example one per chain length of a mixed-length
+ * workload) executed as the parallel branches of one CUDA graph, replayed
+ * with one launch per call under the same rules as
+ * mipt_gb300_batch_execute_graph. Results are fetched per batch. The group
+ * does not own its batches; destroy it before them. */
+typedef struct mipt_gb300_batch_group mipt_gb300_batch_group;
+int mipt_gb300_batch_group_create(mipt_gb300_batch *const *batches, int count, mipt_gb300_batch_group **out);
+int mipt_gb300_batch_group_execute(mipt_gb300_batch_group *group, void *stream);
+void mipt_gb300_batch_group_destroy(mipt_gb300_batch_group *group);
 /* Wait for the batch and copy results to host (each pointer nullable):
  *   measured[count][layers], outcomes[count][layers]  site bit masks
  *   surprisal[count][layers]                          -log P per layer
@@ -407,6 +435,8 @@ typedef struct mipt_gb300_ff_config
     int n_blocks;         /* entropies of the mode blocks [0, block_len[i]) */
     const int *block_len;
     int host_threads;     /* sampler threads, 0 = all */
+    int fp64;             /* 1: Gamma evolves in FP64 (the plain method); 0: FP32 with FP64
+                           * denominators, re-purification and eigensolves */
 } mipt_gb300_ff_config;
 
 /* Runs `count` trajectories (seeds[i], rate p[i]). forced (nullable,

@@ -32,7 +32,7 @@ class MiptError(RuntimeError):
 class FFConfig(ctypes.Structure):
     _fields_ = [("n_modes", ctypes.c_int), ("depth", ctypes.c_int), ("closed", ctypes.c_int),
                 ("repurify_every", ctypes.c_int), ("n_blocks", ctypes.c_int),
-                ("block_len", ctypes.POINTER(ctypes.c_int)), ("host_threads", ctypes.c_int)]
+                ("block_len", ctypes.POINTER(ctypes.c_int)), ("host_threads", ctypes.c_int), ("fp64", ctypes.c_int)]
 
 
 class BatchConfig(ctypes.Structure):
@@ -112,6 +112,12 @@ def lib():
     L.mipt_gb300_trajectory_seed.restype = u64
     L.mipt_gb300_draw_haar.argtypes = [u64, ci, ci, cd, ci, ci, vp, vp, vp, vp, vp, vp]
     L.mipt_gb300_ff_run.argtypes = [ctypes.POINTER(FFConfig), vp, vp, ci, vp, vp, vp, vp, vp, vp]
+    L.mipt_gb300_batch_execute_graph.argtypes = [vp, vp]
+    L.mipt_gb300_batch_group_create.argtypes = [vp, ci, ctypes.POINTER(vp)]
+    L.mipt_gb300_batch_group_execute.argtypes = [vp, vp]
+    L.mipt_gb300_batch_group_destroy.argtypes = [vp]
+    L.mipt_gb300_batch_group_destroy.restype = None
+    L.mipt_gb300_test_withhold_tile_loads.argtypes = [ci]
     _lib = L
     return L
 
@@ -365,6 +371,10 @@ class Batch:
     def execute(self, stream=None):
         _check(lib().mipt_gb300_batch_execute(self._h, stream))
 
+    def execute_graph(self, stream=None):
+        """execute() through a captured CUDA graph (one launch once captured)."""
+        _check(lib().mipt_gb300_batch_execute_graph(self._h, stream))
+
     def fetch(self):
         c, T = self.count, self.layers
         measured = np.zeros((c, T), np.uint64)
@@ -418,6 +428,31 @@ class Batch:
     @property
     def launches(self):
         return lib().mipt_gb300_batch_launches(self._h)
+
+
+class BatchGroup:
+    """Batches executed as the parallel branches of one CUDA graph."""
+
+    def __init__(self, batches):
+        self.batches = list(batches)
+        arr = (ctypes.c_void_p * len(self.batches))(*[b._h.value for b in self.batches])
+        h = ctypes.c_void_p()
+        _check(lib().mipt_gb300_batch_group_create(arr, len(self.batches), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().mipt_gb300_batch_group_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def execute(self, stream=None):
+        _check(lib().mipt_gb300_batch_group_execute(self._h, stream))
 
     def set_profiling(self, enable=True):
         _check(lib().mipt_gb300_batch_set_profiling(self._h, int(enable)))
@@ -530,14 +565,15 @@ def outcomes_to_mask(sites, outcomes):
 
 # ----------------------------------------------------------- free fermions
 def ff_run(seeds, p, n_modes, depth, closed=True, repurify_every=64, blocks=(), tmi=True, forced=None,
-           want_gamma=False, host_threads=0):
-    """Monitored free-fermion trajectories on the Majorana covariance matrix."""
+           want_gamma=False, host_threads=0, fp64=False):
+    """Monitored free-fermion trajectories on the Majorana covariance matrix
+    (fp64: Gamma evolves in FP64, the plain method)."""
     seeds = np.ascontiguousarray(seeds, np.uint64)
     c = len(seeds)
     p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, np.float64), seeds.shape))
     bl = np.ascontiguousarray(blocks, np.int32)
     cfg = FFConfig(n_modes, depth, int(closed), repurify_every, len(bl),
-                   bl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if len(bl) else None, host_threads)
+                   bl.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if len(bl) else None, host_threads, int(fp64))
     outcomes = np.zeros((c, depth, n_modes), np.int32)
     probs = np.zeros((c, depth, n_modes))
     gamma = np.zeros((c, 2 * n_modes, 2 * n_modes)) if want_gamma else None

@@ -22,7 +22,7 @@ APP_TARGETS = [("mipt.cpp", "mipt.exe"), ("sim_tmi.cpp", "sim_tmi.exe"), ("gmn.c
                ("entropy.cpp", "entropy.exe"), ("free_energy.cpp", "free_energy.exe")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["engine.cu", "observables.cu", "capi.cu", "fermion.cu", "noalloc.cu", "parity.cu", "gmn.cu", "mlp.cu"]
+CUDA_SOURCES = ["engine.cu", "observables.cu", "eigen.cu", "capi.cu", "fermion.cu", "noalloc.cu", "parity.cu", "gmn.cu", "mlp.cu"]
 CXX_SOURCES = ["sampler.cpp"]
 
 
@@ -81,7 +81,7 @@ def build(force=False, verbose=False, ptxas_info=False):
                     print(log)
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcusolver", "-lpthread"]
+        cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"]
         _compile(cmd)
         os.replace(tmp, LIB)
     build_apps(force)

@@ -7,7 +7,6 @@
 #include "sampler.hpp"
 
 #include <cuda_runtime.h>
-#include <cusolverDn.h>
 
 #include <algorithm>
 #include <atomic>
@@ -104,6 +103,59 @@ struct PinnedBuf
     template <typename T> T *as() { return static_cast<T *>(p); }
 };
 
+// Pinned staging for the small host tables an execute uploads (Gram job
+// records, output slots). Each upload takes the next chunk in call order; the
+// chunks live until the owner is destroyed, so a captured CUDA graph can copy
+// from them on every replay. A chunk is rewritten only when its content
+// changes, after the device has finished any earlier copy out of it.
+struct PinnedArena
+{
+    std::vector<std::pair<void *, std::size_t>> blocks;
+    std::size_t block = 0, off = 0;
+    PinnedArena() = default;
+    PinnedArena(const PinnedArena &) = delete;
+    PinnedArena &operator=(const PinnedArena &) = delete;
+    ~PinnedArena()
+    {
+        for (auto &b : blocks) cudaFreeHost(b.first);
+    }
+    void rewind()
+    {
+        block = 0;
+        off = 0;
+    }
+    cudaError_t stage(const void *src, std::size_t bytes, void **out)
+    {
+        const std::size_t need = (std::max<std::size_t>(bytes, 1) + 255) & ~std::size_t{255};
+        while (block < blocks.size() && off + need > blocks[block].second)
+        {
+            ++block;
+            off = 0;
+        }
+        if (block == blocks.size())
+        {
+            void *p = nullptr;
+            const std::size_t sz = std::max<std::size_t>(need, std::size_t{1} << 20);
+            cudaError_t e = cudaMallocHost(&p, sz);
+            if (e != cudaSuccess) return e;
+            std::memset(p, 0, sz);
+            blocks.push_back({p, sz});
+            off = 0;
+        }
+        unsigned char *h = static_cast<unsigned char *>(blocks[block].first) + off;
+        off += need;
+        if (std::memcmp(h, src, bytes) != 0)
+        {
+            // An earlier execute may still be copying out of this chunk.
+            cudaError_t e = cudaDeviceSynchronize();
+            if (e != cudaSuccess) return e;
+            std::memcpy(h, src, bytes);
+        }
+        *out = h;
+        return cudaSuccess;
+    }
+};
+
 __global__ void k_fill_double(double *p, std::size_t n, double v)
 {
     for (std::size_t i = blockIdx.x * static_cast<std::size_t>(blockDim.x) + threadIdx.x; i < n;
@@ -156,27 +208,6 @@ __global__ void k_scatter(const double *in, const int *idx, int n, double *out, 
 
 // S = -sum lambda log2 lambda over lambda > 1e-15 (fixed-order reduction).
 // Block b: entropy (bits) of the spectrum w[b*d .. b*d + d) into out[b].
-__global__ void k_entropy_from_eigs(const double *w, int d, double *out)
-{
-    __shared__ double red[256];
-    w += static_cast<std::size_t>(blockIdx.x) * d;
-    out += blockIdx.x;
-    double s = 0.0;
-    for (int i = threadIdx.x; i < d; i += blockDim.x)
-    {
-        const double l = w[i];
-        if (l > 1e-15) s -= l * log2(l);
-    }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int k = blockDim.x / 2; k > 0; k /= 2)
-    {
-        if (threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[0] = fabs(red[0]) < 1e-12 ? 0.0 : red[0];
-}
-
 // ------------------------------------------------------------ entropies
 
 struct EntReq
@@ -190,15 +221,15 @@ struct EntReq
 
 struct Workspace
 {
-    DevBuf jobs, rho, scratch, vals, idx, eig, work, info, err, rows;
-    cusolverDnHandle_t solver = nullptr;
-    cusolverDnParams_t params = nullptr;
-    std::vector<char> host_work;
-    bool batched_eig_failed = false;
-    ~Workspace()
+    DevBuf jobs, rho, scratch, vals, idx, eig, err, eig_err, rows;
+    PinnedArena stage;
+    // Host -> device copy of a small table through the pinned staging arena.
+    cudaError_t upload(void *dst, const void *src, std::size_t bytes, cudaStream_t s)
     {
-        if (params) cusolverDnDestroyParams(params);
-        if (solver) cusolverDnDestroy(solver);
+        void *h = nullptr;
+        cudaError_t e = stage.stage(src, bytes, &h);
+        if (e != cudaSuccess) return e;
+        return cudaMemcpyAsync(dst, h, bytes, cudaMemcpyHostToDevice, s);
     }
 };
 
@@ -237,8 +268,8 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
             for (auto *r : list) idx.push_back(r->out);
             MG_CUDA(ws.vals.ensure(sizeof(double) * zeros.size()));
             MG_CUDA(ws.idx.ensure(sizeof(int) * idx.size()));
-            MG_CUDA(cudaMemcpyAsync(ws.vals.p, zeros.data(), sizeof(double) * zeros.size(), cudaMemcpyHostToDevice, s));
-            MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, s));
+            MG_CUDA(ws.upload(ws.vals.p, zeros.data(), sizeof(double) * zeros.size(), s));
+            MG_CUDA(ws.upload(ws.idx.p, idx.data(), sizeof(int) * idx.size(), s));
             k_scatter<<<(static_cast<int>(idx.size()) + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(),
                                                                               static_cast<int>(idx.size()), d_out, 0);
             ++launches;
@@ -274,8 +305,8 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                     MG_CUDA(ws.err.ensure(sizeof(int)));
                     MG_CUDA(cudaMemsetAsync(ws.err.p, 0, sizeof(int), s));
                 }
-                MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
-                MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+                MG_CUDA(ws.upload(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, s));
+                MG_CUDA(ws.upload(ws.idx.p, idx.data(), sizeof(int) * nb, s));
                 // Low cuts: TF32 operand rows split once per observation, in
                 // job groups of at most kMaxRowsBytes.
                 bool presplit = low_cut && k <= gram_tc_presplit_max_k() && gram_tc_presplit_enabled();
@@ -314,8 +345,8 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
             MG_CUDA(ws.jobs.ensure(sizeof(GramJob) * nb));
             MG_CUDA(ws.idx.ensure(sizeof(int) * nb));
             MG_CUDA(ws.vals.ensure(sizeof(double) * nb));
-            MG_CUDA(cudaMemcpyAsync(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, cudaMemcpyHostToDevice, s));
-            MG_CUDA(cudaMemcpyAsync(ws.idx.p, idx.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, s));
+            MG_CUDA(ws.upload(ws.jobs.p, jobs.data(), sizeof(GramJob) * nb, s));
+            MG_CUDA(ws.upload(ws.idx.p, idx.data(), sizeof(int) * nb, s));
             const int nbi = static_cast<int>(nb);
             if (tile_purity)
             {
@@ -348,60 +379,17 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
             }
             else
             {
-                // Large spectra: FP64 eigenvalues from cuSOLVER, all matrices of
-                // the group in one batched call; one matrix at a time only if
-                // the batched routine is unavailable.
-                if (!ws.solver)
+                // Large spectra: FP64 Householder tridiagonalisation and
+                // implicit QL of every matrix of the group (eigen.cu).
+                MG_CUDA(ws.eig.ensure(sizeof(double) * hermitian_eig_scratch_doubles(d, nbi)));
+                if (!ws.eig_err.p)
                 {
-                    if (cusolverDnCreate(&ws.solver) != CUSOLVER_STATUS_SUCCESS)
-                        return fail(MIPT_GB300_E_INTERNAL, "cusolverDnCreate failed");
+                    MG_CUDA(ws.eig_err.ensure(sizeof(int)));
+                    MG_CUDA(cudaMemsetAsync(ws.eig_err.p, 0, sizeof(int), s));
                 }
-                cusolverDnSetStream(ws.solver, s);
-                if (!ws.params && cusolverDnCreateParams(&ws.params) != CUSOLVER_STATUS_SUCCESS)
-                    return fail(MIPT_GB300_E_INTERNAL, "cusolverDnCreateParams failed");
-                std::size_t dev_bytes = 0, host_bytes = 0;
-                if (!ws.batched_eig_failed &&
-                    cusolverDnXsyevBatched_bufferSize(ws.solver, ws.params, CUSOLVER_EIG_MODE_NOVECTOR,
-                                                      CUBLAS_FILL_MODE_LOWER, d, CUDA_C_64F, ws.rho.p, d, CUDA_R_64F,
-                                                      ws.eig.p, CUDA_C_64F, &dev_bytes, &host_bytes,
-                                                      nbi) == CUSOLVER_STATUS_SUCCESS)
-                {
-                    MG_CUDA(ws.work.ensure(std::max<std::size_t>(dev_bytes, 16)));
-                    MG_CUDA(ws.eig.ensure(sizeof(double) * d * static_cast<std::size_t>(nbi)));
-                    MG_CUDA(ws.info.ensure(sizeof(int) * static_cast<std::size_t>(nbi)));
-                    ws.host_work.resize(std::max<std::size_t>(host_bytes, 16));
-                    if (cusolverDnXsyevBatched(ws.solver, ws.params, CUSOLVER_EIG_MODE_NOVECTOR,
-                                               CUBLAS_FILL_MODE_LOWER, d, CUDA_C_64F, ws.rho.p, d, CUDA_R_64F,
-                                               ws.eig.p, CUDA_C_64F, ws.work.p, dev_bytes, ws.host_work.data(),
-                                               host_bytes, ws.info.as<int>(), nbi) == CUSOLVER_STATUS_SUCCESS)
-                    {
-                        k_entropy_from_eigs<<<nbi, 256, 0, s>>>(ws.eig.as<double>(), d, ws.vals.as<double>());
-                        launches += 2;
-                        k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi,
-                                                                    d_out, 0);
-                        ++launches;
-                        continue;
-                    }
-                }
-                ws.batched_eig_failed = true;
-                int lwork = 0;
-                if (cusolverDnZheevd_bufferSize(ws.solver, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, d,
-                                                ws.rho.as<cuDoubleComplex>(), d, ws.eig.as<double>(), &lwork) !=
-                    CUSOLVER_STATUS_SUCCESS)
-                    return fail(MIPT_GB300_E_INTERNAL, "cusolverDnZheevd_bufferSize failed");
-                MG_CUDA(ws.work.ensure(sizeof(cuDoubleComplex) * static_cast<std::size_t>(std::max(lwork, 1))));
-                MG_CUDA(ws.eig.ensure(sizeof(double) * d));
-                MG_CUDA(ws.info.ensure(sizeof(int)));
-                for (int i = 0; i < nbi; ++i)
-                {
-                    cuDoubleComplex *A = ws.rho.as<cuDoubleComplex>() + static_cast<std::size_t>(i) * d * d;
-                    if (cusolverDnZheevd(ws.solver, CUSOLVER_EIG_MODE_NOVECTOR, CUBLAS_FILL_MODE_LOWER, d, A, d,
-                                         ws.eig.as<double>(), ws.work.as<cuDoubleComplex>(), lwork,
-                                         ws.info.as<int>()) != CUSOLVER_STATUS_SUCCESS)
-                        return fail(MIPT_GB300_E_INTERNAL, "cusolverDnZheevd failed");
-                    k_entropy_from_eigs<<<1, 256, 0, s>>>(ws.eig.as<double>(), d, ws.vals.as<double>() + i);
-                    launches += 2;
-                }
+                MG_CUDA(hermitian_eig_entropy(ws.rho.as<double>(), d, nbi, ws.vals.as<double>(), nullptr,
+                                              ws.eig.as<double>(), ws.eig_err.as<int>(), s));
+                launches += 2;
                 k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 0);
                 ++launches;
             }
@@ -433,6 +421,9 @@ int compat_entropy(const void *state, int n, const int *kept, int k, int fermion
     for (int i = 0; i < k; ++i)
         if (kept[i] < 0 || kept[i] >= n) return fail(MIPT_GB300_E_INVALID, "kept mode out of range");
     MG_CUDA(c.out.ensure(sizeof(double)));
+    c.ws.stage.rewind();
+    if (c.ws.err.p) MG_CUDA(cudaMemsetAsync(c.ws.err.p, 0, sizeof(int), 0));
+    if (c.ws.eig_err.p) MG_CUDA(cudaMemsetAsync(c.ws.eig_err.p, 0, sizeof(int), 0));
     long long l = 0;
     try
     {
@@ -450,6 +441,13 @@ int compat_entropy(const void *state, int n, const int *kept, int k, int fermion
         int err = 0;
         MG_CUDA(cudaMemcpy(&err, c.ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) return fail(MIPT_GB300_E_INTERNAL, "tensor-core Gram pipeline wait timed out");
+    }
+    if (c.ws.eig_err.p)
+    {
+        int err = 0;
+        MG_CUDA(cudaMemcpy(&err, c.ws.eig_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err & 2) return fail(MIPT_GB300_E_INTERNAL, "eigensolver barrier wait timed out");
+        if (err) return fail(MIPT_GB300_E_NUMERIC, "an eigenvalue iteration did not converge");
     }
     return 0;
 }
@@ -769,6 +767,17 @@ constexpr TileChoice kTunedTiles[] = {
     {20, 0, 1, 14},
 };
 
+// MIPT_GB300_SPARSE_PASS=0 makes the first pass after a measurement visit
+// every tile (default: only the tiles that agree with the outcome).
+bool use_sparse_pass()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_SPARSE_PASS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 int chosen_tile(const mipt_gb300_batch_config &cfg, int capacity)
 {
     const bool fp64 = cfg.fp64 != 0;
@@ -875,9 +884,17 @@ struct mipt_gb300_batch
     std::size_t next_event = 0;
     double kind_ms[5] = {0, 0, 0, 0, 0};
     long long kind_launches[5] = {0, 0, 0, 0, 0};
+    // CUDA graph of one execute (mipt_gb300_batch_execute_graph) and the
+    // host-side structure it was captured for.
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    std::vector<long long> graph_key;
+    long long graph_launches = 0;
     ~mipt_gb300_batch()
     {
         for (auto e : event_pool) cudaEventDestroy(e);
+        if (graph_exec) cudaGraphExecDestroy(graph_exec);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
     }
     cudaEvent_t take_event()
     {
@@ -1355,6 +1372,13 @@ int set_rho3_subs(mipt_gb300_batch *b, const std::vector<int> &subs)
 } // namespace
 
 extern "C" {
+int mipt_gb300_test_withhold_tile_loads(int count)
+{
+    if (count < 0) return fail(MIPT_GB300_E_INVALID, "count must be >= 0");
+    set_withheld_tile_loads(count);
+    return 0;
+}
+
 int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, int lattice_y, int trajectories,
                              int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count)
 {
@@ -1831,6 +1855,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     long long L = 0;
     b->marks.clear();
     b->next_event = 0;
+    b->ws.stage.rewind();
     {
         Mark m(b, K_OTHER, s);
         int custom = 0;
@@ -1867,6 +1892,9 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     k_reset_layers<<<std::min<std::size_t>((slots + 255) / 256, 1024), 256, 0, s>>>(col, res, slots);
     ++L;
     MG_CUDA(cudaMemsetAsync(b->err.p, 0, sizeof(int), s));
+    // A timed-out Gram wait of an earlier execute is reported once.
+    if (b->ws.err.p) MG_CUDA(cudaMemsetAsync(b->ws.err.p, 0, sizeof(int), s));
+    if (b->ws.eig_err.p) MG_CUDA(cudaMemsetAsync(b->ws.eig_err.p, 0, sizeof(int), s));
     if (b->reqs_per_point > 0)
     {
         const std::size_t ne = static_cast<std::size_t>(count) * b->points * b->reqs_per_point;
@@ -1929,14 +1957,29 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             }
         };
         if (jw) jw_closure();
+        // After a measurement the layer's first pass visits only the tiles
+        // that agree with the outcome on its non-local measured bits (the
+        // rest are zero); the second pass zeroes those bits' other values as
+        // it loads.
+        const bool sparse = t > 0 && plan.size() >= 2 && use_sparse_pass() &&
+                            sparse_pass_supported(plan[0], sizeof(Real) == 4, count) &&
+                            sparse_pass_supported(plan[1], sizeof(Real) == 4, count);
         for (std::size_t pi = 0; pi < plan.size(); ++pi)
         {
             const Collapse *cin = (pi == 0 && t > 0) ? col + (t - 1) : nullptr;
+            std::uint64_t keep = ~0ull;
+            int scaled = 1;
+            if (sparse && pi == 1)
+            {
+                cin = col + (t - 1);
+                keep = nonlocal_mask(plan[0].geom);
+                scaled = 0;
+            }
             const bool last = pi + 1 == plan.size();
             Mark m(b, K_PASS, s);
             MG_CUDA(launch_pass<Real>(states, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
                                       cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0,
-                                      b->err.as<int>(), s));
+                                      b->err.as<int>(), s, keep, scaled, sparse && pi == 0 ? 1 : 0));
             ++L;
         }
         if (jw) jw_closure();
@@ -2008,12 +2051,10 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
 }
 } // namespace
 
-extern "C" {
-
-int mipt_gb300_batch_execute(mipt_gb300_batch *b, void *stream)
+namespace
 {
-    if (!b || b->count <= 0) return fail(MIPT_GB300_E_INVALID, "batch has no prepared trajectories");
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
+int execute_any(mipt_gb300_batch *b, cudaStream_t s)
+{
     try
     {
         return b->cfg.fp64 ? batch_execute<double>(b, s) : batch_execute<float>(b, s);
@@ -2022,6 +2063,211 @@ int mipt_gb300_batch_execute(mipt_gb300_batch *b, void *stream)
     {
         return fail(MIPT_GB300_E_INTERNAL, e.what());
     }
+}
+
+// Everything on the host that decides which kernels an execute enqueues and
+// with which arguments (the device buffers themselves are fixed per batch).
+std::vector<long long> structure_key(const mipt_gb300_batch *b)
+{
+    std::vector<long long> k{b->count, b->has_forced ? 1 : 0, b->points, b->reqs_per_point, b->rho3_count,
+                             b->tmi_cycles};
+    for (char c : b->any_meas) k.push_back(c);
+    for (char c : b->fusable) k.push_back(c);
+    for (int c : b->max_chunks) k.push_back(c);
+    for (char c : b->direct_hist) k.push_back(c);
+    for (int c : b->obs_point) k.push_back(c);
+    for (char c : b->custom_init) k.push_back(c);
+    for (int i = 0; i < b->count && b->cfg.circuit == 2; ++i)
+    {
+        k.push_back(b->folded[i]);
+        k.push_back(b->sector[i]);
+    }
+    for (const auto &r : b->reqs)
+    {
+        k.push_back(r.order * 4 + r.fermion);
+        k.push_back(static_cast<long long>(r.kept.size()));
+        for (int q : r.kept) k.push_back(q);
+    }
+    return k;
+}
+
+bool graph_ready(const mipt_gb300_batch *b)
+{
+    for (char c : b->custom_init)
+        if (c) return false;
+    return !b->profile;
+}
+
+// Captures one execute of each batch into a graph, batch i on streams[i]
+// forked from and joined into `root`. The caller has run each batch once
+// normally, so every buffer has its final size and no capture allocates.
+int capture_graph(mipt_gb300_batch *const *bs, int nb, cudaStream_t root, cudaStream_t *streams,
+                  cudaEvent_t *events, cudaGraphExec_t *exec)
+{
+    cudaError_t e = cudaStreamBeginCapture(root, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+    int rc = 0;
+    if (nb == 1 && streams[0] == root)
+        rc = execute_any(bs[0], root);
+    else
+    {
+        e = cudaEventRecord(events[nb], root);
+        for (int i = 0; i < nb && !rc && e == cudaSuccess; ++i)
+        {
+            e = cudaStreamWaitEvent(streams[i], events[nb], 0);
+            if (e == cudaSuccess) rc = execute_any(bs[i], streams[i]);
+            if (!rc && e == cudaSuccess) e = cudaEventRecord(events[i], streams[i]);
+            if (!rc && e == cudaSuccess) e = cudaStreamWaitEvent(root, events[i], 0);
+        }
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(root, &g);
+    if (rc || e != cudaSuccess || ee != cudaSuccess)
+    {
+        if (g) cudaGraphDestroy(g);
+        if (rc) return rc;
+        return cuda_fail(e != cudaSuccess ? e : ee, "graph capture of a batch execute");
+    }
+    e = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return 0;
+}
+} // namespace
+
+extern "C" {
+
+int mipt_gb300_batch_execute(mipt_gb300_batch *b, void *stream)
+{
+    if (!b || b->count <= 0) return fail(MIPT_GB300_E_INVALID, "batch has no prepared trajectories");
+    return execute_any(b, static_cast<cudaStream_t>(stream));
+}
+
+int mipt_gb300_batch_execute_graph(mipt_gb300_batch *b, void *stream)
+{
+    if (!b || b->count <= 0) return fail(MIPT_GB300_E_INVALID, "batch has no prepared trajectories");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!graph_ready(b)) return execute_any(b, s);
+    const std::vector<long long> key = structure_key(b);
+    if (b->graph_exec && key == b->graph_key)
+    {
+        std::fill(b->sector.begin(), b->sector.end(), 0);
+        MG_CUDA(cudaGraphLaunch(b->graph_exec, s));
+        b->launches = b->graph_launches;
+        b->executed = true;
+        return 0;
+    }
+    // This call's results come from a normal execute, which also sizes every
+    // buffer; the graph is captured from a second execute on a private stream.
+    if (const int rc = execute_any(b, s)) return rc;
+    MG_CUDA(cudaStreamSynchronize(s));
+    if (b->graph_exec)
+    {
+        cudaGraphExecDestroy(b->graph_exec);
+        b->graph_exec = nullptr;
+    }
+    if (!b->cap_stream) MG_CUDA(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    mipt_gb300_batch *one[1] = {b};
+    if (const int rc = capture_graph(one, 1, b->cap_stream, &b->cap_stream, nullptr, &b->graph_exec)) return rc;
+    b->graph_key = key;
+    b->graph_launches = b->launches;
+    return 0;
+}
+
+} // extern "C"
+
+struct mipt_gb300_batch_group
+{
+    std::vector<mipt_gb300_batch *> batches;
+    std::vector<cudaStream_t> streams; // one per batch
+    std::vector<cudaEvent_t> events;   // one per batch + the fork event
+    cudaStream_t root = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<std::vector<long long>> keys;
+    ~mipt_gb300_batch_group()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto st : streams) cudaStreamDestroy(st);
+        for (auto ev : events) cudaEventDestroy(ev);
+        if (root) cudaStreamDestroy(root);
+    }
+};
+
+extern "C" {
+
+int mipt_gb300_batch_group_create(mipt_gb300_batch *const *batches, int count, mipt_gb300_batch_group **out)
+{
+    if (!batches || count < 1 || !out) return fail(MIPT_GB300_E_INVALID, "a batch group needs at least one batch");
+    std::unique_ptr<mipt_gb300_batch_group> g(new mipt_gb300_batch_group());
+    for (int i = 0; i < count; ++i)
+    {
+        if (!batches[i]) return fail(MIPT_GB300_E_INVALID, "null batch in group");
+        for (int j = 0; j < i; ++j)
+            if (batches[j] == batches[i]) return fail(MIPT_GB300_E_INVALID, "a batch appears twice in the group");
+        g->batches.push_back(batches[i]);
+    }
+    MG_CUDA(cudaStreamCreateWithFlags(&g->root, cudaStreamNonBlocking));
+    for (int i = 0; i < count; ++i)
+    {
+        cudaStream_t st;
+        MG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        g->streams.push_back(st);
+    }
+    for (int i = 0; i <= count; ++i)
+    {
+        cudaEvent_t ev;
+        MG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        g->events.push_back(ev);
+    }
+    *out = g.release();
+    return 0;
+}
+
+void mipt_gb300_batch_group_destroy(mipt_gb300_batch_group *g) { delete g; }
+
+int mipt_gb300_batch_group_execute(mipt_gb300_batch_group *g, void *stream)
+{
+    if (!g) return fail(MIPT_GB300_E_INVALID, "null batch group");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int nb = static_cast<int>(g->batches.size());
+    for (auto *b : g->batches)
+        if (b->count <= 0) return fail(MIPT_GB300_E_INVALID, "batch has no prepared trajectories");
+    bool ready = true;
+    for (auto *b : g->batches) ready = ready && graph_ready(b);
+    if (!ready)
+    {
+        for (auto *b : g->batches)
+            if (const int rc = execute_any(b, s)) return rc;
+        return 0;
+    }
+    std::vector<std::vector<long long>> keys;
+    for (auto *b : g->batches) keys.push_back(structure_key(b));
+    if (g->exec && keys == g->keys)
+    {
+        for (auto *b : g->batches) std::fill(b->sector.begin(), b->sector.end(), 0);
+        MG_CUDA(cudaGraphLaunch(g->exec, s));
+        for (auto *b : g->batches)
+        {
+            b->launches = b->graph_launches;
+            b->executed = true;
+        }
+        return 0;
+    }
+    // This call runs every batch normally (its results, and every buffer at
+    // its final size); the graph is captured from a second execute.
+    for (auto *b : g->batches)
+        if (const int rc = execute_any(b, s)) return rc;
+    MG_CUDA(cudaStreamSynchronize(s));
+    if (g->exec)
+    {
+        cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+    }
+    if (const int rc = capture_graph(g->batches.data(), nb, g->root, g->streams.data(), g->events.data(), &g->exec))
+        return rc;
+    for (auto *b : g->batches) b->graph_launches = b->launches;
+    g->keys = keys;
+    return 0;
 }
 
 int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::uint64_t *outcomes, double *surprisal,
@@ -2049,6 +2295,12 @@ int mipt_gb300_batch_fetch(mipt_gb300_batch *b, std::uint64_t *measured, std::ui
     {
         MG_CUDA(cudaMemcpy(&err, b->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (err) return fail(MIPT_GB300_E_INTERNAL, "tensor-core Gram pipeline wait timed out");
+    }
+    if (b->ws.eig_err.p)
+    {
+        MG_CUDA(cudaMemcpy(&err, b->ws.eig_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err & 2) return fail(MIPT_GB300_E_INTERNAL, "eigensolver barrier wait timed out");
+        if (err) return fail(MIPT_GB300_E_NUMERIC, "an eigenvalue iteration did not converge");
     }
     const int count = b->count, T = b->T;
     if (measured) std::copy(b->measured.begin(), b->measured.end(), measured);

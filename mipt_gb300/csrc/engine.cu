@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -512,16 +513,14 @@ __device__ __forceinline__ bool tile_bar_wait(std::uint64_t *bar, std::uint32_t 
     return false;
 }
 
-// One thread: fetches the tile of work item `item` (trajectory item >> n_nl,
-// tile item mod 2^n_nl) into `tile` in plain tile order with one TMA tensor
-// load. Dimension d of the map covers global index bits [lo[d], lo[d] +
-// bits[d]) (the last one also the trajectory index above bit n); its
-// coordinate is those bits of the item's base index, 0 on local runs.
+// One thread: fetches the tile whose first amplitude has batch-global index
+// gb (trajectory << n | tile base) into `tile` in plain tile order with one
+// TMA tensor load. Dimension d of the map covers global index bits [lo[d],
+// lo[d] + bits[d]) (the last one also the trajectory index above bit n); its
+// coordinate is those bits of gb, 0 on local runs.
 __device__ __forceinline__ void tile_tma_load(void *tile, const CUtensorMap *map, const TileTma &t, const PassGeom &g,
-                                              std::uint64_t item, std::uint64_t *bar)
+                                              std::uint64_t gb, std::uint64_t *bar)
 {
-    const std::uint64_t gb =
-        ((item >> g.n_nl) << g.n) | scatter_bits(item & ((1ull << g.n_nl) - 1), g.nl, g.n_nl);
     int c[5] = {0, 0, 0, 0, 0};
     for (int d = 0; d < t.rank; ++d)
     {
@@ -562,6 +561,108 @@ __device__ __forceinline__ void tile_tma_load(void *tile, const CUtensorMap *map
     }
 }
 
+// Work items of a pass. Dense: item = trajectory * 2^n_nl + tile. Sparse
+// (the first pass of a layer that follows a measurement): a tile whose
+// non-local measured bits differ from the outcome is zero once the pending
+// collapse is applied, and the pass's gates (all on local qubits) keep it
+// zero, so only the 2^(n_nl - m_b) tiles of trajectory b that agree with its
+// outcome on its m_b non-local measured bits are items. pref[b] is the first
+// item of trajectory b (pref[batch] = the total); the r-th item of b has r's
+// bits on the free non-local bits, the outcome on the fixed ones, ascending.
+struct ItemSpace
+{
+    const std::uint32_t *pref;
+    std::uint64_t nlq; // non-local qubits of the pass (mask)
+};
+
+__device__ __forceinline__ void decode_item(std::uint64_t item, bool sparse, const ItemSpace &sp, const PassGeom &g,
+                                            const Collapse *col_in, std::size_t col_stride, int batch, int &b,
+                                            std::uint64_t &tix)
+{
+    if (!sparse)
+    {
+        b = static_cast<int>(item >> g.n_nl);
+        tix = item & ((1ull << g.n_nl) - 1);
+        return;
+    }
+    int lo = 0, hi = batch - 1; // largest b with pref[b] <= item
+    while (lo < hi)
+    {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sp.pref[mid] <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    b = lo;
+    const Collapse c = col_in[static_cast<std::size_t>(b) * col_stride];
+    std::uint64_t r = item - sp.pref[b];
+    tix = 0;
+    for (int i = 0; i < g.n_nl; ++i)
+    {
+        const int q = g.nl[i];
+        std::uint64_t bit;
+        if ((c.mask >> q) & 1ull)
+            bit = (c.value >> q) & 1ull;
+        else
+        {
+            bit = r & 1ull;
+            r >>= 1;
+        }
+        tix |= bit << i;
+    }
+}
+
+// Builds pref[0..batch] of the sparse item space (all threads of the CTA;
+// red holds at least 32 words). Returns the item count.
+__device__ std::uint32_t build_item_prefix(std::uint32_t *pref, std::uint32_t *red, const PassGeom &g,
+                                           std::uint64_t nlq, const Collapse *col_in, std::size_t col_stride,
+                                           int batch)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int per = (batch + nt - 1) / nt;
+    const int b0 = tid * per, b1 = min(batch, b0 + per);
+    auto count = [&](int b) {
+        const std::uint64_t m = col_in[static_cast<std::size_t>(b) * col_stride].mask & nlq;
+        return 1u << (g.n_nl - __popcll(m));
+    };
+    std::uint32_t sum = 0;
+    for (int b = b0; b < b1; ++b) sum += count(b);
+    // Exclusive scan of the per-thread sums over the CTA.
+    const int lane = tid & 31, warp = tid >> 5;
+    std::uint32_t x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const std::uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) red[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        std::uint32_t w = lane < (nt >> 5) ? red[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const std::uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < (nt >> 5)) red[lane] = w; // inclusive warp totals
+    }
+    __syncthreads();
+    std::uint32_t run = x - sum + (warp > 0 ? red[warp - 1] : 0u);
+    for (int b = b0; b < b1; ++b)
+    {
+        pref[b] = run;
+        run += count(b);
+    }
+    const std::uint32_t total = red[(nt >> 5) - 1];
+    if (tid == 0) pref[batch] = total;
+    __syncthreads();
+    return total;
+}
+
 // One tiled pass with register rounds: global -> registers (lanes on the
 // contiguous low qubits), gates applied in registers, swizzled shared-memory
 // transposes between rounds, registers -> global, optional fused histogram.
@@ -581,7 +682,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
                   const LayerMeas *__restrict__ meas, std::size_t meas_stride, double *__restrict__ partials,
                   int fuse_hist, int packed, int batch, const __grid_constant__ CUtensorMap tmap, TileTma tt,
-                  int *err)
+                  int *err, std::uint64_t col_keep, int col_scaled, int sparse, int withhold_first_load)
 {
     constexpr int NA = 1 << RB;
     extern __shared__ __align__(128) unsigned char smem_dyn[];
@@ -596,12 +697,32 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     const PassGeom &g = P.geom;
     const int TB = g.k - RB;
     const int tid = threadIdx.x;
-    const std::uint64_t items = static_cast<std::uint64_t>(batch) << g.n_nl;
+    const bool sp_on = sparse != 0;
+    ItemSpace sp{nullptr, 0};
+    std::uint64_t items = static_cast<std::uint64_t>(batch) << g.n_nl;
+    if (sp_on)
+    {
+        // The item prefix table follows the tile (and, with TMA, the
+        // histogram values) in dynamic shared memory.
+        __shared__ std::uint32_t sred[32];
+        std::uint32_t *pref = reinterpret_cast<std::uint32_t *>(
+            smem_raw + (sizeof(Cx<Real>) << g.k) + (TMA ? (sizeof(float) << g.k) : 0));
+        for (int i = 0; i < g.n_nl; ++i) sp.nlq |= 1ull << g.nl[i];
+        items = build_item_prefix(pref, sred, g, sp.nlq, col_in, col_stride, batch);
+        sp.pref = pref;
+    }
     const std::uint64_t step = static_cast<std::uint64_t>(gridDim.x) * gridDim.y;
     const std::uint64_t first = static_cast<std::uint64_t>(blockIdx.y) * gridDim.x + blockIdx.x;
     __shared__ __align__(8) std::uint64_t tile_bar;
     __shared__ int tile_fail;
     std::uint32_t tile_phase = 0;
+    // Batch-global index of the first amplitude of an item's tile.
+    auto item_base = [&](std::uint64_t it) {
+        int bb;
+        std::uint64_t tt_;
+        decode_item(it, sp_on, sp, g, col_in, col_stride, batch, bb, tt_);
+        return (static_cast<std::uint64_t>(bb) << g.n) | scatter_bits(tt_, g.nl, g.n_nl);
+    };
     if constexpr (TMA)
     {
         if (tid == 0)
@@ -611,13 +732,17 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
             tile_fail = 0;
         }
         __syncthreads();
-        if (tid == 0 && first < items) tile_tma_load(tile, &tmap, tt, g, first, &tile_bar);
+        // withhold_first_load (a test hook): CTA 0 does not issue its first
+        // tile load, so its bounded wait runs out and the pass reports it.
+        const bool withhold = withhold_first_load != 0 && first == 0;
+        if (tid == 0 && first < items && !withhold) tile_tma_load(tile, &tmap, tt, g, item_base(first), &tile_bar);
     }
     int cur_b = -1;
     for (std::uint64_t item = first; item < items; item += step)
     {
-        const int b = static_cast<int>(item >> g.n_nl);
-        const std::uint64_t tix = item & ((1ull << g.n_nl) - 1);
+        int b;
+        std::uint64_t tix;
+        decode_item(item, sp_on, sp, g, col_in, col_stride, batch, b, tix);
         __syncthreads(); // the previous item's shared-memory reads are complete
         Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
         const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
@@ -627,7 +752,15 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
         cur_b = b;
         Collapse cl{0, 0, 1.0, 0.0};
         const bool has_col = col_in != nullptr;
-        if (has_col) cl = col_in[b * col_stride];
+        if (has_col)
+        {
+            // col_keep < all ones: the residual of a collapse whose scale an
+            // earlier pass of the layer applied (the bits that pass skipped).
+            cl = col_in[b * col_stride];
+            cl.mask &= col_keep;
+            cl.value &= col_keep;
+            if (!col_scaled) cl.scale = 1.0;
+        }
         const Real scale = static_cast<Real>(cl.scale);
 
         const std::uint64_t next = item + step;
@@ -704,7 +837,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                 }
                 return;
             }
-            if (P.rounds == 1 && next < items && tid == 0) tile_tma_load(tile, &tmap, tt, g, next, &tile_bar);
+            if (P.rounds == 1 && next < items && tid == 0) tile_tma_load(tile, &tmap, tt, g, item_base(next), &tile_bar);
         }
 
         for (int ri = 0; ri < P.rounds; ++ri)
@@ -752,7 +885,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                     if (ri == P.rounds - 1 && next < items)
                     {
                         __syncthreads(); // the last reads of the tile buffer for this item are done
-                        if (tid == 0) tile_tma_load(tile, &tmap, tt, g, next, &tile_bar);
+                        if (tid == 0) tile_tma_load(tile, &tmap, tt, g, item_base(next), &tile_bar);
                     }
                 }
             }
@@ -1934,15 +2067,28 @@ bool encode_tile_map(CUtensorMap &map, TileTma &t, const Cx<float> *states, int 
                               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Test hook: the next `count` TMA-fed pass launches withhold CTA 0's first
+// tile load (set_withheld_tile_loads), so their bounded tile waits run out.
+std::atomic<int> g_withheld_loads{0};
+
+int take_withheld_load()
+{
+    int c = g_withheld_loads.load();
+    while (c > 0 && !g_withheld_loads.compare_exchange_weak(c, c - 1)) {}
+    return c > 0 ? 1 : 0;
+}
+
 // Launches k_pass_rounds<Real, RB, TMA> on its grid.
 template <typename Real, int RB, bool TMA>
 cudaError_t launch_rounds(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                           std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                           const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                          const CUtensorMap &map, const TileTma &tt, int *err, cudaStream_t s)
+                          const CUtensorMap &map, const TileTma &tt, int *err, cudaStream_t s,
+                          std::uint64_t col_keep, int col_scaled, int sparse)
 {
     const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, RB, TMA>);
-    const std::size_t smem = (sizeof(Cx<Real>) << plan.geom.k) + (TMA ? (sizeof(float) << plan.geom.k) + 128 : 0);
+    const std::size_t smem = (sizeof(Cx<Real>) << plan.geom.k) + (TMA ? (sizeof(float) << plan.geom.k) + 128 : 0) +
+                             (sparse ? sizeof(std::uint32_t) * (static_cast<std::size_t>(batch) + 1) : 0);
     cudaError_t e = ensure_smem_attr<Real>(fn, smem);
     if (e != cudaSuccess) return e;
     const int threads = 1 << (plan.geom.k - RB);
@@ -1950,17 +2096,35 @@ cudaError_t launch_rounds(Cx<Real> *states, int batch, const PassPlan &plan, con
     k_pass_rounds<Real, RB, TMA><<<pgrid, threads, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
                                                                collapse_stride, meas, meas_stride, partials,
                                                                fuse_hist, use_packed_fma() ? 1 : 0, batch, map, tt,
-                                                               err);
+                                                               err, col_keep, col_scaled, sparse,
+                                                               TMA ? take_withheld_load() : 0);
     return cudaGetLastError();
+}
+
+
+bool sparse_pass_supported(const PassPlan &plan, bool fp32, int batch)
+{
+    if (plan.rounds <= 0 || plan.geom.n_nl <= 0 || batch < 1) return false;
+    if (fp32 && plan.cluster_rounds > 0 && use_cluster_kernel()) return false;
+    if (fp32 && plan.rb != 5 && plan.rb != 6) return false;
+    if (!fp32 && plan.rb != 5) return false;
+    if ((static_cast<std::uint64_t>(batch) << plan.geom.n_nl) >= (1ull << 31)) return false;
+    // Tile (+ histogram values and alignment with TMA) + item table.
+    const std::size_t base = fp32 ? (sizeof(Cx<float>) << plan.geom.k) + (sizeof(float) << plan.geom.k) + 128
+                                  : (sizeof(Cx<double>) << plan.geom.k);
+    return base + sizeof(std::uint32_t) * (static_cast<std::size_t>(batch) + 1) <= (200u << 10);
 }
 
 template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                        int *err, cudaStream_t s)
+                        int *err, cudaStream_t s, std::uint64_t col_keep, int col_scaled, int sparse)
 {
     dim3 grid(1u << plan.geom.n_nl, batch);
+    if ((sparse || col_keep != ~0ull || !col_scaled) && !sparse_pass_supported(plan, sizeof(Real) == 4, batch))
+        return cudaErrorInvalidValue;
+    if (sparse && (collapse_in == nullptr || fuse_hist)) return cudaErrorInvalidValue;
     if constexpr (sizeof(Real) == 4)
     {
         if (plan.cluster_rounds > 0 && use_cluster_kernel())
@@ -1998,17 +2162,17 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
             if (plan.rb == 6)
                 return tma ? launch_rounds<Real, 6, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                          map, tt, err, s)
+                                                          map, tt, err, s, col_keep, col_scaled, sparse)
                            : launch_rounds<Real, 6, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
                                                            collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                           map, tt, err, s);
+                                                           map, tt, err, s, col_keep, col_scaled, sparse);
             if (plan.rb == 5)
                 return tma ? launch_rounds<Real, 5, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                          map, tt, err, s)
+                                                          map, tt, err, s, col_keep, col_scaled, sparse)
                            : launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
                                                            collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                           map, tt, err, s);
+                                                           map, tt, err, s, col_keep, col_scaled, sparse);
             return cudaErrorInvalidValue;
         }
         else
@@ -2018,7 +2182,7 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
             std::memset(&map, 0, sizeof(map));
             return launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
                                                  collapse_stride, meas, meas_stride, partials, fuse_hist, map,
-                                                 TileTma{}, err, s);
+                                                 TileTma{}, err, s, col_keep, col_scaled, sparse);
         }
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
@@ -2071,11 +2235,13 @@ cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, cons
     return cudaGetLastError();
 }
 
+void set_withheld_tile_loads(int count) { g_withheld_loads.store(count > 0 ? count : 0); }
+
 #define MG_INSTANTIATE(R)                                                                                        \
     template cudaError_t launch_init_zero<R>(Cx<R> *, std::uint64_t, int, cudaStream_t);                         \
     template cudaError_t launch_pass<R>(Cx<R> *, int, const PassPlan &, const Cx<R> *, std::size_t,              \
                                         const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
-                                        int, int *, cudaStream_t);                                               \
+                                        int, int *, cudaStream_t, std::uint64_t, int, int);                      \
     template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
                                         const LayerMeas *, std::size_t, double *, bool, cudaStream_t);           \
     template cudaError_t launch_collapse<R>(Cx<R> *, std::uint64_t, int, const Collapse *, std::size_t,          \

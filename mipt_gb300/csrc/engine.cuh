@@ -127,11 +127,37 @@ struct EngineLaunch
 template <typename Real>
 cudaError_t launch_init_zero(Cx<Real> *states, std::uint64_t dim, int batch, cudaStream_t s);
 
+// collapse_in (if any) is applied as the tiles load: amplitudes whose bits on
+// mask & col_keep differ from value become zero, the others are scaled by the
+// collapse's scale (col_scaled) or kept as they are. sparse: the pass visits
+// only the tiles that agree with collapse_in's outcome on the pass's
+// non-local measured bits (the others are zero before and after the pass and
+// are left untouched in memory); the layer's next pass must then load with
+// col_keep = those non-local qubits and col_scaled = 0. Needs a register-round
+// plan (sparse_pass_supported) and no fused histogram.
 template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                        int *err, cudaStream_t s);
+                        int *err, cudaStream_t s, std::uint64_t col_keep = ~0ull, int col_scaled = 1,
+                        int sparse = 0);
+
+// Test hook: the next `count` TMA-fed pass launches do not issue CTA 0's
+// first tile load; its bounded wait (well under a second) runs out, the CTA
+// sets bit 8 of the error flag and returns. No load is left in flight.
+void set_withheld_tile_loads(int count);
+
+// Whether launch_pass accepts sparse / residual-collapse arguments for this
+// plan and batch size.
+bool sparse_pass_supported(const PassPlan &plan, bool fp32, int batch);
+
+// Non-local qubits of a pass (mask).
+inline std::uint64_t nonlocal_mask(const PassGeom &g)
+{
+    std::uint64_t m = 0;
+    for (int i = 0; i < g.n_nl; ++i) m |= 1ull << g.nl[i];
+    return m;
+}
 
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,

@@ -45,13 +45,15 @@ constexpr int FF_THREADS = 512;
 
 __device__ __forceinline__ int tri_index(int k, int l, int M) { return k * M - (k * (k + 1)) / 2 + (l - k - 1); }
 
-__device__ __forceinline__ float tri_get(const float *T, int i, int j, int M)
+template <typename Real>
+__device__ __forceinline__ Real tri_get(const Real *T, int i, int j, int M)
 {
-    if (i == j) return 0.f;
+    if (i == j) return Real(0);
     return i < j ? T[tri_index(i, j, M)] : -T[tri_index(j, i, M)];
 }
 
-__device__ __forceinline__ void tri_set(float *T, int i, int j, int M, float v)
+template <typename Real>
+__device__ __forceinline__ void tri_set(Real *T, int i, int j, int M, Real v)
 {
     if (i < j)
         T[tri_index(i, j, M)] = v;
@@ -59,33 +61,40 @@ __device__ __forceinline__ void tri_set(float *T, int i, int j, int M, float v)
         T[tri_index(j, i, M)] = -v;
 }
 
-// Runs layers [t0, t1) for one trajectory per block. Gamma (full FP32 matrix
-// in global memory) is loaded into a packed upper triangle in shared memory
-// and written back at the end.
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return fma(a, b, c); }
+
+// Runs layers [t0, t1) for one trajectory per block. Gamma (full matrix in
+// global memory) is loaded into a packed upper triangle and written back at
+// the end. FP32: the triangle lives in shared memory. FP64: it does not fit
+// there at N = 128 (261 KB), so it lives in the trajectory's slice of
+// tri_global (L2-resident while the block runs); the work is the same.
 //   rot    [traj][depth][G][16]    row-major rotation of group g
 //   groups [2][G][4]               Majorana indices of group g (by layer parity)
 //   mcount [traj][depth], mmode/unif/forced/outc/prob [traj][depth][N]
+template <typename Real>
 __global__ void __launch_bounds__(FF_THREADS)
-    k_ff_evolve(int N, int depth, int G, int t0, int t1, const float *__restrict__ rot,
+    k_ff_evolve(int N, int depth, int G, int t0, int t1, const Real *__restrict__ rot,
                 const unsigned char *__restrict__ groups, const int *__restrict__ mcount,
                 const unsigned char *__restrict__ mmode, const double *__restrict__ unif,
                 const signed char *__restrict__ forced, signed char *__restrict__ outc, double *__restrict__ prob,
-                float *__restrict__ gamma)
+                Real *__restrict__ gamma, Real *__restrict__ tri_global)
 {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int M = 2 * N;
     const int P = M * (M - 1) / 2;
-    float *T = smem;
-    float *Ucol = T + P;
-    float *Vcol = Ucol + M;
-    float *R = Vcol + M;
+    Real *sm = reinterpret_cast<Real *>(smem_raw);
+    Real *T = tri_global ? tri_global + static_cast<std::size_t>(blockIdx.x) * P : sm;
+    Real *Ucol = tri_global ? sm : sm + P;
+    Real *Vcol = Ucol + M;
+    Real *R = Vcol + M;
     unsigned char *grp = reinterpret_cast<unsigned char *>(R + G * 16);
-    __shared__ float s_sign, s_coef;
+    __shared__ Real s_sign, s_coef;
 
     const int traj = blockIdx.x;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int warp = tid >> 5, lane = tid & 31, nwarps = nthr >> 5;
-    float *Gm = gamma + static_cast<std::size_t>(traj) * M * M;
+    Real *Gm = gamma + static_cast<std::size_t>(traj) * M * M;
 
     for (int k = warp; k < M; k += nwarps)
         for (int l = k + 1 + lane; l < M; l += 32) T[tri_index(k, l, M)] = Gm[k * M + l];
@@ -112,20 +121,20 @@ __global__ void __launch_bounds__(FF_THREADS)
                 ia[r] = grp[a * 4 + r];
                 ib[r] = grp[b * 4 + r];
             }
-            float X[4][4], Y[4][4];
+            Real X[4][4], Y[4][4];
             for (int r = 0; r < 4; ++r)
                 for (int c = 0; c < 4; ++c) X[r][c] = tri_get(T, ia[r], ib[c], M);
-            const float *Oa = R + a * 16, *Ob = R + b * 16;
+            const Real *Oa = R + a * 16, *Ob = R + b * 16;
             // Y = Oa X Ob^T
             for (int r = 0; r < 4; ++r)
                 for (int c = 0; c < 4; ++c)
                 {
-                    float acc = 0.f;
+                    Real acc = Real(0);
                     for (int k = 0; k < 4; ++k)
                     {
-                        float xo = 0.f;
-                        for (int l = 0; l < 4; ++l) xo = fmaf(X[k][l], Ob[c * 4 + l], xo);
-                        acc = fmaf(Oa[r * 4 + k], xo, acc);
+                        Real xo = Real(0);
+                        for (int l = 0; l < 4; ++l) xo = fmaR(X[k][l], Ob[c * 4 + l], xo);
+                        acc = fmaR(Oa[r * 4 + k], xo, acc);
                     }
                     Y[r][c] = acc;
                 }
@@ -164,29 +173,29 @@ __global__ void __launch_bounds__(FF_THREADS)
                     s = unif[lt * N + i] < pplus ? 1 : -1;
                 const double pr = s > 0 ? pplus : 1.0 - pplus;
                 const double den = g + static_cast<double>(s);
-                s_sign = static_cast<float>(s);
-                s_coef = (den != 0.0) ? static_cast<float>(1.0 / den) : 0.f;
+                s_sign = static_cast<Real>(s);
+                s_coef = (den != 0.0) ? static_cast<Real>(1.0 / den) : Real(0);
                 outc[lt * N + i] = static_cast<signed char>(s);
                 prob[lt * N + i] = pr;
             }
             __syncthreads();
-            const float coef = s_coef;
+            const Real coef = s_coef;
             for (int k = warp; k < M; k += nwarps)
             {
                 if (k == a || k == b) continue;
-                const float uk = Ucol[k], vk = Vcol[k];
+                const Real uk = Ucol[k], vk = Vcol[k];
                 for (int l = k + 1 + lane; l < M; l += 32)
                 {
                     if (l == a || l == b) continue;
-                    float &x = T[tri_index(k, l, M)];
-                    x = fmaf(coef, fmaf(vk, Ucol[l], -uk * Vcol[l]), x);
+                    Real &x = T[tri_index(k, l, M)];
+                    x = fmaR(coef, fmaR(vk, Ucol[l], -uk * Vcol[l]), x);
                 }
             }
             __syncthreads();
             for (int k = tid; k < M; k += nthr)
             {
-                if (k != a) tri_set(T, k, a, M, 0.f);
-                if (k != b) tri_set(T, k, b, M, 0.f);
+                if (k != a) tri_set(T, k, a, M, Real(0));
+                if (k != b) tri_set(T, k, b, M, Real(0));
             }
             __syncthreads();
             if (tid == 0) tri_set(T, a, b, M, s_sign);
@@ -497,7 +506,8 @@ extern "C" int mipt_gb300_ff_run(const mipt_gb300_ff_config *cfg, const std::uin
     }
     const int M = 2 * N, G = N / 2;
     const std::size_t C = count, D = depth;
-    std::vector<float> h_rot(C * D * G * 16, 0.f);
+    const bool fp64 = cfg->fp64 != 0;
+    std::vector<double> h_rot(C * D * G * 16, 0.0);
     std::vector<int> h_mc(C * D);
     std::vector<unsigned char> h_mm(C * D * N);
     std::vector<double> h_u(C * D * N);
@@ -507,13 +517,12 @@ extern "C" int mipt_gb300_ff_run(const mipt_gb300_ff_config *cfg, const std::uin
         const FermionDraw &d = draws[b];
         for (int t = 0; t < depth; ++t)
         {
-            float *dst = &h_rot[((b * D + t) * G) * 16];
+            double *dst = &h_rot[((b * D + t) * G) * 16];
             const int gc = d.gate_count[t];
             for (int g = 0; g < gc; ++g)
-                for (int e = 0; e < 16; ++e)
-                    dst[g * 16 + e] = static_cast<float>(d.rot[(static_cast<std::size_t>(t) * d.max_gates + g) * 16 + e]);
+                for (int e = 0; e < 16; ++e) dst[g * 16 + e] = d.rot[(static_cast<std::size_t>(t) * d.max_gates + g) * 16 + e];
             for (int g = gc; g < G; ++g)
-                for (int e = 0; e < 16; ++e) dst[g * 16 + e] = (e % 5 == 0) ? 1.f : 0.f;
+                for (int e = 0; e < 16; ++e) dst[g * 16 + e] = (e % 5 == 0) ? 1.0 : 0.0;
             h_mc[b * D + t] = d.meas_count[t];
             for (int i = 0; i < d.meas_count[t]; ++i)
             {
@@ -544,8 +553,9 @@ extern "C" int mipt_gb300_ff_run(const mipt_gb300_ff_config *cfg, const std::uin
         }
     }
 
-    Dev d_rot, d_grp, d_mc, d_mm, d_u, d_f, d_oc, d_pr, d_g32, d_g64, d_t1, d_t2, d_jobs, d_ent;
-    FF_CUDA(d_rot.alloc(sizeof(float) * h_rot.size()));
+    Dev d_rot, d_grp, d_mc, d_mm, d_u, d_f, d_oc, d_pr, d_g32, d_g64, d_t1, d_t2, d_tri, d_jobs, d_ent;
+    const std::size_t rot_elem = fp64 ? sizeof(double) : sizeof(float);
+    FF_CUDA(d_rot.alloc(rot_elem * h_rot.size()));
     FF_CUDA(d_grp.alloc(h_grp.size()));
     FF_CUDA(d_mc.alloc(sizeof(int) * h_mc.size()));
     FF_CUDA(d_mm.alloc(h_mm.size()));
@@ -553,11 +563,18 @@ extern "C" int mipt_gb300_ff_run(const mipt_gb300_ff_config *cfg, const std::uin
     if (forced) FF_CUDA(d_f.alloc(h_forced.size()));
     FF_CUDA(d_oc.alloc(C * D * N));
     FF_CUDA(d_pr.alloc(sizeof(double) * C * D * N));
-    FF_CUDA(d_g32.alloc(sizeof(float) * C * M * M));
+    if (!fp64) FF_CUDA(d_g32.alloc(sizeof(float) * C * M * M));
     FF_CUDA(d_g64.alloc(sizeof(double) * C * M * M));
+    if (fp64) FF_CUDA(d_tri.alloc(sizeof(double) * C * (static_cast<std::size_t>(M) * (M - 1) / 2)));
     FF_CUDA(d_t1.alloc(sizeof(double) * C * M * M));
     FF_CUDA(d_t2.alloc(sizeof(double) * C * M * M));
-    FF_CUDA(cudaMemcpy(d_rot.p, h_rot.data(), sizeof(float) * h_rot.size(), cudaMemcpyHostToDevice));
+    if (fp64)
+        FF_CUDA(cudaMemcpy(d_rot.p, h_rot.data(), sizeof(double) * h_rot.size(), cudaMemcpyHostToDevice));
+    else
+    {
+        std::vector<float> r32(h_rot.begin(), h_rot.end());
+        FF_CUDA(cudaMemcpy(d_rot.p, r32.data(), sizeof(float) * r32.size(), cudaMemcpyHostToDevice));
+    }
     FF_CUDA(cudaMemcpy(d_grp.p, h_grp.data(), h_grp.size(), cudaMemcpyHostToDevice));
     FF_CUDA(cudaMemcpy(d_mc.p, h_mc.data(), sizeof(int) * h_mc.size(), cudaMemcpyHostToDevice));
     FF_CUDA(cudaMemcpy(d_mm.p, h_mm.data(), h_mm.size(), cudaMemcpyHostToDevice));
@@ -566,31 +583,57 @@ extern "C" int mipt_gb300_ff_run(const mipt_gb300_ff_config *cfg, const std::uin
     FF_CUDA(cudaMemset(d_oc.p, 0, C * D * N));
     FF_CUDA(cudaMemset(d_pr.p, 0, sizeof(double) * C * D * N));
     {
-        std::vector<float> g0(static_cast<std::size_t>(M) * M, 0.f);
+        std::vector<double> g0(static_cast<std::size_t>(M) * M, 0.0);
         for (int j = 0; j < N; ++j)
         {
-            g0[(2 * j) * M + 2 * j + 1] = 1.f;
-            g0[(2 * j + 1) * M + 2 * j] = -1.f;
+            g0[(2 * j) * M + 2 * j + 1] = 1.0;
+            g0[(2 * j + 1) * M + 2 * j] = -1.0;
         }
+        std::vector<float> g0f(g0.begin(), g0.end());
         for (std::size_t b = 0; b < C; ++b)
-            FF_CUDA(cudaMemcpy(d_g32.as<float>() + b * M * M, g0.data(), sizeof(float) * M * M, cudaMemcpyHostToDevice));
+        {
+            if (fp64)
+                FF_CUDA(cudaMemcpy(d_g64.as<double>() + b * M * M, g0.data(), sizeof(double) * M * M,
+                                   cudaMemcpyHostToDevice));
+            else
+                FF_CUDA(cudaMemcpy(d_g32.as<float>() + b * M * M, g0f.data(), sizeof(float) * M * M,
+                                   cudaMemcpyHostToDevice));
+        }
     }
-    const std::size_t smem = sizeof(float) * (static_cast<std::size_t>(M) * (M - 1) / 2 + 2 * M + G * 16) + G * 4 + 16;
-    FF_CUDA(cudaFuncSetAttribute(k_ff_evolve, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    // Shared memory: the packed triangle (FP32 only), two columns, the
+    // rotations and the group table.
+    const std::size_t tri_bytes = rot_elem * (static_cast<std::size_t>(M) * (M - 1) / 2);
+    const std::size_t smem = (fp64 ? 0 : tri_bytes) + rot_elem * (2 * M + G * 16) + G * 4 + 16;
+    if (fp64)
+        FF_CUDA(cudaFuncSetAttribute(k_ff_evolve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    else
+        FF_CUDA(cudaFuncSetAttribute(k_ff_evolve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
     const int seg = cfg->repurify_every > 0 ? cfg->repurify_every : depth;
     const int cvt_blocks = static_cast<int>(std::min<std::size_t>((C * M * M + 255) / 256, 4096));
     for (int t0 = 0; t0 < depth; t0 += seg)
     {
         const int t1 = std::min(depth, t0 + seg);
-        k_ff_evolve<<<count, FF_THREADS, smem>>>(N, depth, G, t0, t1, d_rot.as<float>(), d_grp.as<unsigned char>(),
-                                                 d_mc.as<int>(), d_mm.as<unsigned char>(), d_u.as<double>(),
-                                                 forced ? d_f.as<signed char>() : nullptr, d_oc.as<signed char>(),
-                                                 d_pr.as<double>(), d_g32.as<float>());
+        if (fp64)
+            k_ff_evolve<double><<<count, FF_THREADS, smem>>>(
+                N, depth, G, t0, t1, d_rot.as<double>(), d_grp.as<unsigned char>(), d_mc.as<int>(),
+                d_mm.as<unsigned char>(), d_u.as<double>(), forced ? d_f.as<signed char>() : nullptr,
+                d_oc.as<signed char>(), d_pr.as<double>(), d_g64.as<double>(), d_tri.as<double>());
+        else
+            k_ff_evolve<float><<<count, FF_THREADS, smem>>>(
+                N, depth, G, t0, t1, d_rot.as<float>(), d_grp.as<unsigned char>(), d_mc.as<int>(),
+                d_mm.as<unsigned char>(), d_u.as<double>(), forced ? d_f.as<signed char>() : nullptr,
+                d_oc.as<signed char>(), d_pr.as<double>(), d_g32.as<float>(), nullptr);
         FF_CUDA(cudaGetLastError());
         // FP64 re-purification between segments (and of the final state).
-        k_f32_to_f64<<<cvt_blocks, 256>>>(d_g32.as<float>(), d_g64.as<double>(), C * M * M);
-        FF_CUDA(cudaGetLastError());
-        const int rc = purify(M, count, d_g64.as<double>(), d_t1.as<double>(), d_t2.as<double>(), d_g32.as<float>());
+        if (!fp64)
+        {
+            k_f32_to_f64<<<cvt_blocks, 256>>>(d_g32.as<float>(), d_g64.as<double>(), C * M * M);
+            FF_CUDA(cudaGetLastError());
+        }
+        const int rc = purify(M, count, d_g64.as<double>(), d_t1.as<double>(), d_t2.as<double>(),
+                              fp64 ? nullptr : d_g32.as<float>());
         if (rc) return rc;
     }
     // Entropy jobs: blocks [0, len) (the shorter side of the cut, the state is

@@ -87,6 +87,19 @@ cudaError_t purity_of(const double *rho, int d, int njobs, double *purity_out, c
 cudaError_t jacobi_entropy(const double *rho, int d, int njobs, double *entropy_out, double *eig_out,
                            cudaStream_t s);
 
+// Von Neumann entropies (bits) of Hermitian matrices rho[job][d][d]
+// (destroyed) for 2 <= d <= 4096: FP64 Householder tridiagonalisation (one
+// CTA per matrix, or, with fewer matrices than resident CTAs, several CTAs
+// per matrix in a cooperative launch), then implicit QL, one thread per
+// matrix (eigen.cu).
+// eig_out (nullable) receives each matrix's eigenvalues (unordered);
+// scratch holds hermitian_eig_scratch_doubles(d, njobs) doubles. A QL
+// iteration limit that runs out sets bit 1 of *err and writes NaN; a timed-out
+// barrier between the CTAs of one matrix sets bit 2.
+std::size_t hermitian_eig_scratch_doubles(int d, int njobs);
+cudaError_t hermitian_eig_entropy(double *rho, int d, int njobs, double *entropy_out, double *eig_out,
+                                  double *scratch, int *err, cudaStream_t s);
+
 // Three-site RDMs of every trajectory, for `count` triples subs[3*i..].
 // out[traj][i][8][8] complex row-major. fermion selects the fermionic trace
 // of the reference's three-site sweep (cpp/src/cuda/rho_reduce.cu:49-110).
