@@ -430,6 +430,18 @@ class Batch:
         return lib().mipt_gb300_batch_launches(self._h)
 
 
+    def set_profiling(self, enable=True):
+        _check(lib().mipt_gb300_batch_set_profiling(self._h, int(enable)))
+
+    KERNEL_KINDS = ("pass", "hist", "measure", "observables", "other")
+
+    def kernel_stats(self):
+        ms = np.zeros(5)
+        n = np.zeros(5, np.int64)
+        _check(lib().mipt_gb300_batch_kernel_stats(self._h, _p(ms), _p(n)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
+
+
 class BatchGroup:
     """Batches executed as the parallel branches of one CUDA graph."""
 
@@ -453,17 +465,6 @@ class BatchGroup:
 
     def execute(self, stream=None):
         _check(lib().mipt_gb300_batch_group_execute(self._h, stream))
-
-    def set_profiling(self, enable=True):
-        _check(lib().mipt_gb300_batch_set_profiling(self._h, int(enable)))
-
-    KERNEL_KINDS = ("pass", "hist", "measure", "observables", "other")
-
-    def kernel_stats(self):
-        ms = np.zeros(5)
-        n = np.zeros(5, np.int64)
-        _check(lib().mipt_gb300_batch_kernel_stats(self._h, _p(ms), _p(n)))
-        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.KERNEL_KINDS)}
 
 
 class GmnConfig(ctypes.Structure):
