@@ -219,6 +219,9 @@ typedef struct mipt_gb300_batch_config
     int split_last;    /* RPPU: measure site n-1 as its own chunk after the others, as the
                           reference's parity-sector engine does (its default; MIPT_CUSV_PARITY=0
                           there is split_last = 0) -- cpp/include/mipt/cusv/engine.hpp:415-458 */
+    int full_state;    /* RPPU with split_last: 0 keeps the reference's parity-sector encoding, 2^(n-1)
+                          stored amplitudes per trajectory when every initial state has a definite parity
+                          (cpp/include/mipt/cusv/parity.hpp:170-252); 1 always keeps the full 2^n state */
 } mipt_gb300_batch_config;
 
 typedef struct mipt_gb300_batch mipt_gb300_batch;
@@ -236,6 +239,10 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *config, int capacity,
 int mipt_gb300_autotune_tile(int n_qubits, int fp64, int closed, int lattice_x, int lattice_y, int trajectories,
                              int *best_tile, int *candidates, double *ms_per_cycle, int *candidate_count);
 void mipt_gb300_batch_destroy(mipt_gb300_batch *batch);
+
+/* 1 if the prepared trajectories run on half-size parity-sector states (see
+ * full_state in mipt_gb300_batch_config), else 0. */
+int mipt_gb300_batch_parity_encoded(const mipt_gb300_batch *batch);
 
 /* Test hook for the bounded device waits (no reference counterpart; the
  * reference's failure contract is its status ladder, cpp/src/cuda/tmi_cuda_svd.cu:203-215).

@@ -39,7 +39,7 @@ class BatchConfig(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int) for name in (
         "n_qubits", "periods", "closed", "fp64", "chunk_bits", "observables", "observe_every", "rho3",
         "fermion_trace", "host_threads", "tile_qubits", "tmi_cycles", "lattice_x", "lattice_y", "circuit",
-        "split_last")]
+        "split_last", "full_state")]
 
 
 def lib():
@@ -103,6 +103,7 @@ def lib():
     L.mipt_gb300_batch_state.argtypes = [vp, ci]
     L.mipt_gb300_batch_state.restype = vp
     L.mipt_gb300_batch_launches.argtypes = [vp]
+    L.mipt_gb300_batch_parity_encoded.argtypes = [vp]
     L.mipt_gb300_batch_launches.restype = ctypes.c_longlong
     L.mipt_gb300_batch_set_profiling.argtypes = [vp, ci]
     L.mipt_gb300_batch_kernel_stats.argtypes = [vp, vp, vp]
@@ -307,11 +308,11 @@ class Batch:
 
     def __init__(self, n, periods, capacity, closed=True, fp64=False, chunk_bits=16, observables=0,
                  observe_every=0, rho3=False, fermion_trace=False, host_threads=0, tile_qubits=0, tmi_cycles=0,
-                 lattice=None, circuit=1, split_last=True):
+                 lattice=None, circuit=1, split_last=True, full_state=False):
         lx, ly = lattice if lattice is not None else (0, 0)
         cfg = BatchConfig(n, periods, int(closed), int(fp64), chunk_bits, observables, observe_every, int(rho3),
                           int(fermion_trace), host_threads, tile_qubits, tmi_cycles, lx, ly, int(circuit),
-                          int(split_last))
+                          int(split_last), int(full_state))
         self.regions = 0
         self.tmi_cycles = max(1, tmi_cycles)
         h = ctypes.c_void_p()
@@ -428,6 +429,11 @@ class Batch:
     @property
     def launches(self):
         return lib().mipt_gb300_batch_launches(self._h)
+
+    @property
+    def parity_encoded(self):
+        """Whether the prepared trajectories run on half-size parity-sector states."""
+        return bool(lib().mipt_gb300_batch_parity_encoded(self._h))
 
 
     def set_profiling(self, enable=True):

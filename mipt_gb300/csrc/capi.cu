@@ -186,12 +186,63 @@ __global__ void k_jw_closure(Cx<Real> *states, int n, int count)
     }
 }
 
+// Parity-sector states: trajectory b keeps the 2^ne amplitudes of its stored
+// qubits 0..ne-1 at cs[b * 2^ne ..]; qubit ne (the chain's top qubit) is
+// sector[b] xor the parity of the stored bits. Expansion writes the full
+// 2^(ne+1) state (at st[b * 2^(ne+1) ..]) with an optional pending collapse
+// applied; compaction reads a full state that lies in the sector.
+template <typename Real>
+__global__ void k_expand(const Cx<Real> *__restrict__ cs, Cx<Real> *__restrict__ st, int ne, int count,
+                         const signed char *__restrict__ sector, const Collapse *__restrict__ col,
+                         std::size_t col_stride)
+{
+    const std::uint64_t edim = 1ull << ne, dim = edim << 1;
+    const std::uint64_t total = dim * static_cast<std::uint64_t>(count);
+    for (std::uint64_t i = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const std::uint64_t b = i / dim, x = i % dim, c = x & (edim - 1);
+        const int top = static_cast<int>(x >> ne);
+        Cx<Real> v{Real(0), Real(0)};
+        if (top == ((sector[b] + __popcll(c)) & 1))
+        {
+            v = cs[b * edim + c];
+            if (col)
+            {
+                const Collapse cl = col[b * col_stride];
+                if (!collapse_keeps(c, cl))
+                    v = Cx<Real>{Real(0), Real(0)};
+                else
+                {
+                    const Real sc = static_cast<Real>(cl.scale);
+                    v = Cx<Real>{v.re * sc, v.im * sc};
+                }
+            }
+        }
+        st[i] = v;
+    }
+}
+
+template <typename Real>
+__global__ void k_compact(const Cx<Real> *__restrict__ st, Cx<Real> *__restrict__ cs, int ne, int b,
+                          const signed char *__restrict__ sector)
+{
+    const std::uint64_t edim = 1ull << ne;
+    for (std::uint64_t c = blockIdx.x * static_cast<std::uint64_t>(blockDim.x) + threadIdx.x; c < edim;
+         c += static_cast<std::uint64_t>(gridDim.x) * blockDim.x)
+    {
+        const std::uint64_t top = static_cast<std::uint64_t>((sector[b] + __popcll(c)) & 1);
+        cs[static_cast<std::uint64_t>(b) * edim + c] = st[(static_cast<std::uint64_t>(b) * edim << 1) + c +
+                                                          (top << ne)];
+    }
+}
+
 __global__ void k_reset_layers(Collapse *col, LayerResult *res, std::size_t n)
 {
     for (std::size_t i = blockIdx.x * static_cast<std::size_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<std::size_t>(gridDim.x) * blockDim.x)
     {
-        col[i] = Collapse{0ull, 0ull, 1.0, 0.0};
+        col[i] = Collapse{0ull, 0ull, 1.0, 0ull};
         LayerResult r{};
         res[i] = r;
     }
@@ -767,6 +818,18 @@ constexpr TileChoice kTunedTiles[] = {
     {20, 0, 1, 14},
 };
 
+// MIPT_GB300_PARITY_ENCODED=0 runs the RPPU / qRPPU gate sets on full-size
+// states (default: half-size parity-sector states where every trajectory has
+// a definite parity).
+bool use_parity_encoding()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_PARITY_ENCODED");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 // MIPT_GB300_SPARSE_PASS=0 makes the first pass after a measurement visit
 // every tile (default: only the tiles that agree with the outcome).
 bool use_sparse_pass()
@@ -842,6 +905,14 @@ struct mipt_gb300_batch
     std::uint64_t dim = 0;
     std::size_t elem = 0;
     std::vector<PassPlan> plan[4]; // per colour: 2 (1-D even/odd) or 4 (2-D)
+    // Parity-sector (half-size) execution of the RPPU / qRPPU gate sets: the
+    // plans over the n-1 stored qubits, whether the prepared trajectories
+    // run that way (every one in a definite parity sector), the compact
+    // states and the device copy of the sectors.
+    std::vector<PassPlan> plan_enc[2];
+    bool can_encode = false, enc = false;
+    std::vector<int> enc_sector; // the sectors the gates were uploaded for
+    DevBuf cstates, d_sector;
     int ncolour = 2;
     bool lattice = false;
     std::vector<int> region_slots; // request index of each added region
@@ -1372,6 +1443,8 @@ int set_rho3_subs(mipt_gb300_batch *b, const std::vector<int> &subs)
 } // namespace
 
 extern "C" {
+int mipt_gb300_batch_parity_encoded(const mipt_gb300_batch *b) { return (b && b->enc) ? 1 : 0; }
+
 int mipt_gb300_test_withhold_tile_loads(int count)
 {
     if (count < 0) return fail(MIPT_GB300_E_INVALID, "count must be >= 0");
@@ -1436,6 +1509,30 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
         for (int colour = 0; colour < b->ncolour; ++colour)
             b->plan[colour] = plan_layer(n, bonds[colour], b->kmax, b->cmin,
                                          cfg->fp64 ? register_bits<double>() : register_bits<float>());
+        if (rppu && n >= 8 && cfg->split_last && !cfg->full_state && use_parity_encoding())
+        {
+            // Half-size states: qubit n-1 is the parity of the others and of
+            // the sector, so a bond on (q, n-1) is a parity-selected 2x2 gate
+            // on q over n-1 stored qubits. Site n-1 must then be measured in
+            // a chunk of its own (split_last), as the reference's encoded
+            // engine does (cpp/include/mipt/cusv/engine.hpp:372-477).
+            for (int colour = 0; colour < 2; ++colour)
+            {
+                std::vector<Bond> eb;
+                for (const Bond &bd : bonds[colour])
+                {
+                    if (bd.q0 == n - 1)
+                        eb.push_back(Bond{bd.q1, -1});
+                    else if (bd.q1 == n - 1)
+                        eb.push_back(Bond{bd.q0, -1});
+                    else
+                        eb.push_back(bd);
+                }
+                b->plan_enc[colour] = plan_layer(n - 1, eb, b->kmax, b->cmin,
+                                                 cfg->fp64 ? register_bits<double>() : register_bits<float>());
+            }
+            b->can_encode = true;
+        }
     }
     catch (const std::exception &e)
     {
@@ -1491,6 +1588,12 @@ int mipt_gb300_batch_create(const mipt_gb300_batch_config *cfg, int capacity, mi
     const std::size_t C = static_cast<std::size_t>(capacity), T = b->T;
     cudaError_t e;
     if ((e = b->states.ensure(C * b->dim * b->elem)) != cudaSuccess) return cuda_fail(e, "state allocation");
+    if (b->can_encode)
+    {
+        if ((e = b->cstates.ensure(C * (b->dim / 2) * b->elem)) != cudaSuccess)
+            return cuda_fail(e, "parity-sector state allocation");
+        if ((e = b->d_sector.ensure(C)) != cudaSuccess) return cuda_fail(e, "sector allocation");
+    }
     if ((e = b->gates.ensure(C * T * b->G * 16 * b->elem)) != cudaSuccess) return cuda_fail(e, "gate allocation");
     if ((e = b->meas.ensure(C * T * sizeof(LayerMeas))) != cudaSuccess) return cuda_fail(e, "meas allocation");
     if ((e = b->forced.ensure(C * T * sizeof(std::uint64_t))) != cudaSuccess) return cuda_fail(e, "forced allocation");
@@ -1557,6 +1660,12 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
     b->direct_hist.assign(static_cast<std::size_t>(T) * kMaxChunks, 1);
     b->max_chunks.assign(T, 0);
     b->has_forced = forced != nullptr;
+    // Parity-sector execution needs every trajectory in a definite sector.
+    b->enc = b->can_encode;
+    for (int i = 0; i < count && b->enc; ++i)
+        if (b->sector[i] < 0) b->enc = false;
+    const int ne = b->enc ? n - 1 : n;
+    const auto *plans = b->enc ? b->plan_enc : b->plan;
     LayerMeas *hm = b->h_meas.as<LayerMeas>();
     std::uint64_t *hf = b->h_forced.as<std::uint64_t>();
     for (int i = 0; i < count; ++i)
@@ -1585,6 +1694,40 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
                 for (int r = 0; r < 4; ++r)
                     for (int c = 0; c < 4; ++c) u[4 * r + c] *= dg[r] * dg[c];
                 src = folded_layer.data();
+            }
+            std::vector<std::complex<double>> enc_layer;
+            if (b->enc)
+            {
+                // The layer's last bond touches qubit n-1: (n-2, n-1) in even
+                // layers (index bit0 = n-2), (n-1, 0) in odd ones (bit0 =
+                // n-1). As a parity-selected 2x2 on the other qubit q it keeps
+                // the pair (00, 11) when q's partner bit equals q (entries
+                // 0..3) and the pair (01, 10) otherwise (entries 4..7); the
+                // stored order puts the block for an even parity of the other
+                // stored bits first, so sector 1 swaps the two.
+                enc_layer.assign(src, src + static_cast<std::size_t>(G) * 16);
+                std::complex<double> *u = enc_layer.data() + static_cast<std::size_t>(G - 1) * 16;
+                const std::complex<double> g[16] = {u[0], u[1], u[2],  u[3],  u[4],  u[5],  u[6],  u[7],
+                                                    u[8], u[9], u[10], u[11], u[12], u[13], u[14], u[15]};
+                auto G4 = [&](int r, int c) { return g[4 * r + c]; };
+                const std::complex<double> E[4] = {G4(0, 0), G4(0, 3), G4(3, 0), G4(3, 3)};
+                std::complex<double> O[4];
+                if ((t & 1) == 0)
+                {
+                    O[0] = G4(2, 2), O[1] = G4(2, 1), O[2] = G4(1, 2), O[3] = G4(1, 1);
+                }
+                else
+                {
+                    O[0] = G4(1, 1), O[1] = G4(1, 2), O[2] = G4(2, 1), O[3] = G4(2, 2);
+                }
+                const bool swap = b->sector[i] == 1;
+                for (int e = 0; e < 4; ++e)
+                {
+                    u[e] = swap ? O[e] : E[e];
+                    u[4 + e] = swap ? E[e] : O[e];
+                    u[8 + e] = u[12 + e] = 0.0;
+                }
+                src = enc_layer.data();
             }
             if (b->cfg.fp64)
             {
@@ -1631,8 +1774,9 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
             for (int cc = 0; cc < M.nchunks; ++cc)
             {
                 M.uniform[cc] = d.uniforms[d.uniform_offset[t] + cc];
+                if (M.chunk[cc] >> ne) continue; // the parity chunk of a half-size state
                 PassGeom hg{};
-                histogram_geometry(n, b->kmax, b->cmin, M.chunk[cc], hg);
+                histogram_geometry(ne, b->kmax, b->cmin, M.chunk[cc], hg);
                 for (int li = 0; li < hg.k; ++li)
                     if ((M.chunk[cc] >> hg.pos[li]) & 1ull) b->direct_hist[static_cast<std::size_t>(t) * kMaxChunks + cc] = 0;
             }
@@ -1642,13 +1786,20 @@ int upload_draws(mipt_gb300_batch *b, const std::vector<TrajectoryDraw> &draws, 
             {
                 b->any_meas[t] = 1;
                 b->max_chunks[t] = std::max(b->max_chunks[t], M.nchunks);
-                const PassGeom &hg = fused_hist_geometry(b->plan[t % b->ncolour].back(), b->cfg.fp64 == 0);
+                const PassGeom &hg = fused_hist_geometry(plans[t % b->ncolour].back(), b->cfg.fp64 == 0);
                 const int ml = local_measured_count(hg, M.chunk[0]);
                 if ((std::size_t{1} << (hg.n_nl + ml)) > kHistScratch) b->fusable[t] = 0;
+                if (M.chunk[0] >> ne) b->fusable[t] = 0;
             }
         }
     }
     const std::size_t C = static_cast<std::size_t>(count);
+    if (b->enc)
+    {
+        b->enc_sector.assign(b->sector.begin(), b->sector.begin() + count);
+        std::vector<signed char> sec(b->sector.begin(), b->sector.begin() + count);
+        MG_CUDA(cudaMemcpy(b->d_sector.p, sec.data(), sec.size(), cudaMemcpyHostToDevice));
+    }
     MG_CUDA(cudaMemcpy(b->gates.p, b->h_gates.p, C * T * G * 16 * b->elem, cudaMemcpyHostToDevice));
     MG_CUDA(cudaMemcpy(b->meas.p, b->h_meas.p, C * T * sizeof(LayerMeas), cudaMemcpyHostToDevice));
     if (forced) MG_CUDA(cudaMemcpy(b->forced.p, b->h_forced.p, C * T * sizeof(std::uint64_t), cudaMemcpyHostToDevice));
@@ -1847,6 +1998,16 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
 {
     const int n = b->cfg.n_qubits, T = b->T, G = b->G, count = b->count;
     Cx<Real> *states = b->states.as<Cx<Real>>();
+    // Parity-sector execution: the layers run on the compact states (ne
+    // stored qubits); observables and the final state are expanded into
+    // `states`.
+    const bool enc = b->enc;
+    const int ne = enc ? n - 1 : n;
+    const std::uint64_t edim = 1ull << ne;
+    Cx<Real> *xs = enc ? b->cstates.as<Cx<Real>>() : states;
+    const signed char *sec = enc ? b->d_sector.as<signed char>() : nullptr;
+    const auto *plans = enc ? b->plan_enc : b->plan;
+    const int xgrid = static_cast<int>(std::min<std::uint64_t>(152ull * 16, (edim * 2 * count + 255) / 256));
     const Cx<Real> *gates = b->gates.as<Cx<Real>>();
     LayerMeas *meas = b->meas.as<LayerMeas>();
     Collapse *col = b->col.as<Collapse>();
@@ -1862,14 +2023,21 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
         for (int i = 0; i < count; ++i) custom += b->custom_init[i] ? 1 : 0;
         if (custom == 0)
         {
-            MG_CUDA(launch_init_zero<Real>(states, b->dim, count, s));
+            MG_CUDA(launch_init_zero<Real>(xs, edim, count, s));
             ++L;
         }
         else
             for (int i = 0; i < count; ++i)
                 if (!b->custom_init[i])
                 {
-                    MG_CUDA(launch_init_zero<Real>(states + static_cast<std::size_t>(i) * b->dim, b->dim, 1, s));
+                    MG_CUDA(launch_init_zero<Real>(xs + static_cast<std::size_t>(i) * edim, edim, 1, s));
+                    ++L;
+                }
+                else if (enc)
+                {
+                    k_compact<Real><<<static_cast<int>(std::min<std::uint64_t>(4096, (edim + 255) / 256)), 256, 0,
+                                      s>>>(states, xs, ne, i, sec);
+                    MG_CUDA(cudaGetLastError());
                     ++L;
                 }
         std::fill(b->custom_init.begin(), b->custom_init.end(), 0);
@@ -1887,6 +2055,12 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                 return fail(MIPT_GB300_E_INVALID,
                             "FermionRPPU: set the initial states before mipt_gb300_batch_prepare_haar*");
         }
+    if (enc)
+        for (int i = 0; i < count; ++i)
+            if (b->sector[i] != b->enc_sector[i])
+                return fail(MIPT_GB300_E_INVALID, "parity-sector batch: set the initial states before "
+                                                  "mipt_gb300_batch_prepare_haar* (the gates are uploaded for "
+                                                  "the initial states' sectors)");
     std::fill(b->sector.begin(), b->sector.end(), 0);
     const std::size_t slots = static_cast<std::size_t>(count) * T;
     k_reset_layers<<<std::min<std::size_t>((slots + 255) / 256, 1024), 256, 0, s>>>(col, res, slots);
@@ -1904,6 +2078,14 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     // Observations of point `point` on the current states (`pending`: the
     // collapse each trajectory still owes, or null).
     auto observe = [&](int point, const Collapse *pending) -> int {
+        if (enc)
+        {
+            Mark m(b, K_OTHER, s);
+            k_expand<Real><<<xgrid, 256, 0, s>>>(xs, states, ne, count, sec, pending, T);
+            MG_CUDA(cudaGetLastError());
+            ++L;
+            pending = nullptr;
+        }
         if (b->reqs_per_point > 0)
         {
             std::vector<EntReq> reqs;
@@ -1940,7 +2122,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     const std::size_t gstride = static_cast<std::size_t>(T) * G * 16;
     for (int t = 0; t < T; ++t)
     {
-        const auto &plan = b->plan[t % b->ncolour];
+        const auto &plan = plans[t % b->ncolour];
         const bool fuse = b->any_meas[t] && b->fusable[t];
         // Fermionic closure: the odd layer's gates run between two JW strings;
         // every other odd-layer bond lies inside the string and preserves its
@@ -1977,7 +2159,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             }
             const bool last = pi + 1 == plan.size();
             Mark m(b, K_PASS, s);
-            MG_CUDA(launch_pass<Real>(states, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
+            MG_CUDA(launch_pass<Real>(xs, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
                                       cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0,
                                       b->err.as<int>(), s, keep, scaled, sparse && pi == 0 ? 1 : 0));
             ++L;
@@ -1991,17 +2173,18 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                 if (!fused)
                 {
                     Mark m(b, K_HIST, s);
-                    MG_CUDA(launch_hist<Real>(states, count, n, b->kmax, b->cmin, ci, col + t, T, meas + t, T,
+                    MG_CUDA(launch_hist<Real>(xs, count, ne, b->kmax, b->cmin, ci, col + t, T, meas + t, T,
                                               b->part.as<double>(),
-                                              b->direct_hist[static_cast<std::size_t>(t) * kMaxChunks + ci] != 0, s));
+                                              b->direct_hist[static_cast<std::size_t>(t) * kMaxChunks + ci] != 0, s,
+                                              sec));
                     ++L;
                 }
                 Mark m(b, K_MEASURE, s);
-                MG_CUDA(launch_measure(count, n, fused ? &fused_hist_geometry(plan.back(), sizeof(Real) == 4) : nullptr,
+                MG_CUDA(launch_measure(count, ne, fused ? &fused_hist_geometry(plan.back(), sizeof(Real) == 4) : nullptr,
                                        b->kmax, b->cmin, ci, meas + t, T,
                                        b->part.as<double>(), b->bins.as<double>(),
                                        std::size_t{1} << b->cfg.chunk_bits, forced ? forced + t : nullptr, T,
-                                       col + t, T, res + t, T, b->err.as<int>(), s));
+                                       col + t, T, res + t, T, b->err.as<int>(), s, sec));
                 ++L;
             }
         }
@@ -2019,7 +2202,13 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     // Leave every trajectory in its collapsed, normalised final state.
     {
         Mark m(b, K_OTHER, s);
-        MG_CUDA(launch_collapse<Real>(states, b->dim, count, col + (T - 1), T, s));
+        if (enc)
+        {
+            k_expand<Real><<<xgrid, 256, 0, s>>>(xs, states, ne, count, sec, col + (T - 1), T);
+            MG_CUDA(cudaGetLastError());
+        }
+        else
+            MG_CUDA(launch_collapse<Real>(states, b->dim, count, col + (T - 1), T, s));
     }
     ++L;
     if (b->reqs_per_point > 0 && !b->per_point())
@@ -2070,7 +2259,7 @@ int execute_any(mipt_gb300_batch *b, cudaStream_t s)
 std::vector<long long> structure_key(const mipt_gb300_batch *b)
 {
     std::vector<long long> k{b->count, b->has_forced ? 1 : 0, b->points, b->reqs_per_point, b->rho3_count,
-                             b->tmi_cycles};
+                             b->tmi_cycles, b->enc ? 1 : 0};
     for (char c : b->any_meas) k.push_back(c);
     for (char c : b->fusable) k.push_back(c);
     for (int c : b->max_chunks) k.push_back(c);

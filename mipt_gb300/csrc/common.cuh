@@ -59,14 +59,30 @@ constexpr int kMaxLocal = 15;
 constexpr int kMaxPassGates = 16;
 
 // Pending projective collapse of a trajectory: amplitudes whose bits on `mask`
-// differ from `value` become zero, the rest are multiplied by `scale`.
+// differ from `value` become zero, the rest are multiplied by `scale`. A
+// nonzero `parity` (parity-sector states, whose top qubit is the parity of
+// the others) also zeroes the amplitudes whose bits on parity & ~kParityBit
+// have a parity other than the bit kParityBit of `parity`.
 struct Collapse
 {
     std::uint64_t mask;
     std::uint64_t value;
     double scale;
-    double pad;
+    std::uint64_t parity;
 };
+constexpr std::uint64_t kParityBit = 1ull << 63;
+
+__host__ __device__ __forceinline__ bool collapse_keeps(std::uint64_t idx, const Collapse &cl)
+{
+    if ((idx & cl.mask) != cl.value) return false;
+    if (cl.parity == 0) return true;
+#ifdef __CUDA_ARCH__
+    const int par = __popcll(idx & cl.parity & ~kParityBit) & 1;
+#else
+    const int par = __builtin_popcountll(idx & cl.parity & ~kParityBit) & 1;
+#endif
+    return par == static_cast<int>(cl.parity >> 63);
+}
 
 // Geometry of one tiled pass over a 2^n state. A tile holds 2^k amplitudes:
 // local bit i <-> qubit pos[i]; the first `c` local bits are the contiguous
@@ -83,12 +99,16 @@ struct PassGeom
 
 // Gates of one pass: indices into the layer's gate list plus local bit
 // positions of the gate's two qubits (a = matrix bit 0, b = matrix bit 1).
+// kind 1: a parity-selected 2x2 gate on qubit a of a parity-sector state
+// (gate entries 0..3 when the other qubits' parity is even, 4..7 when odd,
+// both row-major); b is an untouched partner the register rounds pair it with.
 struct PassGates
 {
     int count;
     std::int16_t gate[kMaxPassGates];
     std::int8_t la[kMaxPassGates];
     std::int8_t lb[kMaxPassGates];
+    std::int8_t kind[kMaxPassGates];
 };
 
 } // namespace mg

@@ -133,7 +133,7 @@ __device__ void tile_histogram(const Cx<Real> *tile, int k, const int *lm, int m
 template <typename Real>
 __device__ __forceinline__ Cx<Real> collapse_value(Cx<Real> v, std::uint64_t gidx, const Collapse &cl, Real scale)
 {
-    if ((gidx & cl.mask) != cl.value) return Cx<Real>{Real(0), Real(0)};
+    if (!collapse_keeps(gidx, cl)) return Cx<Real>{Real(0), Real(0)};
     return Cx<Real>{v.re * scale, v.im * scale};
 }
 
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(Cx<Real> *__restrict__ st
         seg[s] = static_cast<std::uint32_t>(scatter_bits(s, g.pos + g.c, h));
     for (int i = threadIdx.x; i < pg.count * 16; i += blockDim.x)
         U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(pg.gate[i / 16]) * 16 + (i % 16)];
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col_in != nullptr;
     if (has_col) cl = col_in[b * col_stride];
     __syncthreads();
@@ -187,8 +187,28 @@ __global__ void __launch_bounds__(kPassThreads) k_pass(Cx<Real> *__restrict__ st
     __syncthreads();
 
     const std::uint64_t groups = 1ull << (g.k - 2);
+    const int bpar = __popcll(base) & 1;
     for (int gi = 0; gi < pg.count; ++gi)
     {
+        if (pg.kind[gi])
+        {
+            // Parity-selected 2x2 on local bit la: the block is chosen by the
+            // parity of the element's other index bits (tile base + local).
+            const int a = pg.la[gi];
+            Cx<Real> u[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) u[e] = U[gi][e];
+            for (std::uint64_t pr = threadIdx.x; pr < (1ull << (g.k - 1)); pr += blockDim.x)
+            {
+                const std::uint64_t j0 = insert_zero(pr, a), j1 = j0 | (1ull << a);
+                const int o = ((bpar + __popcll(j0)) & 1) * 4;
+                const Cx<Real> x0 = tile[j0], x1 = tile[j1];
+                tile[j0] = cfma(u[o + 1], x1, cmul(u[o], x0));
+                tile[j1] = cfma(u[o + 3], x1, cmul(u[o + 2], x0));
+            }
+            __syncthreads();
+            continue;
+        }
         const int a = pg.la[gi], bb = pg.lb[gi];
         const int lo = a < bb ? a : bb, hi = a < bb ? bb : a;
         Cx<Real> u[16];
@@ -487,6 +507,45 @@ __device__ __forceinline__ void apply_slot_fast(Cx<Real> (&a)[NA], const Cx<Real
     apply_slot<S>(a, Us);
 }
 
+// Parity-selected 2x2 gate on register bit 2S of a parity-sector state: the
+// pair (r, r | bit 2S) gets Us[0..3] when the parity of the element's other
+// index bits is even and Us[4..7] when it is odd. Those bits are the
+// thread's (tpar: the parity of the tile base and the thread index, which
+// map one to one onto index bits) plus register bits other than 2S (a
+// compile-time parity per r).
+template <int S, typename Real, int NA>
+__device__ __forceinline__ void apply_parity_slot(Cx<Real> (&a)[NA], const Cx<Real> *__restrict__ Us, int tpar)
+{
+    Cx<Real> A[4], B[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+    {
+        const Cx<Real> e = Us[i], o = Us[4 + i];
+        A[i] = tpar ? o : e; // register parity even
+        B[i] = tpar ? e : o; // register parity odd
+    }
+#pragma unroll
+    for (int r = 0; r < NA; ++r)
+    {
+        if ((r >> (2 * S)) & 1) continue;
+        const int r1 = r | (1 << (2 * S));
+        int pr = 0;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) pr ^= (r >> b) & 1;
+        const Cx<Real> x0 = a[r], x1 = a[r1];
+        if (pr)
+        {
+            a[r] = cfma(B[1], x1, cmul(B[0], x0));
+            a[r1] = cfma(B[3], x1, cmul(B[2], x0));
+        }
+        else
+        {
+            a[r] = cfma(A[1], x1, cmul(A[0], x0));
+            a[r1] = cfma(A[3], x1, cmul(A[2], x0));
+        }
+    }
+}
+
 __device__ __forceinline__ std::uint32_t smem_u32(const void *p)
 {
     return static_cast<std::uint32_t>(__cvta_generic_to_shared(p));
@@ -746,11 +805,12 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
         __syncthreads(); // the previous item's shared-memory reads are complete
         Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
         const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
+        const int tpar = (__popcll(base) + __popc(static_cast<unsigned>(tid))) & 1;
         if (b != cur_b)
             for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
                 U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
         cur_b = b;
-        Collapse cl{0, 0, 1.0, 0.0};
+        Collapse cl{0, 0, 1.0, 0};
         const bool has_col = col_in != nullptr;
         if (has_col)
         {
@@ -889,9 +949,27 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                     }
                 }
             }
-            if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
-            if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
-            if (RB >= 6 && R.slot[2] >= 0) apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
+            if (R.slot[0] >= 0)
+            {
+                if (P.gates.kind[R.slot[0]])
+                    apply_parity_slot<0>(amp, U[R.slot[0]], tpar);
+                else
+                    apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+            }
+            if (RB >= 4 && R.slot[1] >= 0)
+            {
+                if (P.gates.kind[R.slot[1]])
+                    apply_parity_slot<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], tpar);
+                else
+                    apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
+            }
+            if (RB >= 6 && R.slot[2] >= 0)
+            {
+                if (P.gates.kind[R.slot[2]])
+                    apply_parity_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], tpar);
+                else
+                    apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
+            }
         }
 
         const Round &Z = P.round[P.rounds - 1];
@@ -991,7 +1069,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(1 << (13 - RB), 2)
     const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
     for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
         U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col_in != nullptr;
     if (has_col) cl = col_in[b * col_stride];
     const float scale = static_cast<float>(cl.scale);
@@ -1156,7 +1234,7 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
                                                        int ci, const Collapse *__restrict__ col_in,
                                                        std::size_t col_stride, const LayerMeas *__restrict__ meas,
                                                        std::size_t meas_stride, double *__restrict__ partials,
-                                                       int direct)
+                                                       int direct, const signed char *__restrict__ sector)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ PassGeom g;
@@ -1165,7 +1243,12 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
     const LayerMeas &M = meas[b * meas_stride];
     if (ci >= M.nchunks) return;
     const std::uint64_t chunk = M.chunk[ci];
-    if (threadIdx.x == 0) histogram_geometry(n, kmax, cmin, chunk, g);
+    // A chunk at bit n of a parity-sector state (n qubits stored, the top
+    // qubit of the chain being the parity of the others and of the
+    // trajectory's sector) is that top qubit alone: its two bins sum the
+    // amplitudes by parity, over tiles of the geometry of an empty chunk.
+    const bool par_chunk = (chunk >> n) != 0ull;
+    if (threadIdx.x == 0) histogram_geometry(n, kmax, cmin, par_chunk ? 0ull : chunk, g);
     __syncthreads();
     Cx<Real> *tile = reinterpret_cast<Cx<Real> *>(smem_raw);
     std::uint32_t *seg = reinterpret_cast<std::uint32_t *>(direct ? smem_raw : smem_raw + (sizeof(Cx<Real>) << g.k));
@@ -1176,10 +1259,42 @@ __global__ void __launch_bounds__(kPassThreads) k_hist(const Cx<Real> *__restric
     const int h = g.k - g.c;
     for (std::uint32_t s = threadIdx.x; s < (1u << h); s += blockDim.x)
         seg[s] = static_cast<std::uint32_t>(scatter_bits(s, g.pos + g.c, h));
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col_in != nullptr;
     if (has_col) cl = col_in[b * col_stride];
     __syncthreads();
+    if (par_chunk)
+    {
+        // Tile bins (top qubit 0, 1) in the order of the direct sum below.
+        const int P = sector ? sector[b] : 0;
+        const std::uint64_t nloc = 1ull << g.k, cmask = (1ull << g.c) - 1ull;
+        const Real scale = static_cast<Real>(cl.scale);
+        Acc<Real> acc[2];
+        for (std::uint64_t r = threadIdx.x; r < nloc; r += blockDim.x)
+        {
+            const std::uint64_t gidx = base | seg[r >> g.c] | (r & cmask);
+            Cx<Real> v = psi[gidx];
+            if (has_col) v = collapse_value(v, gidx, cl, scale);
+            const int bit = (P + __popcll(gidx)) & 1;
+            acc[bit].add(norm2(v));
+        }
+        double *pp = partials + static_cast<std::size_t>(b) * kHistScratch + (tix << 1);
+        for (int bin = 0; bin < 2; ++bin)
+        {
+            double v = acc[bin].value();
+            for (int off = 16; off > 0; off /= 2) v += __shfl_down_sync(0xffffffffu, v, off, 32);
+            __syncthreads();
+            if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                double t = 0.0;
+                for (int w = 0; w < static_cast<int>(blockDim.x) / 32; ++w) t += red[w];
+                pp[bin] = t;
+            }
+        }
+        return;
+    }
     int lm[kMaxLocal + 1];
     int m_loc = 0;
     for (int i = 0; i < g.k; ++i)
@@ -1250,7 +1365,8 @@ __global__ void __launch_bounds__(kMeasureThreads)
     k_measure(int n, PassGeom fg, int fused, int kmax, int cmin, int ci, const LayerMeas *__restrict__ meas,
               std::size_t meas_stride, const double *__restrict__ partials, double *__restrict__ bins_scratch,
               std::size_t bins_stride, const std::uint64_t *__restrict__ forced, std::size_t forced_stride, Collapse *__restrict__ col,
-              std::size_t col_stride, LayerResult *__restrict__ res, std::size_t res_stride, int *__restrict__ err)
+              std::size_t col_stride, LayerResult *__restrict__ res, std::size_t res_stride, int *__restrict__ err,
+              const signed char *__restrict__ sector)
 {
     __shared__ PassGeom g;
     __shared__ double sbins[kSmemBins];
@@ -1267,23 +1383,36 @@ __global__ void __launch_bounds__(kMeasureThreads)
     const int m = __popcll(chunk);
     const int tid = threadIdx.x;
     const int T = blockDim.x;
+    // Parity-sector state: a chunk at bit n is the chain's top qubit, whose
+    // two bins k_hist wrote per tile as if it were the tile's lowest local bit.
+    const bool par_chunk = (chunk >> n) != 0ull;
     if (tid == 0)
     {
-        if (fused)
-            g = fg;
+        if (par_chunk)
+        {
+            histogram_geometry(n, kmax, cmin, 0ull, g);
+            lm_bit[0] = 0;
+            s_mloc = 1;
+            s_mhi = 0;
+        }
         else
-            histogram_geometry(n, kmax, cmin, chunk, g);
-        int ml = 0, mh = 0;
-        for (int i = 0; i < g.k; ++i)
-            if ((chunk >> g.pos[i]) & 1ull) lm_bit[ml++] = __popcll(chunk & ((1ull << g.pos[i]) - 1ull));
-        for (int i = 0; i < g.n_nl; ++i)
-            if ((chunk >> g.nl[i]) & 1ull)
-            {
-                hm_pos[mh] = i;
-                hm_bit[mh++] = __popcll(chunk & ((1ull << g.nl[i]) - 1ull));
-            }
-        s_mloc = ml;
-        s_mhi = mh;
+        {
+            if (fused)
+                g = fg;
+            else
+                histogram_geometry(n, kmax, cmin, chunk, g);
+            int ml = 0, mh = 0;
+            for (int i = 0; i < g.k; ++i)
+                if ((chunk >> g.pos[i]) & 1ull) lm_bit[ml++] = __popcll(chunk & ((1ull << g.pos[i]) - 1ull));
+            for (int i = 0; i < g.n_nl; ++i)
+                if ((chunk >> g.nl[i]) & 1ull)
+                {
+                    hm_pos[mh] = i;
+                    hm_bit[mh++] = __popcll(chunk & ((1ull << g.nl[i]) - 1ull));
+                }
+            s_mloc = ml;
+            s_mhi = mh;
+        }
     }
     __syncthreads();
     const int m_loc = s_mloc, m_hi = s_mhi;
@@ -1332,6 +1461,7 @@ __global__ void __launch_bounds__(kMeasureThreads)
             int j = 0;
             for (int q = 0; q < n; ++q)
                 if ((chunk >> q) & 1ull) chosen |= ((f >> q) & 1ull) << j++;
+            if (par_chunk) chosen = (f >> n) & 1ull;
         }
         else if (!bad)
         {
@@ -1386,10 +1516,25 @@ __global__ void __launch_bounds__(kMeasureThreads)
         int j = 0;
         for (int q = 0; q < n; ++q)
             if ((chunk >> q) & 1ull) val |= ((chosen >> j++) & 1ull) << q;
+        if (par_chunk) val = (chosen & 1ull) << n;
         const bool ok = branch > 0.0 && total > 0.0 && isfinite(total);
         const double scale = ok ? 1.0 / sqrt(branch) : 1.0;
         Collapse &c = col[b * col_stride];
-        if (ci == 0)
+        if (par_chunk)
+        {
+            // Top qubit = chosen: the stored bits' parity is sector ^ chosen.
+            const std::uint64_t want = static_cast<std::uint64_t>(((sector ? sector[b] : 0) ^ chosen) & 1);
+            c.parity = ((1ull << n) - 1ull) | (want << 63);
+            if (ci == 0)
+            {
+                c.mask = 0;
+                c.value = 0;
+                c.scale = scale;
+            }
+            else
+                c.scale *= scale;
+        }
+        else if (ci == 0)
         {
             c.mask = chunk;
             c.value = val;
@@ -1598,7 +1743,8 @@ std::vector<PassPlan> pack(int n, const std::vector<Bond> &bonds, std::vector<in
         std::vector<int> taken, rest;
         for (int i : todo)
         {
-            const std::uint64_t need = local | (1ull << bonds[i].q0) | (1ull << bonds[i].q1);
+            const std::uint64_t need =
+                local | (1ull << bonds[i].q0) | (bonds[i].q1 >= 0 ? (1ull << bonds[i].q1) : 0ull);
             if (__builtin_popcountll(need) <= kmax && (taken.size() < static_cast<std::size_t>(kMaxPassGates)))
             {
                 if (first && (need != local))
@@ -1620,11 +1766,29 @@ std::vector<PassPlan> pack(int n, const std::vector<Bond> &bonds, std::vector<in
         PassPlan p{};
         p.geom = make_geom(n, local);
         p.gates.count = static_cast<int>(taken.size());
+        std::uint64_t used = 0;
+        for (int i : taken)
+            used |= (1ull << bonds[i].q0) | (bonds[i].q1 >= 0 ? (1ull << bonds[i].q1) : 0ull);
         for (std::size_t j = 0; j < taken.size(); ++j)
         {
+            const Bond &bd = bonds[taken[j]];
             p.gates.gate[j] = static_cast<std::int16_t>(taken[j]);
-            p.gates.la[j] = static_cast<std::int8_t>(local_index(p.geom, bonds[taken[j]].q0));
-            p.gates.lb[j] = static_cast<std::int8_t>(local_index(p.geom, bonds[taken[j]].q1));
+            p.gates.la[j] = static_cast<std::int8_t>(local_index(p.geom, bd.q0));
+            int q1 = bd.q1;
+            p.gates.kind[j] = 0;
+            if (q1 < 0)
+            {
+                // Parity gate: pair it with a local qubit no other gate of
+                // the pass touches.
+                p.gates.kind[j] = 1;
+                for (int q = 0; q < n && q1 < 0; ++q)
+                    if (((local >> q) & 1ull) && !((used >> q) & 1ull)) q1 = q;
+                if (q1 < 0)
+                    q1 = bd.q0; // no free partner: the pass runs on the shared-memory kernel
+                else
+                    used |= 1ull << q1;
+            }
+            p.gates.lb[j] = static_cast<std::int8_t>(local_index(p.geom, q1));
         }
         if (!taken.empty()) out.push_back(p);
         todo = rest;
@@ -1984,8 +2148,18 @@ std::vector<PassPlan> plan_layer(int n, const std::vector<Bond> &bonds, int kmax
     }
     for (auto &p : best)
     {
+        bool unpaired = false;
+        for (int j = 0; j < p.gates.count; ++j) unpaired = unpaired || (p.gates.kind[j] && p.gates.la[j] == p.gates.lb[j]);
+        if (unpaired)
+        {
+            p.rounds = 0;
+            p.cluster_rounds = 0;
+            continue;
+        }
         plan_rounds(p, rb);
-        if (rb >= 5) plan_cluster_rounds(p, cluster_register_bits());
+        bool parity = false;
+        for (int j = 0; j < p.gates.count; ++j) parity = parity || p.gates.kind[j];
+        if (rb >= 5 && !parity) plan_cluster_rounds(p, cluster_register_bits());
     }
     return best;
 }
@@ -2197,7 +2371,8 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
                         const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
-                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s)
+                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s,
+                        const signed char *sector)
 {
     const int k = std::min(kmax, n);
     // Direct (all measured sites outside the tile): only the segment table.
@@ -2207,7 +2382,7 @@ cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int 
     if (e != cudaSuccess) return e;
     dim3 grid(1u << (n - k), batch);
     k_hist<Real><<<grid, kPassThreads, smem, s>>>(states, n, kmax, cmin, chunk_index, collapse_in, collapse_stride,
-                                                  meas, meas_stride, partials, direct ? 1 : 0);
+                                                  meas, meas_stride, partials, direct ? 1 : 0, sector);
     return cudaGetLastError();
 }
 
@@ -2215,14 +2390,16 @@ cudaError_t launch_measure(int batch, int n, const PassGeom *fused_geom, int kma
                            const LayerMeas *meas, std::size_t meas_stride, const double *partials,
                            double *bins_scratch, std::size_t bins_stride, const std::uint64_t *forced,
                            std::size_t forced_stride, Collapse *collapse_out, std::size_t collapse_stride,
-                           LayerResult *result, std::size_t result_stride, int *error_flag, cudaStream_t s)
+                           LayerResult *result, std::size_t result_stride, int *error_flag, cudaStream_t s,
+                           const signed char *sector)
 {
     PassGeom fg{};
     if (fused_geom) fg = *fused_geom;
     k_measure<<<batch, kMeasureThreads, 0, s>>>(n, fg, fused_geom != nullptr, kmax, cmin, chunk_index, meas,
                                                 meas_stride, partials, bins_scratch, bins_stride, forced,
                                                 forced_stride,
-                                                collapse_out, collapse_stride, result, result_stride, error_flag);
+                                                collapse_out, collapse_stride, result, result_stride, error_flag,
+                                                sector);
     return cudaGetLastError();
 }
 
@@ -2243,7 +2420,8 @@ void set_withheld_tile_loads(int count) { g_withheld_loads.store(count > 0 ? cou
                                         const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
                                         int, int *, cudaStream_t, std::uint64_t, int, int);                      \
     template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
-                                        const LayerMeas *, std::size_t, double *, bool, cudaStream_t);           \
+                                        const LayerMeas *, std::size_t, double *, bool, cudaStream_t,            \
+                                        const signed char *);                                                    \
     template cudaError_t launch_collapse<R>(Cx<R> *, std::uint64_t, int, const Collapse *, std::size_t,          \
                                             cudaStream_t);
 MG_INSTANTIATE(float)

@@ -24,7 +24,7 @@ namespace mg
 
 struct Bond
 {
-    int q0, q1; // matrix index bit 0 <-> q0, bit 1 <-> q1
+    int q0, q1; // matrix index bit 0 <-> q0, bit 1 <-> q1; q1 = -1: parity-selected 2x2 gate on q0
 };
 
 // One register round of a pass: every thread holds 2^rb amplitudes whose
@@ -162,16 +162,21 @@ inline std::uint64_t nonlocal_mask(const PassGeom &g)
 template <typename Real>
 cudaError_t launch_hist(const Cx<Real> *states, int batch, int n, int kmax, int cmin, int chunk_index,
                         const Collapse *collapse_in, std::size_t collapse_stride, const LayerMeas *meas,
-                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s);
+                        std::size_t meas_stride, double *partials, bool direct, cudaStream_t s,
+                        const signed char *sector = nullptr);
 
 // Samples (or replays) the outcome of chunk `chunk_index` from the partial
 // histograms, writes the combined collapse of the layer and the outcome.
+// Parity-sector states (n stored qubits): a chunk at bit n is the chain's top
+// qubit; sector[b] (0 or 1) is trajectory b's total parity, its outcome lands
+// at bit n of the outcome mask and its collapse is a parity condition.
 cudaError_t launch_measure(int batch, int n, const PassGeom *fused_geom, int kmax, int cmin, int chunk_index,
                            const LayerMeas *meas, std::size_t meas_stride, const double *partials,
                            double *bins_scratch, std::size_t bins_stride, const std::uint64_t *forced,
                            std::size_t forced_stride,
                            Collapse *collapse_out, std::size_t collapse_stride, LayerResult *result,
-                           std::size_t result_stride, int *error_flag, cudaStream_t s);
+                           std::size_t result_stride, int *error_flag, cudaStream_t s,
+                           const signed char *sector = nullptr);
 
 template <typename Real>
 cudaError_t launch_collapse(Cx<Real> *states, std::uint64_t dim, int batch, const Collapse *collapse,

@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(kGramThreads)
             if ((i >> b) & 1) o |= 1ull << J.env[b];
         elo[i] = o;
     }
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col != nullptr;
     if (has_col) cl = col[J.traj * col_stride];
     __syncthreads();
@@ -603,7 +603,7 @@ __global__ void __launch_bounds__(R3_THREADS)
         cross[tid] = fermion ? x : 0ull;
         isign[tid] = (fermion && par) ? -1 : 1;
     }
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col != nullptr;
     if (has_col) cl = col[traj * col_stride];
     __syncthreads();
@@ -1040,7 +1040,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if ((i >> b) & 1) o |= 1ull << J.env[b];
         elo[i] = o;
     }
-    Collapse cl{0, 0, 1.0, 0.0};
+    Collapse cl{0, 0, 1.0, 0};
     const bool has_col = col != nullptr;
     if (has_col) cl = col[J.traj * col_stride];
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -1408,7 +1408,7 @@ __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, 
         const int j = static_cast<int>(idx >> (k + cbits));
         const int t = jobs[j].traj;
         const Cx<float> *psi = states + (static_cast<std::size_t>(t) << n);
-        Collapse cl{0, 0, 1.0, 0.0};
+        Collapse cl{0, 0, 1.0, 0};
         if (col != nullptr) cl = col[t * col_stride];
         const float scale = static_cast<float>(cl.scale);
         float re[16], im[16];
