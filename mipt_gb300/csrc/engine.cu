@@ -814,12 +814,18 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
         const bool has_col = col_in != nullptr;
         if (has_col)
         {
-            // col_keep < all ones: the residual of a collapse whose scale an
-            // earlier pass of the layer applied (the bits that pass skipped).
+            // col_keep < all ones: the residual of a collapse that an earlier
+            // pass of the layer applied to every tile it visited; only the
+            // bits of the tiles it skipped are left. A parity condition is not
+            // (that pass's gates may have changed the stored bits' parity).
             cl = col_in[b * col_stride];
             cl.mask &= col_keep;
             cl.value &= col_keep;
-            if (!col_scaled) cl.scale = 1.0;
+            if (!col_scaled)
+            {
+                cl.scale = 1.0;
+                cl.parity = 0;
+            }
         }
         const Real scale = static_cast<Real>(cl.scale);
 
