@@ -2161,7 +2161,7 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             Mark m(b, K_PASS, s);
             MG_CUDA(launch_pass<Real>(xs, count, plan[pi], gates + static_cast<std::size_t>(t) * G * 16, gstride,
                                       cin, T, meas + t, T, b->part.as<double>(), last && fuse ? 1 : 0,
-                                      b->err.as<int>(), s, keep, scaled, sparse && pi == 0 ? 1 : 0));
+                                      b->err.as<int>(), s, keep, scaled, sparse && pi == 0 ? 1 : 0, enc ? 1 : 0));
             ++L;
         }
         if (jw) jw_closure();

@@ -9,7 +9,8 @@
 // own, written from the textbook algorithms:
 //
 //   k_tridiag   one CTA per matrix: Householder reduction of the Hermitian
-//               matrix (full storage, row-major, interleaved re/im) to a real
+//               matrix (row-major, interleaved re/im, the lower triangle
+//               read and updated) to a real
 //               symmetric tridiagonal matrix. Step j reflects the column below
 //               the diagonal onto alpha e_1 with H = I - beta v v^H,
 //               v = x - alpha e_1, alpha = -phase(x_0) |x|, beta = 2 / |v|^2,
@@ -24,8 +25,8 @@
 //               Numerical Recipes, eigenvalues only), then the entropy.
 //
 // All reductions run in a fixed order, so results are reproducible.
-// FP64 throughout: GB300's FP64 rate bounds the reduction at 8 d^3 flops per
-// matrix (full-storage update).
+// FP64 throughout: GB300's FP64 rate bounds the reduction at about 16/3 d^3
+// flops per matrix (full matrix-vector product, lower-triangle update).
 #include "observables.cuh"
 
 #include <cuda_runtime.h>
@@ -127,12 +128,12 @@ __global__ void __launch_bounds__(kTriThreads)
     {
         const int m = d - 1 - j, r0 = j + 1;
         __syncthreads(); // the previous step's reads of v[] and w[] are done
-        // x = column j below the diagonal = conj of row j right of it.
+        // x = column j below the diagonal (the lower triangle is the valid
+        // half of the trailing block).
         double part_sum = 0.0;
         for (int i = tid; i < m; i += nt)
         {
-            const double2 r = a[static_cast<std::size_t>(j) * d + r0 + i];
-            const double2 x = make_double2(r.x, -r.y);
+            const double2 x = a[static_cast<std::size_t>(r0 + i) * d + j];
             v[i] = x;
             if (i > 0) part_sum += x.x * x.x + x.y * x.y;
         }
@@ -151,33 +152,39 @@ __global__ void __launch_bounds__(kTriThreads)
         __syncthreads(); // every thread has read v[0]
         if (tid == 0) v[0] = make_double2(ph.x * (ax0 + norm), ph.y * (ax0 + norm));
         __syncthreads();
-        // p = beta * B v on this CTA's rows, one warp per row; four
-        // independent accumulator pairs per lane keep the FP64 pipe busy.
+        // p = beta * B v on this CTA's rows, one warp per row. Only the lower
+        // triangle of B is kept: row i supplies B_ik for k <= i, column i
+        // (conj(B_ki), a strided read) the rest. Four independent accumulator
+        // pairs per lane keep the FP64 pipe busy.
         for (int i = part + warp * parts; i < m; i += nw * parts)
         {
             const double2 *row = a + static_cast<std::size_t>(r0 + i) * d + r0;
+            const double2 *col = a + static_cast<std::size_t>(r0) * d + r0 + i;
             double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
+            auto acc = [&](int kk, double &ar, double &ai) {
+                double2 bk;
+                if (kk <= i)
+                    bk = row[kk];
+                else
+                {
+                    const double2 t = col[static_cast<std::size_t>(kk) * d];
+                    bk = make_double2(t.x, -t.y);
+                }
+                const double2 x = v[kk];
+                ar = fma(bk.x, x.x, ar);
+                ar = fma(-bk.y, x.y, ar);
+                ai = fma(bk.x, x.y, ai);
+                ai = fma(bk.y, x.x, ai);
+            };
             int k = lane;
             for (; k + 96 < m; k += 128)
             {
 #pragma unroll
-                for (int u = 0; u < 4; ++u)
-                {
-                    const double2 b = row[k + 32 * u], x = v[k + 32 * u];
-                    sr[u] = fma(b.x, x.x, sr[u]);
-                    sr[u] = fma(-b.y, x.y, sr[u]);
-                    si[u] = fma(b.x, x.y, si[u]);
-                    si[u] = fma(b.y, x.x, si[u]);
-                }
+                for (int u = 0; u < 4; ++u) acc(k + 32 * u, sr[u], si[u]);
             }
-            for (int u = 0; k < m; k += 32, ++u)
-            {
-                const double2 b = row[k], x = v[k];
-                sr[u] = fma(b.x, x.x, sr[u]);
-                sr[u] = fma(-b.y, x.y, sr[u]);
-                si[u] = fma(b.x, x.y, si[u]);
-                si[u] = fma(b.y, x.x, si[u]);
-            }
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+                if (k + 32 * u < m) acc(k + 32 * u, sr[u], si[u]);
             double tr = (sr[0] + sr[1]) + (sr[2] + sr[3]);
             double ti = (si[0] + si[1]) + (si[2] + si[3]);
 #pragma unroll
@@ -207,14 +214,15 @@ __global__ void __launch_bounds__(kTriThreads)
         const double K = 0.5 * beta * block_sum(part_sum, red);
         for (int i = tid; i < m; i += nt) w[i] = make_double2(w[i].x - K * v[i].x, w[i].y - K * v[i].y);
         __syncthreads();
-        // B <- B - v w^H - w v^H on this CTA's rows of the trailing block:
-        // b -= v_i conj(w_k) + w_i conj(v_k), eight FMAs per entry.
+        // B <- B - v w^H - w v^H on this CTA's rows of the trailing block's
+        // lower triangle: b -= v_i conj(w_k) + w_i conj(v_k), eight FMAs per
+        // entry (the diagonal's imaginary parts cancel exactly).
         for (int i = part + warp * parts; i < m; i += nw * parts)
         {
             double2 *row = a + static_cast<std::size_t>(r0 + i) * d + r0;
             const double2 vi = v[i], wi = w[i];
 #pragma unroll 4
-            for (int k = lane; k < m; k += 32)
+            for (int k = lane; k <= i; k += 32)
             {
                 const double2 wk = w[k], vk = v[k];
                 double2 b = row[k];
@@ -281,8 +289,9 @@ __device__ bool tridiag_ql(double *dg, double *of, int d)
                     underflow = true;
                     break;
                 }
-                s = f / r;
-                c = g / r;
+                const double ir = 1.0 / r;
+                s = f * ir;
+                c = g * ir;
                 g = dg[i + 1] - p;
                 r = (dg[i] - g) * s + 2.0 * c * b;
                 p = s * r;
@@ -369,7 +378,11 @@ cudaError_t hermitian_eig_entropy(double *rho, int d, int nb, double *entropy_ou
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
-    k_tridiag_ql<<<(nb + 63) / 64, 64, 0, s>>>(diag, off, d, nb, entropy_out, err);
+    // One thread per matrix, spread over every SM: the QL sweep is a serial
+    // FP64 chain per matrix, so few threads per SM run it fastest.
+    const int sm_count = sms > 0 ? sms : 152;
+    const int tpb = std::max(1, std::min(32, (nb + sm_count - 1) / sm_count));
+    k_tridiag_ql<<<(nb + tpb - 1) / tpb, tpb, 0, s>>>(diag, off, d, nb, entropy_out, err);
     return cudaGetLastError();
 }
 

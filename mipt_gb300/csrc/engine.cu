@@ -137,6 +137,16 @@ __device__ __forceinline__ Cx<Real> collapse_value(Cx<Real> v, std::uint64_t gid
     return Cx<Real>{v.re * scale, v.im * scale};
 }
 
+// collapse_value for the register-round pass: the parity condition is only
+// compiled in for parity-sector states (PAR).
+template <bool PAR, typename Real>
+__device__ __forceinline__ Cx<Real> collapse_value_p(Cx<Real> v, std::uint64_t gidx, const Collapse &cl, Real scale)
+{
+    const bool keep = PAR ? collapse_keeps(gidx, cl) : ((gidx & cl.mask) == cl.value);
+    if (!keep) return Cx<Real>{Real(0), Real(0)};
+    return Cx<Real>{v.re * scale, v.im * scale};
+}
+
 // Loads the tile of geometry g with index tix into shared memory, applying a
 // pending collapse. seg[s] holds the offset of high segment s.
 template <typename Real>
@@ -735,7 +745,7 @@ __device__ std::uint32_t build_item_prefix(std::uint32_t *pref, std::uint32_t *r
 // stores and the histogram, whose values then use their own 2^k floats after
 // the tile buffer. A load wait that runs out sets bit 8 of *err and ends the
 // CTA.
-template <typename Real, int RB, bool TMA>
+template <typename Real, int RB, bool TMA, bool PAR>
 __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
     k_pass_rounds(Cx<Real> *__restrict__ states, PassPlan P, const Cx<Real> *__restrict__ gates,
                   std::size_t gate_stride, const Collapse *__restrict__ col_in, std::size_t col_stride,
@@ -805,7 +815,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
         __syncthreads(); // the previous item's shared-memory reads are complete
         Cx<Real> *psi = states + (static_cast<std::size_t>(b) << g.n);
         const std::uint64_t base = scatter_bits(tix, g.nl, g.n_nl);
-        const int tpar = (__popcll(base) + __popc(static_cast<unsigned>(tid))) & 1;
+        const int tpar = PAR ? ((__popcll(base) + __popc(static_cast<unsigned>(tid))) & 1) : 0;
         if (b != cur_b)
             for (int i = tid; i < P.gates.count * 16; i += blockDim.x)
                 U[i / 16][i % 16] = gates[b * gate_stride + static_cast<std::size_t>(P.gates.gate[i / 16]) * 16 + (i % 16)];
@@ -866,7 +876,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                         gi |= gr[i];
                     }
                 Cx<Real> v = tile[j];
-                if (has_col) v = collapse_value(v, gi, cl, scale);
+                if (has_col) v = collapse_value_p<PAR>(v, gi, cl, scale);
                 amp[r] = v;
             }
         }
@@ -887,7 +897,7 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                 for (int i = 0; i < RB; ++i)
                     if ((r >> i) & 1) gi |= gr[i];
                 Cx<Real> v = psi[gi];
-                if (has_col) v = collapse_value(v, gi, cl, scale);
+                if (has_col) v = collapse_value_p<PAR>(v, gi, cl, scale);
                 amp[r] = v;
             }
         }
@@ -955,26 +965,35 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
                     }
                 }
             }
-            if (R.slot[0] >= 0)
+            if constexpr (PAR)
             {
-                if (P.gates.kind[R.slot[0]])
-                    apply_parity_slot<0>(amp, U[R.slot[0]], tpar);
-                else
-                    apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+                if (R.slot[0] >= 0)
+                {
+                    if (P.gates.kind[R.slot[0]])
+                        apply_parity_slot<0>(amp, U[R.slot[0]], tpar);
+                    else
+                        apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+                }
+                if (RB >= 4 && R.slot[1] >= 0)
+                {
+                    if (P.gates.kind[R.slot[1]])
+                        apply_parity_slot<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], tpar);
+                    else
+                        apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
+                }
+                if (RB >= 6 && R.slot[2] >= 0)
+                {
+                    if (P.gates.kind[R.slot[2]])
+                        apply_parity_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], tpar);
+                    else
+                        apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
+                }
             }
-            if (RB >= 4 && R.slot[1] >= 0)
+            else
             {
-                if (P.gates.kind[R.slot[1]])
-                    apply_parity_slot<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], tpar);
-                else
-                    apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
-            }
-            if (RB >= 6 && R.slot[2] >= 0)
-            {
-                if (P.gates.kind[R.slot[2]])
-                    apply_parity_slot<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], tpar);
-                else
-                    apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
+                if (R.slot[0] >= 0) apply_slot_fast<0>(amp, U[R.slot[0]], packed != 0);
+                if (RB >= 4 && R.slot[1] >= 0) apply_slot_fast<(RB >= 4 ? 1 : 0)>(amp, U[R.slot[1]], packed != 0);
+                if (RB >= 6 && R.slot[2] >= 0) apply_slot_fast<(RB >= 6 ? 2 : 0)>(amp, U[R.slot[2]], packed != 0);
             }
         }
 
@@ -2258,22 +2277,22 @@ int take_withheld_load()
     return c > 0 ? 1 : 0;
 }
 
-// Launches k_pass_rounds<Real, RB, TMA> on its grid.
-template <typename Real, int RB, bool TMA>
+// Launches k_pass_rounds<Real, RB, TMA, PAR> on its grid.
+template <typename Real, int RB, bool TMA, bool PAR>
 cudaError_t launch_rounds(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                           std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                           const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
                           const CUtensorMap &map, const TileTma &tt, int *err, cudaStream_t s,
                           std::uint64_t col_keep, int col_scaled, int sparse)
 {
-    const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, RB, TMA>);
+    const void *fn = reinterpret_cast<const void *>(&k_pass_rounds<Real, RB, TMA, PAR>);
     const std::size_t smem = (sizeof(Cx<Real>) << plan.geom.k) + (TMA ? (sizeof(float) << plan.geom.k) + 128 : 0) +
                              (sparse ? sizeof(std::uint32_t) * (static_cast<std::size_t>(batch) + 1) : 0);
     cudaError_t e = ensure_smem_attr<Real>(fn, smem);
     if (e != cudaSuccess) return e;
     const int threads = 1 << (plan.geom.k - RB);
     const dim3 pgrid = pass_grid(fn, threads, smem, dim3(1u << plan.geom.n_nl, batch));
-    k_pass_rounds<Real, RB, TMA><<<pgrid, threads, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
+    k_pass_rounds<Real, RB, TMA, PAR><<<pgrid, threads, smem, s>>>(states, plan, layer_gates, gate_stride, collapse_in,
                                                                collapse_stride, meas, meas_stride, partials,
                                                                fuse_hist, use_packed_fma() ? 1 : 0, batch, map, tt,
                                                                err, col_keep, col_scaled, sparse,
@@ -2299,7 +2318,8 @@ template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
-                        int *err, cudaStream_t s, std::uint64_t col_keep, int col_scaled, int sparse)
+                        int *err, cudaStream_t s, std::uint64_t col_keep, int col_scaled, int sparse,
+                        int parity_mode)
 {
     dim3 grid(1u << plan.geom.n_nl, batch);
     if ((sparse || col_keep != ~0ull || !col_scaled) && !sparse_pass_supported(plan, sizeof(Real) == 4, batch))
@@ -2333,37 +2353,36 @@ cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const
     }
     if (plan.rounds > 0)
     {
+#define MG_ROUNDS(RBV, TMAV, PARV)                                                                                    \
+    launch_rounds<Real, RBV, TMAV, PARV>(states, batch, plan, layer_gates, gate_stride, collapse_in, collapse_stride, \
+                                         meas, meas_stride, partials, fuse_hist, map, tt, err, s, col_keep,            \
+                                         col_scaled, sparse)
+        CUtensorMap map;
+        TileTma tt{};
+        std::memset(&map, 0, sizeof(map));
+        const bool par = parity_mode != 0;
         if constexpr (sizeof(Real) == 4)
         {
-            CUtensorMap map;
-            TileTma tt{};
             const bool tma = use_persistent_pass() && use_tile_tma() && err != nullptr &&
                              encode_tile_map(map, tt, states, batch, plan.geom);
             if (plan.rb == 6)
-                return tma ? launch_rounds<Real, 6, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
-                                                          collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                          map, tt, err, s, col_keep, col_scaled, sparse)
-                           : launch_rounds<Real, 6, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
-                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                           map, tt, err, s, col_keep, col_scaled, sparse);
+            {
+                if (tma) return par ? MG_ROUNDS(6, true, true) : MG_ROUNDS(6, true, false);
+                return par ? MG_ROUNDS(6, false, true) : MG_ROUNDS(6, false, false);
+            }
             if (plan.rb == 5)
-                return tma ? launch_rounds<Real, 5, true>(states, batch, plan, layer_gates, gate_stride, collapse_in,
-                                                          collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                          map, tt, err, s, col_keep, col_scaled, sparse)
-                           : launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
-                                                           collapse_stride, meas, meas_stride, partials, fuse_hist,
-                                                           map, tt, err, s, col_keep, col_scaled, sparse);
+            {
+                if (tma) return par ? MG_ROUNDS(5, true, true) : MG_ROUNDS(5, true, false);
+                return par ? MG_ROUNDS(5, false, true) : MG_ROUNDS(5, false, false);
+            }
             return cudaErrorInvalidValue;
         }
         else
         {
             if (plan.rb != 5) return cudaErrorInvalidValue;
-            CUtensorMap map;
-            std::memset(&map, 0, sizeof(map));
-            return launch_rounds<Real, 5, false>(states, batch, plan, layer_gates, gate_stride, collapse_in,
-                                                 collapse_stride, meas, meas_stride, partials, fuse_hist, map,
-                                                 TileTma{}, err, s, col_keep, col_scaled, sparse);
+            return par ? MG_ROUNDS(5, false, true) : MG_ROUNDS(5, false, false);
         }
+#undef MG_ROUNDS
     }
     const std::size_t smem = pass_smem<Real>(plan.geom.k);
     cudaError_t e = ensure_smem_attr<Real>(reinterpret_cast<const void *>(&k_pass<Real>), smem);
@@ -2424,7 +2443,7 @@ void set_withheld_tile_loads(int count) { g_withheld_loads.store(count > 0 ? cou
     template cudaError_t launch_init_zero<R>(Cx<R> *, std::uint64_t, int, cudaStream_t);                         \
     template cudaError_t launch_pass<R>(Cx<R> *, int, const PassPlan &, const Cx<R> *, std::size_t,              \
                                         const Collapse *, std::size_t, const LayerMeas *, std::size_t, double *, \
-                                        int, int *, cudaStream_t, std::uint64_t, int, int);                      \
+                                        int, int *, cudaStream_t, std::uint64_t, int, int, int);                 \
     template cudaError_t launch_hist<R>(const Cx<R> *, int, int, int, int, int, const Collapse *, std::size_t,   \
                                         const LayerMeas *, std::size_t, double *, bool, cudaStream_t,            \
                                         const signed char *);                                                    \

@@ -134,13 +134,16 @@ cudaError_t launch_init_zero(Cx<Real> *states, std::uint64_t dim, int batch, cud
 // non-local measured bits (the others are zero before and after the pass and
 // are left untouched in memory); the layer's next pass must then load with
 // col_keep = those non-local qubits and col_scaled = 0. Needs a register-round
-// plan (sparse_pass_supported) and no fused histogram.
+// plan (sparse_pass_supported) and no fused histogram. parity_mode: the states
+// are parity-sector states (collapses may carry a parity condition, the plan
+// may hold parity-selected gates); it selects the kernel variant built for
+// them.
 template <typename Real>
 cudaError_t launch_pass(Cx<Real> *states, int batch, const PassPlan &plan, const Cx<Real> *layer_gates,
                         std::size_t gate_stride, const Collapse *collapse_in, std::size_t collapse_stride,
                         const LayerMeas *meas, std::size_t meas_stride, double *partials, int fuse_hist,
                         int *err, cudaStream_t s, std::uint64_t col_keep = ~0ull, int col_scaled = 1,
-                        int sparse = 0);
+                        int sparse = 0, int parity_mode = 0);
 
 // Test hook: the next `count` TMA-fed pass launches do not issue CTA 0's
 // first tile load; its bounded wait (well under a second) runs out, the CTA
