@@ -284,6 +284,20 @@ struct Workspace
     }
 };
 
+// Spectra up to this many rows go to the one-block Jacobi eigensolver, larger
+// ones to Householder tridiagonalisation + QL (MIPT_GB300_JACOBI_MAX_D, at
+// most 64; default 16: from 32 rows on the reduction needs far fewer FP64
+// operations than Jacobi sweeps).
+int jacobi_max_dim()
+{
+    static const int d = [] {
+        const char *v = std::getenv("MIPT_GB300_JACOBI_MAX_D");
+        const int x = v ? std::atoi(v) : 16;
+        return std::max(1, std::min(64, x));
+    }();
+    return d;
+}
+
 constexpr std::size_t kMaxRhoBytes = std::size_t{1} << 31;
 // Largest buffer of pre-split TF32 operand rows (16 bytes per amplitude).
 constexpr std::size_t kMaxRowsBytes = std::size_t{16} << 30;
@@ -421,7 +435,7 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 1);
                 ++launches;
             }
-            else if (d <= 64)
+            else if (d <= jacobi_max_dim())
             {
                 MG_CUDA(jacobi_entropy(ws.rho.as<double>(), d, nbi, ws.vals.as<double>(), nullptr, s));
                 ++launches;
