@@ -12,6 +12,12 @@ value : device time of K steps with the inputs (gates, measured sites,
         uniforms) already resident in HBM, CUDA events on the launch stream.
 e2e   : the same work through the C ABI's one-call entry point
         (host sampling, pinned host->device upload, device run, results back).
+dS    : the final half-chain S_2 of two trajectories of the batch against the
+        CPU FP64 oracle running the same seeds free on host threads.
+per_layer_observables: the same workload with the half-chain S_2 after
+        every layer (one step, device time).
+plain_fp64: the plain FP64 path, one trajectory per launch sequence,
+        device time and end to end.
 The reference arm times the CPU FP64 oracle on the host cores.
 """
 import argparse

@@ -280,16 +280,22 @@ __device__ bool tridiag_ql(double *dg, double *of, int d)
             for (; i >= l; --i)
             {
                 const double f = s * of[i], b = c * of[i];
-                r = hypot(f, g);
-                of[i + 1] = r;
-                if (r == 0.0)
+                // The entries of a density matrix's tridiagonal form are at
+                // most 1 in modulus, so f^2 + g^2 needs no scaling; one
+                // reciprocal square root gives r, s and c (a shorter
+                // dependent chain than hypot and a division).
+                const double t = fma(f, f, g * g);
+                if (t == 0.0)
                 {
+                    of[i + 1] = 0.0;
                     dg[i + 1] -= p;
                     of[m] = 0.0;
                     underflow = true;
                     break;
                 }
-                const double ir = 1.0 / r;
+                const double ir = rsqrt(t);
+                r = t * ir;
+                of[i + 1] = r;
                 s = f * ir;
                 c = g * ir;
                 g = dg[i + 1] - p;
