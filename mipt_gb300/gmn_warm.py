@@ -162,7 +162,43 @@ class WarmStartModel:
         return m
 
 
+class NearestSolved:
+    """Warm start from the solved training state nearest to each new state (in
+    the 64 real parameters of rho): the ADMM state the cold-start solver
+    reached for it. A non-parametric counterpart of WarmStartModel over the
+    same solver-generated pairs; the solver still certifies every result."""
+
+    def __init__(self, x, t, chunk=4096):
+        self.x = np.ascontiguousarray(x, np.float64)
+        self.t = np.ascontiguousarray(t, np.float32)
+        self.x2 = np.sum(self.x ** 2, axis=1)
+        self.chunk = chunk
+
+    def predict(self, rho):
+        f = features(rho).astype(np.float64)
+        out = np.empty((len(f), self.t.shape[1]), np.float32)
+        for a in range(0, len(f), self.chunk):
+            q = f[a:a + self.chunk]
+            d2 = self.x2[None, :] - 2.0 * (q @ self.x.T)
+            out[a:a + len(q)] = self.t[np.argmin(d2, axis=1)]
+        return from_targets(out)
+
+
 # ------------------------------------------------------------ config-4 data
+def trajectory_states(count, seed, n=16, periods=16):
+    """rho3 blocks of the final states of `count` Haar trajectories (L = n
+    periodic ring, FP32 states, p uniform in [0.05, 0.35]): n blocks each,
+    the trajectory half of the GMN workload."""
+    from . import Batch, trajectory_seed
+    rng = np.random.default_rng(seed)
+    b = Batch(n, periods, capacity=count, fp64=False, rho3=True)
+    seeds = np.array([trajectory_seed(seed, i) for i in range(count)], np.uint64)
+    r = b.run(seeds, rng.uniform(0.05, 0.35, size=count))
+    b.close()
+    x = r["rho3"].reshape(-1, 128)
+    return (x[:, 0::2] + 1j * x[:, 1::2]).reshape(-1, 8, 8)
+
+
 def mixtures(count, seed):
     """Seeded GHZ / W / product states and random two-state mixtures of them,
     with white noise of weight U[0, 1] (the synthetic half of the GMN workload)."""

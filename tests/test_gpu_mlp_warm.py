@@ -53,30 +53,39 @@ def test_gradients_match_cpu_reference(mg, dims):
 
 
 def test_warm_start_on_held_out_states(mg):
-    """Train on solver-generated pairs, warm-start held-out states: every
-    warm-started state is certified with the cold-start GMN value, the
-    certified fraction does not drop, and the iteration change is reported.
-    (Warm starts of this ADMM pay off only with accurate predictions: the
-    exact solution cuts iterations ~30x, 0.3% relative noise ~1.5x, 1% noise
-    already costs iterations; the network's ~5% error gives about 1x. The
-    comparison runs at the penalty the warm start is trained for, sigma = 1:
-    the scaled duals grow as 1/sigma, and so do prediction errors in them.)"""
+    """Train on solver-generated pairs from trajectory rho3 blocks and GHZ/W/
+    product mixtures, then warm-start held-out states of each class.
+
+    Checked for both warm starts (the network's prediction, and the solved
+    training state nearest to each new state): every warm-started state that
+    certifies has the cold-start GMN value (2e-6), and the certified fraction
+    drops by at most 0.02. The iteration gains are reported per class; the
+    nearest solved state must gain at least 1.5x on held-out mixtures (about
+    2x measured). The network's predictions are too coarse for this ADMM (its
+    duals need about 0.3 % accuracy to pay off), so its gain is only
+    reported."""
     from mipt_gb300 import gmn_warm
-    train_rho = gmn_warm.mixtures(24000, 1)
-    test_rho = gmn_warm.mixtures(400, 2)
-    x, t, _ = gmn_warm.solve_pairs(train_rho, gap_tol=1e-6, max_iter=3000, sigma=gmn_warm.WARM_SIGMA)
-    assert len(x) > 0.9 * len(train_rho)
+    sigma = gmn_warm.WARM_SIGMA
+    train = np.concatenate([gmn_warm.trajectory_states(256, 21), gmn_warm.mixtures(20000, 1)])
+    held = {"trajectory": gmn_warm.trajectory_states(24, 22), "mixture": gmn_warm.mixtures(400, 2)}
+    x, t, _ = gmn_warm.solve_pairs(train, gap_tol=1e-6, max_iter=3000, sigma=sigma)
+    assert len(x) > 0.8 * len(train)
     model = gmn_warm.WarmStartModel(seed=0)
     first, last = model.fit(x, t)
     assert last < 0.25 * first, (first, last)
-    kw = dict(gap_tol=1e-6, max_iter=3000, check_every=5, sigma=gmn_warm.WARM_SIGMA)
-    cold = mg.gmn_solve(test_rho, **kw)
-    warm = mg.gmn_solve(test_rho, warm_start=model.predict(test_rho), **kw)
-    c_ok, w_ok = cold["iters"] > 0, warm["iters"] > 0
-    ok = c_ok & w_ok
-    gain = cold["iters"][ok].mean() / warm["iters"][ok].mean()
-    print(f"certified within 3000 iterations: cold {c_ok.mean():.3f}, warm {w_ok.mean():.3f}; iterations "
-          f"{cold['iters'][ok].mean():.1f} -> {warm['iters'][ok].mean():.1f} (x{gain:.2f}, {ok.sum()} states)")
-    assert w_ok.mean() >= c_ok.mean() - 0.02
-    np.testing.assert_allclose(warm["gmn"][ok], cold["gmn"][ok], rtol=0, atol=2e-6)
-    assert gain >= 0.8
+    nearest = gmn_warm.NearestSolved(x, t)
+    kw = dict(gap_tol=1e-6, max_iter=3000, check_every=5, sigma=sigma)
+    gains = {}
+    for cls, rho in held.items():
+        cold = mg.gmn_solve(rho, **kw)
+        for name, guess in (("network", model.predict(rho)), ("nearest", nearest.predict(rho))):
+            warm = mg.gmn_solve(rho, warm_start=guess, **kw)
+            c_ok, w_ok = cold["iters"] > 0, warm["iters"] > 0
+            ok = c_ok & w_ok
+            gain = cold["iters"][ok].mean() / warm["iters"][ok].mean()
+            gains[(cls, name)] = gain
+            print(f"{cls:10s} {name:8s} certified cold {c_ok.mean():.3f} warm {w_ok.mean():.3f}; iterations "
+                  f"{cold['iters'][ok].mean():.1f} -> {warm['iters'][ok].mean():.1f} (x{gain:.2f}, {ok.sum()} states)")
+            assert w_ok.mean() >= c_ok.mean() - 0.02, (cls, name)
+            np.testing.assert_allclose(warm["gmn"][ok], cold["gmn"][ok], rtol=0, atol=2e-6)
+    assert gains[("mixture", "nearest")] >= 1.5, gains
