@@ -1446,19 +1446,27 @@ __global__ void __launch_bounds__(kMeasureThreads)
     const double *part = partials + static_cast<std::size_t>(b) * kHistScratch;
     double *bins = NB <= kSmemBins ? sbins : bins_scratch + static_cast<std::size_t>(b) * bins_stride;
 
-    for (std::uint64_t B = tid; B < NB; B += T)
+    // With fewer bins than threads, G consecutive lanes (a power of two, at
+    // most a warp) share one bin: lane g sums its tiles g, g + G, ... and a
+    // fixed shuffle tree joins the G partial sums, so the order is the same
+    // on every run.
+    const int G = NB >= static_cast<std::uint64_t>(T) ? 1 : static_cast<int>(std::min<std::uint64_t>(32, T / NB));
+    const int groups = T / G;
+    for (std::uint64_t B = tid / G; B < NB; B += groups)
     {
+        const int gl = tid % G;
         std::uint64_t bl = 0, th = 0;
         for (int i = 0; i < m_loc; ++i) bl |= ((B >> lm_bit[i]) & 1ull) << i;
         for (int i = 0; i < m_hi; ++i) th |= ((B >> hm_bit[i]) & 1ull) << hm_pos[i];
         double s = 0.0;
-        for (std::uint64_t r = 0; r < per_bin_tiles; ++r)
+        for (std::uint64_t r = gl; r < per_bin_tiles; r += G)
         {
             std::uint64_t t = r;
             for (int i = 0; i < m_hi; ++i) t = insert_zero(t, hm_pos[i]);
             s += part[((t | th) << m_loc) + bl];
         }
-        bins[B] = s;
+        for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
+        if (gl == 0) bins[B] = s;
     }
     __syncthreads();
 
