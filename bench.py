@@ -37,7 +37,7 @@ METRIC = "trajectory-layers/s at L=24 (batched FP32 vs plain FP64) at |dS|<=1e-5
 UNIT = "trajectory-layers/s"
 N_QUBITS = 24
 PERIODS = 24
-PASS_TRAFFIC_PER_TRAJ = 239.3e6  # DRAM bytes per trajectory per pass launch (ncu)
+PASS_TRAFFIC_PER_TRAJ = 191.0e6  # DRAM bytes per trajectory per pass launch, two layers averaged (ncu)
 GRAM_TENSOR_PIPE_PCT = 66.5  # ncu sm__pipe_tensor_cycles_active of the final S_2 Gram
 P_GRID = np.linspace(0.05, 0.35, 16)
 
@@ -319,13 +319,15 @@ def run_gb300(args):
         passes_per_layer = pass_n / T
         achieved = alg_bytes_step / (pass_ms / 1000.0) / 1e9
         peak, peak_kind = measured_peak_hbm()
-        # DRAM traffic per pass launch: ncu measured 239.3 MB per trajectory
-        # (read 134.5 MB + write 104.8 MB, the rest of the writes still in L2)
-        # on 2 trajectories; each launch streams every state once, so it
-        # scales with the batch (profiles/k_pass_rounds_L24_batch2.md).
+        # DRAM traffic per pass launch: ncu dram bytes of four consecutive
+        # launches (two layers: sparse, dense, sparse, dense) at 16
+        # trajectories, 3.06 GB per launch on average = 191 MB per trajectory;
+        # a launch streams each state it visits once, so it scales with the
+        # batch (profiles/k_pass_rounds_L24_traffic_batch16.md).
         traffic = PASS_TRAFFIC_PER_TRAJ * B
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": traffic, "traffic_source": "ncu dram bytes, 2-trajectory capture scaled to B",
+                    "traffic": traffic,
+                    "traffic_source": "ncu dram bytes per launch, 16-trajectory capture of two layers scaled to B",
                     "peak_source": peak_kind,
                     "kernel": "k_pass (tiled brickwork layer pass)",
                     "alg_bytes_per_launch": alg_bytes_step / pass_n, "launch_ms": pass_ms / pass_n,

@@ -272,7 +272,7 @@ struct EntReq
 
 struct Workspace
 {
-    DevBuf jobs, rho, scratch, vals, idx, eig, err, eig_err, rows;
+    DevBuf jobs, rho, scratch, vals, idx, eig, err, eig_err, rows, dims;
     PinnedArena stage;
     // Host -> device copy of a small table through the pinned staging arena.
     cudaError_t upload(void *dst, const void *src, std::size_t bytes, cudaStream_t s)
@@ -386,7 +386,16 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 MG_CUDA(gram_purity_tc(states, n, ws.jobs.as<GramJob>(), nb, k, col, col_stride, ws.vals.as<double>(),
                                        ws.scratch.p, ws.scratch.bytes, ws.err.as<int>(), s, low_cut ? traj_count : 0,
                                        presplit ? ws.rows.p : nullptr, presplit ? ws.rows.bytes : 0));
-                launches += 2;
+                // Pre-split: the job table, then rows + Gram per group of
+                // jobs that fits the row buffer, then the partial sums.
+                if (presplit)
+                {
+                    const std::size_t group = std::max<std::size_t>(
+                        1, std::min<std::size_t>(nb, ws.rows.bytes / gram_tc_rows_bytes_per_job(n)));
+                    launches += 2 + 2 * static_cast<long long>((nb + group - 1) / group);
+                }
+                else
+                    launches += 2;
                 k_scatter<<<(nb + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nb, d_out, 1);
                 ++launches;
                 continue;
@@ -425,8 +434,12 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
             }
             MG_CUDA(ws.rho.ensure(rho_bytes * nb));
             MG_CUDA(ws.scratch.ensure(gram_scratch_bytes(n, k, nbi, true)));
+            // Rows of each rho that hold data once measured sites are left
+            // out; the large-spectrum eigensolver runs on those only.
+            const bool large = vn && d > jacobi_max_dim();
+            if (large) MG_CUDA(ws.dims.ensure(sizeof(int) * nb));
             MG_CUDA(gram_rho<Real>(states, n, ws.jobs.as<GramJob>(), nbi, k, col, col_stride, ws.rho.as<double>(),
-                                   ws.scratch.p, ws.scratch.bytes, s));
+                                   ws.scratch.p, ws.scratch.bytes, s, large ? ws.dims.as<int>() : nullptr));
             launches += 2;
             if (!vn)
             {
@@ -453,7 +466,7 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                     MG_CUDA(cudaMemsetAsync(ws.eig_err.p, 0, sizeof(int), s));
                 }
                 MG_CUDA(hermitian_eig_entropy(ws.rho.as<double>(), d, nbi, ws.vals.as<double>(), nullptr,
-                                              ws.eig.as<double>(), ws.eig_err.as<int>(), s));
+                                              ws.eig.as<double>(), ws.eig_err.as<int>(), s, ws.dims.as<int>()));
                 launches += 2;
                 k_scatter<<<(nbi + 255) / 256, 256, 0, s>>>(ws.vals.as<double>(), ws.idx.as<int>(), nbi, d_out, 0);
                 ++launches;
@@ -2213,6 +2226,28 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             if (rc) return rc;
         }
     }
+    // Final-state entropies. Full states are observed with the last layer's
+    // collapse still pending (so the measured sites leave the Gram), parity-
+    // sector states after their expansion.
+    auto final_entropies = [&](const Collapse *fc, std::size_t fstride) -> int {
+        std::vector<EntReq> reqs;
+        for (int i = 0; i < count; ++i)
+            for (int r = 0; r < b->reqs_per_point; ++r)
+            {
+                EntReq q = b->reqs[r];
+                q.traj = i;
+                q.out = i * b->reqs_per_point + r;
+                reqs.push_back(q);
+            }
+        Mark m(b, K_OBS, s);
+        return run_entropies<Real>(states, n, reqs, fc, fstride, b->ws, s, b->ent.as<double>(), L);
+    };
+    const bool final_obs = b->reqs_per_point > 0 && !b->per_point();
+    if (final_obs && !enc)
+    {
+        const int rc = T > 0 ? final_entropies(col + (T - 1), T) : final_entropies(nullptr, 0);
+        if (rc) return rc;
+    }
     // Leave every trajectory in its collapsed, normalised final state.
     {
         Mark m(b, K_OTHER, s);
@@ -2225,19 +2260,9 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
             MG_CUDA(launch_collapse<Real>(states, b->dim, count, col + (T - 1), T, s));
     }
     ++L;
-    if (b->reqs_per_point > 0 && !b->per_point())
+    if (final_obs && enc)
     {
-        std::vector<EntReq> reqs;
-        for (int i = 0; i < count; ++i)
-            for (int r = 0; r < b->reqs_per_point; ++r)
-            {
-                EntReq q = b->reqs[r];
-                q.traj = i;
-                q.out = i * b->reqs_per_point + r;
-                reqs.push_back(q);
-            }
-        Mark m(b, K_OBS, s);
-        const int rc = run_entropies<Real>(states, n, reqs, nullptr, 0, b->ws, s, b->ent.as<double>(), L);
+        const int rc = final_entropies(nullptr, 0);
         if (rc) return rc;
     }
     if (b->cfg.rho3)

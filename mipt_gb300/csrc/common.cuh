@@ -8,6 +8,16 @@
 namespace mg
 {
 
+// Nanoseconds of the GPU's global timer: the clock the bounded device waits
+// measure their limits against (mbarrier.try_wait suspends for a
+// hardware-chosen time per poll, so a poll count alone is no time limit).
+__device__ __forceinline__ std::uint64_t device_ns()
+{
+    std::uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Interleaved complex amplitude; float2 / double2 layout in HBM.
 template <typename Real> struct Cx;
 template <> struct __align__(8) Cx<float>

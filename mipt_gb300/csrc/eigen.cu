@@ -81,9 +81,10 @@ __device__ bool parts_barrier(unsigned *ctr, unsigned parts, unsigned &epoch, in
         __threadfence();
         atomicAdd(ctr, 1u);
         const unsigned target = (epoch + 1) * parts;
+        const std::uint64_t t0 = device_ns();
         for (unsigned it = 0; *reinterpret_cast<volatile unsigned *>(ctr) < target; ++it)
         {
-            if (it > (1u << 24))
+            if (it > (1u << 24) || ((it & 15u) == 15u && device_ns() - t0 > 2000000000ull))
             {
                 atomicOr(err, 2);
                 ok = 0;
@@ -107,7 +108,8 @@ __device__ bool parts_barrier(unsigned *ctr, unsigned parts, unsigned &epoch, in
 // barriers per step order the row updates against the next step's reads.
 __global__ void __launch_bounds__(kTriThreads)
     k_tridiag(double2 *__restrict__ mats, int d, double *__restrict__ diag, double *__restrict__ off, int parts,
-              double2 *__restrict__ pglob, unsigned *__restrict__ bars, int *__restrict__ err)
+              double2 *__restrict__ pglob, unsigned *__restrict__ bars, int *__restrict__ err,
+              const int *__restrict__ dims)
 {
     extern __shared__ double2 sh[];
     double2 *v = sh;     // Householder vector (length m)
@@ -123,10 +125,13 @@ __global__ void __launch_bounds__(kTriThreads)
     unsigned epoch = 0;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    // Rows that hold data (the rest of the d x d block is zero: their
+    // eigenvalues are 0). The row stride stays d.
+    const int dm = dims != nullptr ? dims[mat] : d;
 
-    for (int j = 0; j + 1 < d; ++j)
+    for (int j = 0; j + 1 < dm; ++j)
     {
-        const int m = d - 1 - j, r0 = j + 1;
+        const int m = dm - 1 - j, r0 = j + 1;
         __syncthreads(); // the previous step's reads of v[] and w[] are done
         // x = column j below the diagonal (the lower triangle is the valid
         // half of the trailing block).
@@ -241,8 +246,9 @@ __global__ void __launch_bounds__(kTriThreads)
     }
     if (tid == 0 && part == 0)
     {
-        dg[d - 1] = a[static_cast<std::size_t>(d - 1) * d + d - 1].x;
-        of[d - 1] = 0.0;
+        dg[dm - 1] = a[static_cast<std::size_t>(dm - 1) * d + dm - 1].x;
+        of[dm - 1] = 0.0;
+        for (int i = dm; i < d; ++i) dg[i] = of[i] = 0.0;
     }
 }
 
@@ -314,20 +320,21 @@ __device__ bool tridiag_ql(double *dg, double *of, int d)
 }
 
 __global__ void k_tridiag_ql(double *__restrict__ diag, double *__restrict__ off, int d, int nb,
-                             double *__restrict__ entropy, int *__restrict__ err)
+                             double *__restrict__ entropy, int *__restrict__ err, const int *__restrict__ dims)
 {
     const int jb = blockIdx.x * blockDim.x + threadIdx.x;
     if (jb >= nb) return;
     double *dg = diag + static_cast<std::size_t>(jb) * d;
     double *of = off + static_cast<std::size_t>(jb) * d;
-    if (!tridiag_ql(dg, of, d))
+    const int dm = dims != nullptr ? dims[jb] : d;
+    if (!tridiag_ql(dg, of, dm))
     {
         atomicOr(err, 1);
         entropy[jb] = NAN;
         return;
     }
     double s = 0.0;
-    for (int i = 0; i < d; ++i)
+    for (int i = 0; i < dm; ++i)
     {
         const double l = dg[i];
         if (l > 1e-15) s -= l * log2(l);
@@ -344,7 +351,7 @@ std::size_t hermitian_eig_scratch_doubles(int d, int nb)
 }
 
 cudaError_t hermitian_eig_entropy(double *rho, int d, int nb, double *entropy_out, double *eig_out, double *scratch,
-                                  int *err, cudaStream_t s)
+                                  int *err, cudaStream_t s, const int *dims)
 {
     if (nb <= 0) return cudaSuccess;
     if (d < 2 || d > 4096) return cudaErrorInvalidValue;
@@ -373,14 +380,14 @@ cudaError_t hermitian_eig_entropy(double *rho, int d, int nb, double *entropy_ou
         e = cudaMemsetAsync(bars, 0, sizeof(unsigned) * nb, s);
         if (e != cudaSuccess) return e;
         int dd = d;
-        void *args[] = {&rho, &dd, &diag, &off, &parts, &pglob, &bars, &err};
+        void *args[] = {&rho, &dd, &diag, &off, &parts, &pglob, &bars, &err, &dims};
         e = cudaLaunchCooperativeKernel(reinterpret_cast<const void *>(&k_tridiag), dim3(nb * parts),
                                         dim3(kTriThreads), args, smem, s);
     }
     else
     {
         k_tridiag<<<nb, kTriThreads, smem, s>>>(reinterpret_cast<double2 *>(rho), d, diag, off, 1, nullptr, nullptr,
-                                                err);
+                                                err, dims);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return e;
@@ -388,7 +395,7 @@ cudaError_t hermitian_eig_entropy(double *rho, int d, int nb, double *entropy_ou
     // FP64 chain per matrix, so few threads per SM run it fastest.
     const int sm_count = sms > 0 ? sms : 152;
     const int tpb = std::max(1, std::min(32, (nb + sm_count - 1) / sm_count));
-    k_tridiag_ql<<<(nb + tpb - 1) / tpb, tpb, 0, s>>>(diag, off, d, nb, entropy_out, err);
+    k_tridiag_ql<<<(nb + tpb - 1) / tpb, tpb, 0, s>>>(diag, off, d, nb, entropy_out, err, dims);
     return cudaGetLastError();
 }
 

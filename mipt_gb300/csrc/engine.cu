@@ -137,14 +137,65 @@ __device__ __forceinline__ Cx<Real> collapse_value(Cx<Real> v, std::uint64_t gid
     return Cx<Real>{v.re * scale, v.im * scale};
 }
 
-// collapse_value for the register-round pass: the parity condition is only
-// compiled in for parity-sector states (PAR).
-template <bool PAR, typename Real>
-__device__ __forceinline__ Cx<Real> collapse_value_p(Cx<Real> v, std::uint64_t gidx, const Collapse &cl, Real scale)
+// Bits r of a register index whose bit i is set (r < 64).
+__host__ __device__ constexpr std::uint64_t reg_bit_pattern(int i)
 {
-    const bool keep = PAR ? collapse_keeps(gidx, cl) : ((gidx & cl.mask) == cl.value);
-    if (!keep) return Cx<Real>{Real(0), Real(0)};
-    return Cx<Real>{v.re * scale, v.im * scale};
+    return i == 0 ? 0xAAAAAAAAAAAAAAAAull
+         : i == 1 ? 0xCCCCCCCCCCCCCCCCull
+         : i == 2 ? 0xF0F0F0F0F0F0F0F0ull
+         : i == 3 ? 0xFF00FF00FF00FF00ull
+         : i == 4 ? 0xFFFF0000FFFF0000ull
+                  : 0xFFFFFFFF00000000ull;
+}
+
+// Which of a thread's 2^RB register elements a pending collapse keeps, as a
+// bit mask over the register index r. Element r has the global index gt | (the
+// gr[i] of r's set bits), the gr[i] being single bits outside gt. The mask /
+// value test splits into the thread's part (all or nothing) and one pattern
+// per register bit in the mask; the parity condition of parity-sector states
+// (PAR) is the XOR of the patterns of the register bits it covers.
+template <int RB, bool PAR>
+__device__ __forceinline__ std::uint64_t collapse_keep_bits(std::uint64_t gt, const std::uint64_t (&gr)[RB],
+                                                            const Collapse &cl)
+{
+    constexpr std::uint64_t full = RB == 6 ? ~0ull : ((1ull << (1 << RB)) - 1ull);
+    std::uint64_t rpos = 0;
+#pragma unroll
+    for (int i = 0; i < RB; ++i) rpos |= gr[i];
+    const std::uint64_t mt = cl.mask & ~rpos;
+    if ((gt & mt) != (cl.value & mt)) return 0;
+    std::uint64_t keep = full;
+#pragma unroll
+    for (int i = 0; i < RB; ++i)
+        if (gr[i] & cl.mask) keep &= (gr[i] & cl.value) ? reg_bit_pattern(i) : ~reg_bit_pattern(i);
+    if constexpr (PAR)
+    {
+        if (cl.parity != 0)
+        {
+            const std::uint64_t pm = cl.parity & ~kParityBit;
+            std::uint64_t odd = 0;
+#pragma unroll
+            for (int i = 0; i < RB; ++i)
+                if (gr[i] & pm) odd ^= reg_bit_pattern(i);
+            const bool want_odd = ((cl.parity >> 63) ^ static_cast<std::uint64_t>(__popcll(gt & pm) & 1)) != 0;
+            keep &= want_odd ? odd : ~odd;
+        }
+    }
+    return keep & full;
+}
+
+// Applies a keep mask and the collapse's renormalisation to the registers.
+template <typename Real, int NA>
+__device__ __forceinline__ void apply_keep_bits(Cx<Real> (&a)[NA], std::uint64_t keep, Real scale)
+{
+    constexpr std::uint64_t full = NA == 64 ? ~0ull : ((1ull << NA) - 1ull);
+    if (keep == full && scale == Real(1)) return;
+#pragma unroll
+    for (int r = 0; r < NA; ++r)
+    {
+        const bool k = (keep >> r) & 1ull;
+        a[r] = k ? Cx<Real>{a[r].re * scale, a[r].im * scale} : Cx<Real>{Real(0), Real(0)};
+    }
 }
 
 // Loads the tile of geometry g with index tix into shared memory, applying a
@@ -409,12 +460,23 @@ __device__ void register_histogram(const Cx<float> (&amp)[1 << RB], const Round 
             }
         }
         float s = 0.f;
-        for (int c = sub * per; c < (sub + 1) * per && c < (1 << uc); ++c)
+        // This lane's terms c0 .. c0 + cnt - 1 (cnt is 0 or `per`, a power of
+        // two). The offsets of the unmeasured bits are distinct powers of
+        // two, so the terms are visited in Gray-code order of their low bits:
+        // each step flips one bit of the offset.
+        const int c0 = sub * per;
+        const int cnt = (1 << uc) - c0 < per ? (1 << uc) - c0 : per;
+        if (cnt > 0)
         {
             int o = off;
             for (int t = 0; t < uc; ++t)
-                if ((c >> t) & 1) o += tab[16 + t];
-            s += S[o];
+                if ((c0 >> t) & 1) o += tab[16 + t];
+            for (int i = 0;;)
+            {
+                s += S[o];
+                if (++i >= cnt) break;
+                o ^= tab[16 + __ffs(i) - 1];
+            }
         }
         for (int d = G >> 1; d > 0; d >>= 1) s += __shfl_down_sync(lanes, s, d, G);
         if (sub == 0) out[w] = static_cast<double>(s);
@@ -571,12 +633,15 @@ __device__ __forceinline__ bool tile_bar_try(std::uint64_t *bar, std::uint32_t p
     return ok != 0;
 }
 
-// Bounded wait for a tile load (about 0.3 s at most).
+// Bounded wait for a tile load: gives up after 0.3 s (or 2^22 polls).
 __device__ __forceinline__ bool tile_bar_wait(std::uint64_t *bar, std::uint32_t parity)
 {
+    if (tile_bar_try(bar, parity)) return true;
+    const std::uint64_t t0 = device_ns();
     for (int i = 0; i < (1 << 22); ++i)
     {
         if (tile_bar_try(bar, parity)) return true;
+        if ((i & 15) == 15 && device_ns() - t0 > 300000000ull) return false;
         if (i >= 32) __nanosleep(64);
     }
     return false;
@@ -867,18 +932,12 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
             for (int r = 0; r < NA; ++r)
             {
                 std::uint32_t j = jt;
-                std::uint64_t gi = gt;
 #pragma unroll
                 for (int i = 0; i < RB; ++i)
-                    if ((r >> i) & 1)
-                    {
-                        j |= jr[i];
-                        gi |= gr[i];
-                    }
-                Cx<Real> v = tile[j];
-                if (has_col) v = collapse_value_p<PAR>(v, gi, cl, scale);
-                amp[r] = v;
+                    if ((r >> i) & 1) j |= jr[i];
+                amp[r] = tile[j];
             }
+            if (has_col) apply_keep_bits(amp, collapse_keep_bits<RB, PAR>(gt, gr, cl), scale);
         }
         else
         {
@@ -896,10 +955,9 @@ __global__ void __launch_bounds__(RB == 5 && sizeof(Real) == 4 ? 512 : 256)
 #pragma unroll
                 for (int i = 0; i < RB; ++i)
                     if ((r >> i) & 1) gi |= gr[i];
-                Cx<Real> v = psi[gi];
-                if (has_col) v = collapse_value_p<PAR>(v, gi, cl, scale);
-                amp[r] = v;
+                amp[r] = psi[gi];
             }
+            if (has_col) apply_keep_bits(amp, collapse_keep_bits<RB, PAR>(gt, gr, cl), scale);
         }
         __syncthreads(); // gate matrices visible; round-0 reads of the tile buffer are done
         if constexpr (TMA)

@@ -59,6 +59,17 @@ GramJob make_gram_job(int traj, int n, const int *kept, int k, bool fermion)
 
 namespace
 {
+// MIPT_GB300_MEASURED_COMPACT=0 keeps the sites a pending collapse measures
+// in the Gram (see CompactJob and k_gram).
+bool measured_compact_enabled()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_MEASURED_COMPACT");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 constexpr int TM = kGramTile;
 constexpr int TK = 32;
 constexpr int kGramThreads = 256;
@@ -80,14 +91,16 @@ __device__ __forceinline__ void tile_coords(int id, int &tr, int &tc)
     tc = id - r * (r + 1) / 2;
 }
 
+// check: apply the collapse's mask test; scale: its renormalisation (also
+// for reduced jobs, whose addresses all pass the test).
 template <typename Real>
 __device__ __forceinline__ Cx<Real> gather(const Cx<Real> *__restrict__ psi, std::uint64_t addr, const Collapse &cl,
-                                           bool has_col, bool negate)
+                                           bool check, bool scale, bool negate)
 {
     Cx<Real> v = psi[addr];
-    if (has_col)
+    if (check && (addr & cl.mask) != cl.value) return Cx<Real>{Real(0), Real(0)};
+    if (scale)
     {
-        if ((addr & cl.mask) != cl.value) return Cx<Real>{Real(0), Real(0)};
         const Real sc = static_cast<Real>(cl.scale);
         v.re *= sc;
         v.im *= sc;
@@ -115,7 +128,7 @@ template <typename Real, typename Acc, bool kMixed = false>
 __global__ void __launch_bounds__(kGramThreads)
     k_gram(const Cx<Real> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
            const Collapse *__restrict__ col, std::size_t col_stride, int splits, std::uint64_t kchunk, int mode,
-           Acc *__restrict__ part_out, double *__restrict__ pur_out)
+           Acc *__restrict__ part_out, double *__restrict__ pur_out, int compact, int *__restrict__ dims_out)
 {
     constexpr int TK = GramK<Real>::TK;
     constexpr int KB = GramK<Real>::BITS;
@@ -124,17 +137,52 @@ __global__ void __launch_bounds__(kGramThreads)
     __shared__ Cx<Real> Bs[TK][TM + 1];
     __shared__ std::uint64_t roffA[TM], roffB[TM], crossA[TM], crossB[TM], elo[TK];
     __shared__ double red[kGramThreads / 32];
+    __shared__ std::uint64_t s_fixed;
+    __shared__ int s_reduced, s_nenv;
 
     const int tid = threadIdx.x;
     const int job = blockIdx.z;
-    if (tid == 0) J = jobs[job];
+    const bool has_col = col != nullptr;
+    if (tid == 0)
+    {
+        J = jobs[job];
+        // Reduced job (compact): the sites the pending collapse measured
+        // leave the kept and environment lists and their outcome bits join
+        // every address. The state is |outcome> (x) phi on them, so rho is
+        // phi's reduced matrix on the kept modes left, padded with zero
+        // rows and columns (the same spectrum and purity); fermionic jobs
+        // keep every mode.
+        s_fixed = 0;
+        s_reduced = 0;
+        s_nenv = n - J.k;
+        if (compact && has_col && !J.fermion)
+        {
+            const Collapse c0 = col[J.traj * col_stride];
+            if (c0.parity == 0 && c0.mask != 0)
+            {
+                const int kf = J.k;
+                int a = 0, e = 0;
+                for (int i = 0; i < kf; ++i)
+                    if (!((c0.mask >> J.kept[i]) & 1ull)) J.kept[a++] = J.kept[i];
+                for (int i = 0; i < n - kf; ++i)
+                    if (!((c0.mask >> J.env[i]) & 1ull)) J.env[e++] = J.env[i];
+                J.k = a;
+                J.rows_fastest = (a > 0 && J.kept[0] == 0) ? 1 : 0;
+                s_nenv = e;
+                s_fixed = c0.value & c0.mask;
+                s_reduced = 1;
+            }
+        }
+        if (dims_out != nullptr && blockIdx.x == 0 && blockIdx.y == 0) dims_out[job] = 1 << J.k;
+    }
     __syncthreads();
+    const int D = 1 << jobs[job].k; // rows of the output matrix
     const int k = J.k;
-    const int d = 1 << k;
+    const int d = 1 << k; // rows with data
     int tr, tc;
     tile_coords(blockIdx.x, tr, tc);
     const int r0 = tr * TM, c0 = tc * TM;
-    const int nenv = n - k;
+    const int nenv = s_nenv;
     const std::uint64_t E = 1ull << nenv;
     const std::uint64_t ebeg = static_cast<std::uint64_t>(blockIdx.y) * kchunk;
     const std::uint64_t eend = ebeg + kchunk < E ? ebeg + kchunk : E;
@@ -172,8 +220,9 @@ __global__ void __launch_bounds__(kGramThreads)
         elo[i] = o;
     }
     Collapse cl{0, 0, 1.0, 0};
-    const bool has_col = col != nullptr;
     if (has_col) cl = col[J.traj * col_stride];
+    const bool check = has_col && !s_reduced;
+    const std::uint64_t fixed = s_fixed;
     __syncthreads();
 
     const Cx<Real> *psi = states + (static_cast<std::size_t>(J.traj) << n);
@@ -198,7 +247,7 @@ __global__ void __launch_bounds__(kGramThreads)
 
     for (std::uint64_t e0 = ebeg; e0 < eend; e0 += TK)
     {
-        std::uint64_t ehi = 0;
+        std::uint64_t ehi = fixed;
         for (int b = KB; b < nenv; ++b)
             if ((e0 >> b) & 1ull) ehi |= 1ull << J.env[b];
         for (int idx = tid; idx < TM * TK; idx += kGramThreads)
@@ -220,9 +269,9 @@ __global__ void __launch_bounds__(kGramThreads)
             {
                 const std::uint64_t eo = ehi | elo[kk];
                 if (r0 + i < d)
-                    va = gather(psi, eo | roffA[i], cl, has_col, (__popcll(e & crossA[i]) & 1) != 0);
+                    va = gather(psi, eo | roffA[i], cl, check, has_col, (__popcll(e & crossA[i]) & 1) != 0);
                 if (c0 + i < d)
-                    vb = gather(psi, eo | roffB[i], cl, has_col, (__popcll(e & crossB[i]) & 1) != 0);
+                    vb = gather(psi, eo | roffB[i], cl, check, has_col, (__popcll(e & crossB[i]) & 1) != 0);
             }
             As[kk][i] = va;
             Bs[kk][i] = vb;
@@ -282,17 +331,18 @@ __global__ void __launch_bounds__(kGramThreads)
 
     if (mode == 0)
     {
-        Acc *out = part_out + (static_cast<std::size_t>(job) * splits + blockIdx.y) * static_cast<std::size_t>(d) * d * 2;
+        // Rows and columns past d (a reduced job) are zero and written as such.
+        Acc *out = part_out + (static_cast<std::size_t>(job) * splits + blockIdx.y) * static_cast<std::size_t>(D) * D * 2;
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j)
             {
                 const int r = r0 + ty * 4 + i, c = c0 + tx * 4 + j;
-                if (r < d && c < d && r >= c)
+                if (r < D && c < D && r >= c)
                 {
-                    out[(static_cast<std::size_t>(r) * d + c) * 2] = accr[i][j];
-                    out[(static_cast<std::size_t>(r) * d + c) * 2 + 1] = acci[i][j];
+                    out[(static_cast<std::size_t>(r) * D + c) * 2] = accr[i][j];
+                    out[(static_cast<std::size_t>(r) * D + c) * 2 + 1] = acci[i][j];
                 }
             }
     }
@@ -729,7 +779,7 @@ std::size_t gram_scratch_bytes(int n, int k, int njobs, bool rho)
 template <typename Real>
 cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int njobs, int k,
                      const Collapse *collapse, std::size_t collapse_stride, double *rho_out, void *scratch,
-                     std::size_t scratch_bytes, cudaStream_t s)
+                     std::size_t scratch_bytes, cudaStream_t s, int *dims_out)
 {
     if (njobs <= 0) return cudaSuccess;
     const int splits = gram_splits(n, k, njobs, true);
@@ -738,12 +788,15 @@ cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int n
     const std::uint64_t E = 1ull << (n - k);
     const std::uint64_t kchunk = (E + splits - 1) / splits;
     dim3 grid(gram_tiles(k), splits, njobs);
+    const int compact = measured_compact_enabled() ? 1 : 0;
     if (sizeof(Real) == 4 && n >= 20)
         k_gram<Real, double, sizeof(Real) == 4><<<grid, kGramThreads, 0, s>>>(
-            states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0, static_cast<double *>(scratch), nullptr);
+            states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0, static_cast<double *>(scratch), nullptr,
+            compact, dims_out);
     else
         k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits,
-                                                           kchunk, 0, static_cast<double *>(scratch), nullptr);
+                                                           kchunk, 0, static_cast<double *>(scratch), nullptr,
+                                                           compact, dims_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int d = 1 << k;
@@ -764,7 +817,8 @@ cudaError_t gram_purity(const Cx<Real> *states, int n, const GramJob *d_jobs, in
     const std::uint64_t E = 1ull << (n - k);
     dim3 grid(tiles, 1, njobs);
     k_gram<Real, Real><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, 1, E, 1, nullptr,
-                                                     static_cast<double *>(scratch));
+                                                     static_cast<double *>(scratch),
+                                                     measured_compact_enabled() ? 1 : 0, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
@@ -783,10 +837,10 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
     // gram_rho; below that every product is summed in FP64.
     if (n >= 20)
         k_gram<float, double, true><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
-                                                                  static_cast<double *>(scratch));
+                                                                  static_cast<double *>(scratch), 0, nullptr);
     else
         k_gram<float, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
-                                                            static_cast<double *>(scratch));
+                                                            static_cast<double *>(scratch), 0, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_sum_rows<<<njobs, 256, 0, s>>>(static_cast<const double *>(scratch), tiles, purity_out);
@@ -900,15 +954,21 @@ __device__ __forceinline__ bool mbar_try(std::uint64_t *bar, std::uint32_t parit
     return ok != 0;
 }
 
-// Bounded wait: gives up after TC_SPIN polls, raises the error flag and the
-// block-wide abort flag (so every later wait returns at once).
+// Limit of one bounded mbarrier wait of the tensor-core Gram.
+constexpr std::uint64_t TC_WAIT_NS = 2000000000ull;
+
+// Bounded wait: gives up after 2 s (or TC_SPIN polls), raises the error flag
+// and the block-wide abort flag (so every later wait returns at once).
 __device__ __forceinline__ bool mbar_wait(std::uint64_t *bar, std::uint32_t parity, volatile int *abort_flag,
                                           int *err)
 {
+    if (mbar_try(bar, parity)) return true;
+    const std::uint64_t t0 = device_ns();
     for (long long i = 0; i < TC_SPIN; ++i)
     {
         if (*abort_flag) return false;
         if (mbar_try(bar, parity)) return true;
+        if ((i & 15) == 15 && device_ns() - t0 > TC_WAIT_NS) break;
     }
     *abort_flag = 1;
     atomicOr(err, 4);
@@ -919,8 +979,12 @@ __device__ __forceinline__ bool mbar_wait(std::uint64_t *bar, std::uint32_t pari
 // block's own bulk copies land before it exits.
 __device__ __forceinline__ void mbar_settle(std::uint64_t *bar, std::uint32_t parity)
 {
+    const std::uint64_t t0 = device_ns();
     for (long long i = 0; i < TC_SPIN; ++i)
+    {
         if (mbar_try(bar, parity)) return;
+        if ((i & 15) == 15 && device_ns() - t0 > TC_WAIT_NS) return;
+    }
 }
 
 // 3xTF32 split with integer ops: hi = x rounded to the nearest TF32 value
@@ -1391,11 +1455,64 @@ static_assert(TP_BUFS * TP_N <= 512 && TP_DCOLS % 32 == 0, "tensor memory or dra
 constexpr std::uint32_t kTpIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((TP_C >> 3) << 17) | ((TCM >> 4) << 24);
 constexpr std::uint32_t kTpIdescNegA = kTpIdesc | (1u << 13);
 
-// One thread per operand row: 16 amplitudes of job j's state (pending
-// collapse applied), split into TF32 hi/lo.
+// Geometry of one pre-split Gram job after the sites its trajectory's
+// pending collapse measures are taken out. After a projective measurement the
+// state is a product |outcome> (x) phi on the measured sites, so rho of the
+// kept modes has the spectrum of phi's reduced matrix on the kept modes left:
+// M keeps only the rows and columns whose measured bits equal the outcome
+// (every other entry is zero), so Tr(rho^2) = ||M' M'^H||_F^2 with M' the
+// 2^kq x 2^eq block of them. Fermionic jobs are not reduced (their sign
+// factors depend on every mode).
+struct CompactJob
+{
+    std::uint64_t fixed; // the measured sites' outcome bits
+    std::uint64_t mask, value; // collapse test still to apply (unreduced jobs)
+    float scale;
+    int kq, eq; // kept and environment modes left
+    std::int8_t kpos[16]; // their global positions, ascending
+    std::int8_t epos[32];
+};
+
+// One thread per job: the reduced geometry of each pre-split Gram job.
+__global__ void k_compact_jobs(const GramJob *__restrict__ jobs, int njobs, int n, int k,
+                               const Collapse *__restrict__ col, std::size_t col_stride, int compact,
+                               CompactJob *__restrict__ out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= njobs) return;
+    const GramJob &J = jobs[j];
+    Collapse cl{0, 0, 1.0, 0};
+    if (col != nullptr) cl = col[J.traj * col_stride];
+    CompactJob c{};
+    c.scale = static_cast<float>(cl.scale);
+    const bool reduce = compact && !J.fermion && cl.parity == 0;
+    std::uint64_t drop = reduce ? cl.mask : 0ull;
+    c.fixed = reduce ? (cl.value & cl.mask) : 0ull;
+    c.mask = reduce ? 0ull : cl.mask;
+    c.value = reduce ? 0ull : cl.value;
+    int kq = 0, eq = 0;
+    for (int i = 0; i < k; ++i)
+        if (!((drop >> J.kept[i]) & 1ull)) c.kpos[kq++] = J.kept[i];
+    for (int i = 0; i < n - k; ++i)
+        if (!((drop >> J.env[i]) & 1ull)) c.epos[eq++] = J.env[i];
+    c.kq = kq;
+    c.eq = eq;
+    out[j] = c;
+}
+
+// Operand rows and chunks of a reduced job the Gram reads: rows below
+// max(2^kq, 128) (one whole 128-row block), chunks of 16 environment
+// columns below max(2^eq / 16, 1).
+__host__ __device__ __forceinline__ std::uint32_t compact_rows(int kq) { return kq >= 7 ? (1u << kq) : 128u; }
+__host__ __device__ __forceinline__ int compact_chunks(int eq) { return eq >= 4 ? (1 << (eq - 4)) : 1; }
+
+// One thread per operand row: 16 environment columns of job j's reduced
+// matrix (pending collapse applied; columns past 2^eq and rows past 2^kq are
+// zero), split into TF32 hi/lo. Rows and chunks the Gram does not read are
+// skipped.
 __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, const GramJob *__restrict__ jobs,
-                            int njobs, const Collapse *__restrict__ col, std::size_t col_stride,
-                            float4 *__restrict__ rows, std::uint64_t lo_rows)
+                            const CompactJob *__restrict__ cjobs, int njobs, float4 *__restrict__ rows,
+                            std::uint64_t lo_rows)
 {
     const std::uint64_t d = 1ull << k;
     const int cbits = n - k - 4;
@@ -1406,20 +1523,36 @@ __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, 
         const std::uint64_t a = idx & (d - 1);
         const std::uint64_t c = (idx >> k) & ((1ull << cbits) - 1);
         const int j = static_cast<int>(idx >> (k + cbits));
-        const int t = jobs[j].traj;
-        const Cx<float> *psi = states + (static_cast<std::size_t>(t) << n);
-        Collapse cl{0, 0, 1.0, 0};
-        if (col != nullptr) cl = col[t * col_stride];
-        const float scale = static_cast<float>(cl.scale);
+        const CompactJob &C = cjobs[j];
+        if (a >= compact_rows(C.kq) || c >= static_cast<std::uint64_t>(compact_chunks(C.eq))) continue;
         float re[16], im[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
+        if (a >= (1ull << C.kq))
         {
-            const std::uint64_t gi = a | (((c << 4) + i) << k);
-            const Cx<float> v = psi[gi];
-            const bool keep = col == nullptr || (gi & cl.mask) == cl.value;
-            re[i] = keep ? v.re * scale : 0.f;
-            im[i] = keep ? v.im * scale : 0.f;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) re[i] = im[i] = 0.f;
+        }
+        else
+        {
+            const Cx<float> *psi = states + (static_cast<std::size_t>(jobs[j].traj) << n);
+            std::uint64_t base = C.fixed;
+            for (int b = 0; b < C.kq; ++b)
+                if ((a >> b) & 1ull) base |= 1ull << C.kpos[b];
+            for (int b = 4; b < C.eq; ++b)
+                if ((c >> (b - 4)) & 1ull) base |= 1ull << C.epos[b];
+            std::uint64_t low[4] = {0, 0, 0, 0};
+            for (int b = 0; b < 4 && b < C.eq; ++b) low[b] = 1ull << C.epos[b];
+            const int ncols = C.eq >= 4 ? 16 : (1 << C.eq);
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+            {
+                const std::uint64_t gi = base | ((i & 1) ? low[0] : 0ull) | ((i & 2) ? low[1] : 0ull) |
+                                         ((i & 4) ? low[2] : 0ull) | ((i & 8) ? low[3] : 0ull);
+                Cx<float> v{0.f, 0.f};
+                if (i < ncols) v = psi[gi];
+                const bool keep = i < ncols && (gi & C.mask) == C.value;
+                re[i] = keep ? v.re * C.scale : 0.f;
+                im[i] = keep ? v.im * C.scale : 0.f;
+            }
         }
         float4 *hi = rows + idx * 8, *lo = rows + (idx + lo_rows) * 8;
 #pragma unroll
@@ -1456,7 +1589,7 @@ __device__ __forceinline__ void tp_mma(std::uint32_t d, std::uint64_t a, std::ui
 // weighted squares as k_gram_tc does. Every wait is bounded (bit 4 of *err).
 __global__ void __launch_bounds__(TP_THREADS, 1)
     k_gram_tc_pre(int n, int k, int job0, double *__restrict__ pur_out, int *__restrict__ err, std::uint32_t lo_rows,
-                  const __grid_constant__ CUtensorMap tmap)
+                  const __grid_constant__ CUtensorMap tmap, const CompactJob *__restrict__ cjobs)
 {
     extern __shared__ __align__(1024) unsigned char tp_raw[];
     __shared__ __align__(8) std::uint64_t full_bar[TP_STAGES], empty_bar[TP_STAGES], seg_bar[TP_BUFS],
@@ -1471,6 +1604,13 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
     const int job = blockIdx.z;
     int tr, tc;
     tile_coords(blockIdx.x, tr, tc);
+    // A block past the job's reduced rows holds zeros only.
+    const CompactJob &C = cjobs[job];
+    if (static_cast<std::uint32_t>(tr * TCM) >= compact_rows(C.kq))
+    {
+        if (tid == 0) pur_out[static_cast<std::size_t>(job0 + job) * gridDim.x + blockIdx.x] = 0.0;
+        return;
+    }
     if (tid == 0)
     {
         for (int st = 0; st < TP_STAGES; ++st)
@@ -1498,7 +1638,8 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const std::uint32_t tmem = tmem_base;
     const int r0 = tr * TCM, c0 = tc * TCM;
-    const int nchunks = 1 << (n - k - 4);
+    const int row_chunks = 1 << (n - k - 4); // chunks per job in the row buffer
+    const int nchunks = compact_chunks(C.eq); // chunks streamed
     const int nseg = (nchunks + TC_SEG - 1) / TC_SEG;
 
     if (warp < TC_PWARPS)
@@ -1611,7 +1752,7 @@ __global__ void __launch_bounds__(TP_THREADS, 1)
             asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TP_STAGE)
                          : "memory");
             const std::uint32_t base = sm_addr(smem + st * TP_STAGE);
-            const int yb = static_cast<int>((static_cast<std::uint32_t>(job) * nchunks + chunk) << k);
+            const int yb = static_cast<int>((static_cast<std::uint32_t>(job) * row_chunks + chunk) << k);
             const int lo = static_cast<int>(lo_rows);
             const std::uint32_t Bb = base + 2 * TP_A_BYTES;
             const std::uint32_t dst[8] = {base, base + 8192, base + TP_A_BYTES, base + TP_A_BYTES + 8192,
@@ -1669,7 +1810,9 @@ int gram_tc_tiles(int k) { return 2 * gram_tc_blocks(k); }
 
 std::size_t gram_tc_scratch_bytes(int k, int njobs)
 {
-    return sizeof(double) * static_cast<std::size_t>(gram_tc_tiles(k)) * njobs;
+    // Purity partials, then the reduced job table of the pre-split path.
+    return sizeof(double) * static_cast<std::size_t>(gram_tc_tiles(k)) * njobs +
+           sizeof(CompactJob) * static_cast<std::size_t>(njobs);
 }
 
 namespace
@@ -1731,6 +1874,13 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
         cudaError_t e = cudaFuncSetAttribute(k_gram_tc_pre, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(TP_SMEM));
         if (e != cudaSuccess) return e;
+        CompactJob *cjobs = reinterpret_cast<CompactJob *>(static_cast<char *>(scratch) +
+                                                           sizeof(double) * static_cast<std::size_t>(gram_tc_tiles(k)) *
+                                                               njobs);
+        k_compact_jobs<<<(njobs + 127) / 128, 128, 0, s>>>(d_jobs, njobs, n, k, collapse, collapse_stride,
+                                                           measured_compact_enabled() ? 1 : 0, cjobs);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
         for (int g0 = 0; g0 < njobs; g0 += group)
         {
             const int g = std::min(group, njobs - g0);
@@ -1749,13 +1899,13 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
                 return cudaErrorInvalidValue;
             const std::uint64_t nrows = lo_rows;
             const int blocks = static_cast<int>(std::min<std::uint64_t>((nrows + 255) / 256, 152ull * 8));
-            k_tf32_rows<<<blocks, 256, 0, s>>>(states, n, k, d_jobs + g0, g, collapse, collapse_stride,
+            k_tf32_rows<<<blocks, 256, 0, s>>>(states, n, k, d_jobs + g0, cjobs + g0, g,
                                                static_cast<float4 *>(rows), lo_rows);
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
             dim3 grid(gram_tc_blocks(k), 1, g);
             k_gram_tc_pre<<<grid, TP_THREADS, TP_SMEM, s>>>(n, k, g0, static_cast<double *>(scratch), err,
-                                                            static_cast<std::uint32_t>(lo_rows), map);
+                                                            static_cast<std::uint32_t>(lo_rows), map, cjobs + g0);
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
@@ -1793,7 +1943,7 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
 
 #define MG_INST(R)                                                                                               \
     template cudaError_t gram_rho<R>(const Cx<R> *, int, const GramJob *, int, int, const Collapse *, std::size_t, \
-                                     double *, void *, std::size_t, cudaStream_t);                               \
+                                     double *, void *, std::size_t, cudaStream_t, int *);                        \
     template cudaError_t gram_purity<R>(const Cx<R> *, int, const GramJob *, int, int, const Collapse *,          \
                                         std::size_t, double *, void *, std::size_t, cudaStream_t);               \
     template cudaError_t rho3_sweep<R>(const Cx<R> *, int, int, const int *, int, int, const Collapse *,          \

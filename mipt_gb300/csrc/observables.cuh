@@ -39,11 +39,15 @@ inline int gram_tiles(int k)
 }
 
 // rho for every job (all jobs share k): full FP64 d x d Hermitian matrices
-// written to rho_out[job][d][d] (row-major complex).
+// written to rho_out[job][d][d] (row-major complex). With a pending collapse,
+// non-fermionic jobs leave out the sites it measured (the state is a product
+// on them, so the spectrum and purity are those of the reduced matrix): rho
+// then holds that 2^k' x 2^k' matrix in its leading rows and columns, zeros
+// elsewhere, and dims_out[job] (nullable) receives 2^k'.
 template <typename Real>
 cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int njobs, int k,
                      const Collapse *collapse, std::size_t collapse_stride, double *rho_out, void *scratch,
-                     std::size_t scratch_bytes, cudaStream_t s);
+                     std::size_t scratch_bytes, cudaStream_t s, int *dims_out = nullptr);
 
 // Purity Tr(rho^2) of every job without materialising rho.
 template <typename Real>
@@ -96,9 +100,11 @@ cudaError_t jacobi_entropy(const double *rho, int d, int njobs, double *entropy_
 // scratch holds hermitian_eig_scratch_doubles(d, njobs) doubles. A QL
 // iteration limit that runs out sets bit 1 of *err and writes NaN; a timed-out
 // barrier between the CTAs of one matrix sets bit 2.
+// dims (nullable): the rows of each matrix that hold data (the rest of
+// its d x d block is zero); the reduction and QL then run on those only.
 std::size_t hermitian_eig_scratch_doubles(int d, int njobs);
 cudaError_t hermitian_eig_entropy(double *rho, int d, int njobs, double *entropy_out, double *eig_out,
-                                  double *scratch, int *err, cudaStream_t s);
+                                  double *scratch, int *err, cudaStream_t s, const int *dims = nullptr);
 
 // Three-site RDMs of every trajectory, for `count` triples subs[3*i..].
 // out[traj][i][8][8] complex row-major. fermion selects the fermionic trace
