@@ -118,12 +118,12 @@ __device__ __forceinline__ Cx<Real> gather(const Cx<Real> *__restrict__ psi, std
 // Acc is the type of the totals: FP64 whenever rho is materialised (its
 // small eigenvalues feed -lambda log lambda, so accumulation rounding must
 // stay below the state's own second-order error), the operand type for the
-// purity-only mode. With kMixed (FP32 states, FP64 totals) the products are
-// summed in FP32 runs of 64 before each run joins the FP64 totals: FP32 FMA
-// throughput instead of GB300's FP64 rate. A run's rounding is about
-// 2^-24 * 64 * |amplitude|^2 ~ 2^(6 - 24 - n), which keeps the spurious
-// eigenvalues of rho, and their -lambda log lambda, negligible for n >= 20;
-// smaller states keep exact FP64 sums of the (exact) FP32 products.
+// purity-only mode. With kMixed (FP32 states, FP64 totals; purity only) the
+// products are summed in FP32 runs of 64 before each run joins the FP64
+// totals: FP32 FMA throughput instead of GB300's FP64 rate. A run's relative
+// rounding (about 5e-7) moves the purity by as little, but it is too coarse
+// for rho's small eigenvalues, so materialised rho always sums exactly in
+// FP64.
 template <typename Real, typename Acc, bool kMixed = false>
 __global__ void __launch_bounds__(kGramThreads)
     k_gram(const Cx<Real> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
@@ -789,14 +789,13 @@ cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int n
     const std::uint64_t kchunk = (E + splits - 1) / splits;
     dim3 grid(gram_tiles(k), splits, njobs);
     const int compact = measured_compact_enabled() ? 1 : 0;
-    if (sizeof(Real) == 4 && n >= 20)
-        k_gram<Real, double, sizeof(Real) == 4><<<grid, kGramThreads, 0, s>>>(
-            states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0, static_cast<double *>(scratch), nullptr,
-            compact, dims_out);
-    else
-        k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits,
-                                                           kchunk, 0, static_cast<double *>(scratch), nullptr,
-                                                           compact, dims_out);
+    // Exact FP64 sums of the (exact) products: rho feeds -lambda log lambda,
+    // and FP32 runs of 64 products left about 5e-7 relative error in its
+    // entries, which moved the S_vN of near-pure reduced states by up to
+    // 2e-5 at n = 20 (the measured-site reduction keeps the FP64 work small).
+    k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits, kchunk,
+                                                       0, static_cast<double *>(scratch), nullptr, compact,
+                                                       dims_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int d = 1 << k;
@@ -833,8 +832,8 @@ cudaError_t gram_purity_f64acc(const Cx<float> *states, int n, const GramJob *d_
     if (sizeof(double) * static_cast<std::size_t>(tiles) * njobs > scratch_bytes) return cudaErrorInvalidValue;
     const std::uint64_t E = 1ull << (n - k);
     dim3 grid(tiles, 1, njobs);
-    // From n = 20 the products run in FP32 runs of 64 into FP64 totals, as in
-    // gram_rho; below that every product is summed in FP64.
+    // From n = 20 the products run in FP32 runs of 64 into FP64 totals (the
+    // purity needs no more); below that every product is summed in FP64.
     if (n >= 20)
         k_gram<float, double, true><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, nullptr, 0, 1, E, 1, nullptr,
                                                                   static_cast<double *>(scratch), 0, nullptr);

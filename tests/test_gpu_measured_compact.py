@@ -45,13 +45,12 @@ def test_per_layer_s2_of_measured_states(mg, n, p):
 
 
 @pytest.mark.parametrize("fp64", [True, False])
-@pytest.mark.parametrize("n,p", [(16, 0.35), (18, 0.2)])
-def test_per_layer_svn_and_tmi_of_measured_states(mg, fp64, n, p):
-    """Half-chain S_vN (256- and 512-row spectra: the Householder eigensolver
+@pytest.mark.parametrize("n,p,periods,count", [(16, 0.35, 2, 3), (20, 0.2, 1, 2)])
+def test_per_layer_svn_and_tmi_of_measured_states(mg, fp64, n, p, periods, count):
+    """Half-chain S_vN (256- and 1024-row spectra: the Householder eigensolver
     on the reduced rows only) and the von Neumann TMI after every layer,
     against the oracle: FP64 1e-10, FP32 1e-5."""
     from oracle import pyoracle as orc
-    periods, count = 2, 3
     flags = mg.OBS_SVN_HALF | mg.OBS_TMI_VN
     seeds = [mg.trajectory_seed(37, 100 * n + i) for i in range(count)]
     b = mg.Batch(n, periods, capacity=count, fp64=fp64, observables=flags, observe_every=1)
