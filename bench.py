@@ -18,6 +18,10 @@ per_layer_observables: the same workload with the half-chain S_2 after
         every layer (one step, device time).
 plain_fp64: the plain FP64 path, one trajectory per launch sequence,
         device time and end to end.
+gram  : the final S_2 Gram's time and algorithmic flops. The entropies are
+        taken with the last layer's collapse pending, so each trajectory's
+        Gram covers only the rows and columns outside its measured sites
+        (the state is a product on them); the flops count that block.
 The reference arm times the CPU FP64 oracle on the host cores.
 """
 import argparse
@@ -333,15 +337,23 @@ def run_gb300(args):
                     "alg_bytes_per_launch": alg_bytes_step / pass_n, "launch_ms": pass_ms / pass_n,
                     "passes_per_layer": passes_per_layer,
                     "kernel_ms_per_step": {k: v[0] for k, v in stats.items()}}
-        # Final half-chain S_2: tensor-core Gram, 4 d_A^2 d_B real flops per
-        # trajectory for the Hermitian half (d_A = d_B = 2^12).
+        # Final half-chain S_2: tensor-core Gram of each trajectory's block
+        # without the sites its last layer measured (the state is a product
+        # on them): d_A' = 2^(12 - measured sites among 0..11), d_B' likewise
+        # for 12..23, 4 d_A'^2 d_B' real flops for the Hermitian half.
         obs_ms = stats["observables"][0]
-        gram_flops = B * 4.0 * float(1 << (N_QUBITS // 2)) ** 3
+        half = N_QUBITS // 2
+        last = np.asarray(out["measured"])[:, -1].astype(np.uint64)
+        lo_meas = np.array([bin(int(m) & ((1 << half) - 1)).count("1") for m in last])
+        hi_meas = np.array([bin(int(m) >> half).count("1") for m in last])
+        gram_flops = float(np.sum(4.0 * 2.0 ** (2 * (half - lo_meas)) * 2.0 ** (half - hi_meas)))
+        full_flops = B * 4.0 * float(1 << half) ** 3
         gram = {"kernel": "k_tf32_rows + k_gram_tc_pre (tcgen05 3xTF32, TMA-fed)", "ms_per_step": obs_ms,
                 "alg_tflops": gram_flops / (obs_ms / 1000.0) / 1e12 if obs_ms > 0 else None,
-                "tensor_pipe_active_pct": GRAM_TENSOR_PIPE_PCT,
-                "tensor_pipe_source": "ncu sm__pipe_tensor_cycles_active, 2-trajectory capture of the same kernel "
-                                      "(profiles/k_gram_tc_L24_halfcut_batch2.md)"}
+                "alg_flops_per_step": gram_flops, "unreduced_flops_per_step": full_flops,
+                "tensor_pipe_active_pct_unreduced": GRAM_TENSOR_PIPE_PCT,
+                "tensor_pipe_source": "ncu sm__pipe_tensor_cycles_active, 2-trajectory capture of the unreduced "
+                                      "half-chain Gram (profiles/k_gram_tc_L24_halfcut_batch2.md)"}
 
         # Plain FP64 per-trajectory path on the same GPU, one trajectory:
         # device time (CUDA events around the execute, as for `value`) and

@@ -186,6 +186,19 @@ __global__ void k_jw_closure(Cx<Real> *states, int n, int count)
     }
 }
 
+// Collapse records with the outcome test of `col` and no renormalisation or
+// parity condition: for states the collapse has already been applied to
+// (expanded parity-sector states), so that the entropies can still leave
+// the measured stored sites out of the Gram.
+__global__ void k_mask_records(const Collapse *__restrict__ col, std::size_t col_stride, int count,
+                               Collapse *__restrict__ out)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= count) return;
+    const Collapse c = col[b * col_stride];
+    out[b] = Collapse{c.mask, c.value, 1.0, 0};
+}
+
 // Parity-sector states: trajectory b keeps the 2^ne amplitudes of its stored
 // qubits 0..ne-1 at cs[b * 2^ne ..]; qubit ne (the chain's top qubit) is
 // sector[b] xor the parity of the stored bits. Expansion writes the full
@@ -940,6 +953,7 @@ struct mipt_gb300_batch
     bool can_encode = false, enc = false;
     std::vector<int> enc_sector; // the sectors the gates were uploaded for
     DevBuf cstates, d_sector;
+    DevBuf mask_col; // outcome-only collapse records of expanded states (count)
     int ncolour = 2;
     bool lattice = false;
     std::vector<int> region_slots; // request index of each added region
@@ -2104,14 +2118,28 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     }
     // Observations of point `point` on the current states (`pending`: the
     // collapse each trajectory still owes, or null).
+    // Expanded parity-sector states carry their collapse already; their
+    // entropies get outcome-only records (stride 1) instead.
+    auto mask_records = [&](const Collapse *pending) -> const Collapse * {
+        k_mask_records<<<(count + 127) / 128, 128, 0, s>>>(pending, T, count, b->mask_col.as<Collapse>());
+        ++L;
+        return b->mask_col.as<Collapse>();
+    };
+    if (enc) MG_CUDA(b->mask_col.ensure(sizeof(Collapse) * static_cast<std::size_t>(b->capacity)));
     auto observe = [&](int point, const Collapse *pending) -> int {
+        std::size_t pstride = T;
         if (enc)
         {
             Mark m(b, K_OTHER, s);
             k_expand<Real><<<xgrid, 256, 0, s>>>(xs, states, ne, count, sec, pending, T);
             MG_CUDA(cudaGetLastError());
             ++L;
-            pending = nullptr;
+            if (pending != nullptr)
+            {
+                pending = mask_records(pending);
+                MG_CUDA(cudaGetLastError());
+                pstride = 1;
+            }
         }
         if (b->reqs_per_point > 0)
         {
@@ -2125,14 +2153,14 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
                     reqs.push_back(q);
                 }
             Mark m(b, K_OBS, s);
-            const int rc = run_entropies<Real>(states, n, reqs, pending, T, b->ws, s, b->ent.as<double>(), L);
+            const int rc = run_entropies<Real>(states, n, reqs, pending, pstride, b->ws, s, b->ent.as<double>(), L);
             if (rc) return rc;
         }
         if (b->cfg.rho3)
         {
             Mark m(b, K_OBS, s);
             MG_CUDA(rho3_sweep<Real>(states, n, count, b->subs.as<int>(), b->rho3_count,
-                                     b->cfg.fermion_trace ? 1 : 0, pending, T,
+                                     b->cfg.fermion_trace ? 1 : 0, pending, pstride,
                                      b->rho3_pts.as<double>() +
                                          static_cast<std::size_t>(point) * b->capacity * b->rho3_count * 128,
                                      b->r3scratch.p, b->r3scratch.bytes, s));
@@ -2262,7 +2290,9 @@ int batch_execute(mipt_gb300_batch *b, cudaStream_t s)
     ++L;
     if (final_obs && enc)
     {
-        const int rc = final_entropies(nullptr, 0);
+        const Collapse *mc = mask_records(col + (T - 1));
+        MG_CUDA(cudaGetLastError());
+        const int rc = final_entropies(mc, 1);
         if (rc) return rc;
     }
     if (b->cfg.rho3)

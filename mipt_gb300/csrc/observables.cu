@@ -184,8 +184,36 @@ __global__ void __launch_bounds__(kGramThreads)
     const int r0 = tr * TM, c0 = tc * TM;
     const int nenv = s_nenv;
     const std::uint64_t E = 1ull << nenv;
-    const std::uint64_t ebeg = static_cast<std::uint64_t>(blockIdx.y) * kchunk;
-    const std::uint64_t eend = ebeg + kchunk < E ? ebeg + kchunk : E;
+    // A reduced job spreads its (smaller) environment evenly over the same
+    // splits, in multiples of TK columns.
+    std::uint64_t kc = kchunk;
+    if (s_reduced)
+    {
+        kc = (E + splits - 1) / splits;
+        kc = (kc + TK - 1) / TK * TK;
+    }
+    const std::uint64_t ebeg = static_cast<std::uint64_t>(blockIdx.y) * kc;
+    const std::uint64_t eend = ebeg + kc < E ? ebeg + kc : E;
+    if (r0 >= d)
+    {
+        // Rows past the reduced block: this tile of rho is zero.
+        if (mode == 0)
+        {
+            Acc *out = part_out + (static_cast<std::size_t>(job) * splits + blockIdx.y) * static_cast<std::size_t>(D) * D * 2;
+            for (int i = tid; i < TM * TM; i += kGramThreads)
+            {
+                const int r = r0 + i / TM, c = c0 + i % TM;
+                if (r < D && c < D && r >= c)
+                {
+                    out[(static_cast<std::size_t>(r) * D + c) * 2] = Acc(0);
+                    out[(static_cast<std::size_t>(r) * D + c) * 2 + 1] = Acc(0);
+                }
+            }
+        }
+        else if (tid == 0)
+            pur_out[static_cast<std::size_t>(job) * gridDim.x + blockIdx.x] = 0.0;
+        return;
+    }
 
     if (tid < TM)
     {
