@@ -387,7 +387,10 @@ int run_entropies(const Cx<Real> *states, int n, const std::vector<EntReq> &reqs
                 MG_CUDA(ws.upload(ws.idx.p, idx.data(), sizeof(int) * nb, s));
                 // Low cuts: TF32 operand rows split once per observation, in
                 // job groups of at most kMaxRowsBytes.
-                bool presplit = low_cut && k <= gram_tc_presplit_max_k() && gram_tc_presplit_enabled();
+                // Pre-split operand rows for any kept set (the row split
+                // gathers, with fermionic signs); the state's own tensor map
+                // only serves the gathered fallback of low cuts.
+                bool presplit = k <= gram_tc_presplit_max_k() && gram_tc_presplit_enabled();
                 if (presplit)
                 {
                     const std::size_t per_job = gram_tc_rows_bytes_per_job(n);

@@ -1534,9 +1534,9 @@ __host__ __device__ __forceinline__ std::uint32_t compact_rows(int kq) { return 
 __host__ __device__ __forceinline__ int compact_chunks(int eq) { return eq >= 4 ? (1 << (eq - 4)) : 1; }
 
 // One thread per operand row: 16 environment columns of job j's reduced
-// matrix (pending collapse applied; columns past 2^eq and rows past 2^kq are
-// zero), split into TF32 hi/lo. Rows and chunks the Gram does not read are
-// skipped.
+// matrix (pending collapse applied; fermionic signs for fermionic jobs;
+// columns past 2^eq and rows past 2^kq are zero), split into TF32 hi/lo.
+// Rows and chunks the Gram does not read are skipped.
 __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, const GramJob *__restrict__ jobs,
                             const CompactJob *__restrict__ cjobs, int njobs, float4 *__restrict__ rows,
                             std::uint64_t lo_rows)
@@ -1560,10 +1560,16 @@ __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, 
         }
         else
         {
-            const Cx<float> *psi = states + (static_cast<std::size_t>(jobs[j].traj) << n);
-            std::uint64_t base = C.fixed;
+            const GramJob &J = jobs[j];
+            const Cx<float> *psi = states + (static_cast<std::size_t>(J.traj) << n);
+            std::uint64_t base = C.fixed, cross = 0;
             for (int b = 0; b < C.kq; ++b)
-                if ((a >> b) & 1ull) base |= 1ull << C.kpos[b];
+                if ((a >> b) & 1ull)
+                {
+                    base |= 1ull << C.kpos[b];
+                    cross ^= J.below[b]; // fermionic jobs are never reduced: kpos = kept
+                }
+            if (!J.fermion) cross = 0;
             for (int b = 4; b < C.eq; ++b)
                 if ((c >> (b - 4)) & 1ull) base |= 1ull << C.epos[b];
             std::uint64_t low[4] = {0, 0, 0, 0};
@@ -1577,8 +1583,11 @@ __global__ void k_tf32_rows(const Cx<float> *__restrict__ states, int n, int k, 
                 Cx<float> v{0.f, 0.f};
                 if (i < ncols) v = psi[gi];
                 const bool keep = i < ncols && (gi & C.mask) == C.value;
-                re[i] = keep ? v.re * C.scale : 0.f;
-                im[i] = keep ? v.im * C.scale : 0.f;
+                // Fermionic sign: one flip per occupied environment mode
+                // below each occupied kept mode (environment index 16c + i).
+                const float sg = (__popcll(((c << 4) | static_cast<std::uint64_t>(i)) & cross) & 1) ? -C.scale : C.scale;
+                re[i] = keep ? v.re * sg : 0.f;
+                im[i] = keep ? v.im * sg : 0.f;
             }
         }
         float4 *hi = rows + idx * 8, *lo = rows + (idx + lo_rows) * 8;
@@ -1892,8 +1901,7 @@ cudaError_t gram_purity_tc(const Cx<float> *states, int n, const GramJob *d_jobs
     // Measured against the gathered path: L = 24 half cut (k = 12) 85 -> 39 ms
     // for 32 states, L = 28 lattice half (k = 14) 1.8x faster per layer; k = 15
     // and 16 stay on the gathered path (not measured).
-    if (tma_traj_count > 0 && k <= gram_tc_presplit_max_k() && rows != nullptr && rows_bytes >= per_job &&
-        tensor_map_encoder() != nullptr &&
+    if (k <= gram_tc_presplit_max_k() && rows != nullptr && rows_bytes >= per_job && tensor_map_encoder() != nullptr &&
         (reinterpret_cast<std::uintptr_t>(rows) & 15u) == 0)
     {
         // Pre-split operand rows, jobs in groups that fit `rows`.

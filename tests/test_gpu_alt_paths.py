@@ -5,7 +5,9 @@ results as the defaults: per-thread tile loads instead of TMA tensor loads
 operands (MIPT_GB300_TC_PRESPLIT=0), a live tile autotune instead of the
 measured table (MIPT_GB300_AUTOTUNE=1). The switches are read once per process,
 so each variant runs in a child process on the same seeds. Tolerances: state
-amplitudes and entropies 1e-6 (the FP32 path's rounding)."""
+amplitudes 1e-6 (the FP32 path's rounding); entropies 1e-5, the FP32 entropy
+bound (the gathered Gram keeps the measured sites' zero rows and columns that
+the pre-split path leaves out, so its FP32 sums run in another order)."""
 import json
 import os
 import subprocess
@@ -58,7 +60,7 @@ def test_switch_gives_the_same_trajectories(default_run, env):
     assert alt["outcomes"] == default_run["outcomes"]
     np.testing.assert_allclose(alt["psi_re"], default_run["psi_re"], rtol=0, atol=1e-6)
     np.testing.assert_allclose(alt["psi_im"], default_run["psi_im"], rtol=0, atol=1e-6)
-    np.testing.assert_allclose(alt["obs"], default_run["obs"], rtol=0, atol=1e-6)
+    np.testing.assert_allclose(alt["obs"], default_run["obs"], rtol=0, atol=1e-5)
     np.testing.assert_allclose(alt["s2"], default_run["s2"], rtol=0, atol=1e-6)
 
 

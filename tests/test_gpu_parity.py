@@ -256,8 +256,10 @@ def test_full_size_chain_L24(mg, orc):
                                          (17, [1, 0, 2, 3, 4, 5, 6, 7], False)])
 def test_tensor_core_renyi2(mg, orc, n, kept, ferm):
     """FP32 Renyi-2 through the tcgen05 3xTF32 Gram (cuts with >= 128 rows)
-    against the FP64 oracle's RDM purity. Cuts keeping modes 0..k-1 in order
-    take the TMA operand path, the others the gathered one."""
+    against the FP64 oracle's RDM purity. Every kept set up to 14 modes
+    (contiguous, gathered, reversed, fermionic) goes through the pre-split
+    operand rows, whose row split gathers the kept modes and applies the
+    fermionic signs."""
     psi = random_state(n, 77 + n)
     e = device_state(mg, psi, False)
     got = mg.renyi2(e.data, n, kept, ferm, False)
@@ -267,8 +269,8 @@ def test_tensor_core_renyi2(mg, orc, n, kept, ferm):
 
 
 def test_fp32_region_svn_large_state(mg):
-    """S_vN of 8-qubit regions of L=20 FP32 states, whose rho Gram sums FP32
-    runs of 64 products into FP64 totals, against the FP64 path on the same
+    """S_vN of 8-qubit regions of L=20 FP32 states (rho summed exactly in
+    FP64, measured sites left out) against the FP64 path on the same
     measurement outcomes (|dS| within the FP32 path's 1e-5)."""
     n, periods, p = 20, 3, 0.25
     seeds = [mg.trajectory_seed(20, i) for i in range(2)]
