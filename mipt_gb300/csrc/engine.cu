@@ -1510,6 +1510,22 @@ __global__ void __launch_bounds__(kMeasureThreads)
     // on every run.
     const int G = NB >= static_cast<std::uint64_t>(T) ? 1 : static_cast<int>(std::min<std::uint64_t>(32, T / NB));
     const int groups = T / G;
+    // The bin's tiles: tile index t = tile-index bits of r deposited into the
+    // unmeasured positions (`free`); stepping r by G adds G's deposit there,
+    // carried across the measured positions by setting them first.
+    std::uint64_t free_bits = (g.n_nl >= 64 ? ~0ull : ((1ull << g.n_nl) - 1ull));
+    for (int i = 0; i < m_hi; ++i) free_bits &= ~(1ull << hm_pos[i]);
+    auto deposit = [&](std::uint64_t x) {
+        std::uint64_t out = 0, f = free_bits;
+        for (int i = 0; f != 0ull; ++i)
+        {
+            const std::uint64_t low = f & (~f + 1ull);
+            if ((x >> i) & 1ull) out |= low;
+            f &= f - 1ull;
+        }
+        return out;
+    };
+    const std::uint64_t t_step = deposit(static_cast<std::uint64_t>(G));
     for (std::uint64_t B = tid / G; B < NB; B += groups)
     {
         const int gl = tid % G;
@@ -1517,11 +1533,11 @@ __global__ void __launch_bounds__(kMeasureThreads)
         for (int i = 0; i < m_loc; ++i) bl |= ((B >> lm_bit[i]) & 1ull) << i;
         for (int i = 0; i < m_hi; ++i) th |= ((B >> hm_bit[i]) & 1ull) << hm_pos[i];
         double s = 0.0;
+        std::uint64_t t = deposit(static_cast<std::uint64_t>(gl));
         for (std::uint64_t r = gl; r < per_bin_tiles; r += G)
         {
-            std::uint64_t t = r;
-            for (int i = 0; i < m_hi; ++i) t = insert_zero(t, hm_pos[i]);
             s += part[((t | th) << m_loc) + bl];
+            t = ((t | ~free_bits) + t_step) & free_bits;
         }
         for (int o = G / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, G);
         if (gl == 0) bins[B] = s;
@@ -1539,12 +1555,28 @@ __global__ void __launch_bounds__(kMeasureThreads)
         seg_sum[tid] = s;
     }
     __syncthreads();
-    if (tid == 0)
+    // Total and CDF search by warp 0: lane l sums segments [l Q, (l+1) Q) in
+    // order, a shuffle scan gives each lane's cumulative range, and the first
+    // lane whose range passes the draw walks its segments, then the bins of
+    // the segment it lands in.
+    if (tid < 32)
     {
-        double total = 0.0;
-        for (std::uint64_t i = 0; i < P; ++i) total += seg_sum[i];
+        const int lane = tid;
+        const std::uint64_t Q = (P + 31) / 32;
+        const std::uint64_t s0 = lane * Q < P ? lane * Q : P, s1 = (lane + 1) * Q < P ? (lane + 1) * Q : P;
+        double partial = 0.0;
+        for (std::uint64_t i = s0; i < s1; ++i) partial += seg_sum[i];
+        double incl = partial;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const double y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        double excl = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) excl = 0.0;
+        const double total = __shfl_sync(0xffffffffu, incl, 31);
         std::uint64_t chosen = NB - 1;
-        bool bad = !(total > 0.0) || !isfinite(total);
+        const bool bad = !(total > 0.0) || !isfinite(total);
         if (forced != nullptr)
         {
             const std::uint64_t f = forced[b * forced_stride];
@@ -1557,46 +1589,58 @@ __global__ void __launch_bounds__(kMeasureThreads)
         else if (!bad)
         {
             const double draw = M.uniform[ci] * total;
-            double run = 0.0;
-            std::uint64_t segi = P;
-            for (std::uint64_t i = 0; i < P; ++i)
+            const unsigned past = __ballot_sync(0xffffffffu, s0 < s1 && draw < incl);
+            if (past != 0u)
             {
-                if (draw < run + seg_sum[i])
+                const int leader = __ffs(past) - 1;
+                std::uint64_t pick = NB - 1;
+                if (lane == leader)
                 {
-                    segi = i;
-                    break;
-                }
-                run += seg_sum[i];
-            }
-            if (segi < P)
-            {
-                const std::uint64_t lo = segi * S, hi = (segi + 1) * S < NB ? (segi + 1) * S : NB;
-                for (std::uint64_t i = lo; i < hi; ++i)
-                {
-                    run += bins[i];
-                    if (draw < run)
+                    double run = excl;
+                    std::uint64_t segi = s1 - 1;
+                    for (std::uint64_t i = s0; i < s1; ++i)
                     {
-                        chosen = i;
-                        break;
+                        if (draw < run + seg_sum[i])
+                        {
+                            segi = i;
+                            break;
+                        }
+                        run += seg_sum[i];
+                    }
+                    const std::uint64_t lo = segi * S, hi = (segi + 1) * S < NB ? (segi + 1) * S : NB;
+                    pick = hi - 1;
+                    for (std::uint64_t i = lo; i < hi; ++i)
+                    {
+                        run += bins[i];
+                        if (draw < run)
+                        {
+                            pick = i;
+                            break;
+                        }
                     }
                 }
+                chosen = __shfl_sync(0xffffffffu, pick, leader);
             }
         }
-        double branch = bins[chosen];
-        if (!bad && !(branch > 0.0) && forced == nullptr)
+        if (lane == 0)
         {
-            // Numerically starved bin: take the heaviest (first on ties).
-            std::uint64_t best = 0;
-            for (std::uint64_t i = 1; i < NB; ++i)
-                if (bins[i] > bins[best]) best = i;
-            chosen = best;
-            branch = bins[best];
+            double branch = bins[chosen];
+            bool fail = bad;
+            if (!bad && !(branch > 0.0) && forced == nullptr)
+            {
+                // Numerically starved bin: take the heaviest (first on ties).
+                std::uint64_t best = 0;
+                for (std::uint64_t i = 1; i < NB; ++i)
+                    if (bins[i] > bins[best]) best = i;
+                chosen = best;
+                branch = bins[best];
+            }
+            if (!(branch > 0.0)) fail = true;
+            s_chosen = chosen;
+            s_branch = branch;
+            s_total = total;
+            if (fail) atomicOr(err, 1);
         }
-        if (!(branch > 0.0)) bad = true;
-        s_chosen = chosen;
-        s_branch = branch;
-        s_total = total;
-        if (bad) atomicOr(err, 1);
     }
     __syncthreads();
     if (tid == 0)
