@@ -70,6 +70,17 @@ bool measured_compact_enabled()
     return on;
 }
 
+// MIPT_GB300_RHO_SUMS=fp64 sums the rho of FP32 states exactly in FP64
+// instead of in compensated FP32 runs.
+bool compensated_rho_sums()
+{
+    static const bool on = [] {
+        const char *v = std::getenv("MIPT_GB300_RHO_SUMS");
+        return !(v && std::strcmp(v, "fp64") == 0);
+    }();
+    return on;
+}
+
 constexpr int TM = kGramTile;
 constexpr int TK = 32;
 constexpr int kGramThreads = 256;
@@ -118,13 +129,30 @@ __device__ __forceinline__ Cx<Real> gather(const Cx<Real> *__restrict__ psi, std
 // Acc is the type of the totals: FP64 whenever rho is materialised (its
 // small eigenvalues feed -lambda log lambda, so accumulation rounding must
 // stay below the state's own second-order error), the operand type for the
-// purity-only mode. With kMixed (FP32 states, FP64 totals; purity only) the
-// products are summed in FP32 runs of 64 before each run joins the FP64
-// totals: FP32 FMA throughput instead of GB300's FP64 rate. A run's relative
-// rounding (about 5e-7) moves the purity by as little, but it is too coarse
-// for rho's small eigenvalues, so materialised rho always sums exactly in
-// FP64.
-template <typename Real, typename Acc, bool kMixed = false>
+// purity-only mode. With kMixed (FP32 states, FP64 totals) the products are
+// summed in FP32 runs before each run joins the FP64 totals: FP32
+// throughput instead of GB300's FP64 rate. Plain runs of 64 (the
+// allocation-free purity) have a relative rounding of about 5e-7, which
+// moves a purity by as little but is too coarse for rho's small
+// eigenvalues; materialised rho of FP32 states uses compensated runs
+// (kComp), of FP64 states exact FP64 sums.
+// One step of a compensated dot product (Ogita, Rump and Oishi, "Accurate sum
+// and dot product", 2005, Dot2): s += x * y in FP32, with the exact rounding
+// errors of the product (TwoProduct by FMA) and of the sum (Knuth's TwoSum)
+// added to c. The _rn intrinsics keep the product and the additions from being
+// contracted into FMAs, which the error-free transformations rely on.
+__device__ __forceinline__ void comp_fma(float x, float y, float &s, float &c)
+{
+    const float p = __fmul_rn(x, y);
+    const float ep = fmaf(x, y, -p);
+    const float t = __fadd_rn(s, p);
+    const float z = __fsub_rn(t, s);
+    const float es = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    c = __fadd_rn(c, __fadd_rn(ep, es));
+    s = t;
+}
+
+template <typename Real, typename Acc, bool kMixed = false, bool kComp = false>
 __global__ void __launch_bounds__(kGramThreads)
     k_gram(const Cx<Real> *__restrict__ states, int n, const GramJob *__restrict__ jobs,
            const Collapse *__restrict__ col, std::size_t col_stride, int splits, std::uint64_t kchunk, int mode,
@@ -138,7 +166,7 @@ __global__ void __launch_bounds__(kGramThreads)
     __shared__ std::uint64_t roffA[TM], roffB[TM], crossA[TM], crossB[TM], elo[TK];
     __shared__ double red[kGramThreads / 32];
     __shared__ std::uint64_t s_fixed;
-    __shared__ int s_reduced, s_nenv;
+    __shared__ int s_reduced, s_nenv, s_check;
 
     const int tid = threadIdx.x;
     const int job = blockIdx.z;
@@ -155,22 +183,40 @@ __global__ void __launch_bounds__(kGramThreads)
         s_fixed = 0;
         s_reduced = 0;
         s_nenv = n - J.k;
-        if (compact && has_col && !J.fermion)
+        s_check = has_col ? 1 : 0;
+        if (compact && !J.fermion)
         {
-            const Collapse c0 = col[J.traj * col_stride];
-            if (c0.parity == 0 && c0.mask != 0)
+            Collapse c0{0, 0, 1.0, 0};
+            if (has_col) c0 = col[J.traj * col_stride];
+            const std::uint64_t drop = c0.parity == 0 ? c0.mask : 0ull;
+            const int kf = J.k;
+            int a = 0, e = 0;
+            for (int i = 0; i < kf; ++i)
+                if (!((drop >> J.kept[i]) & 1ull)) J.kept[a++] = J.kept[i];
+            for (int i = 0; i < n - kf; ++i)
+                if (!((drop >> J.env[i]) & 1ull)) J.env[e++] = J.env[i];
+            // The smaller side: M M^H and M^H M have the same non-zero
+            // spectrum (the pure state's Schmidt values), so the Gram runs over
+            // the environment when it has fewer modes left.
+            const bool swap = e < a;
+            if (swap)
             {
-                const int kf = J.k;
-                int a = 0, e = 0;
-                for (int i = 0; i < kf; ++i)
-                    if (!((c0.mask >> J.kept[i]) & 1ull)) J.kept[a++] = J.kept[i];
-                for (int i = 0; i < n - kf; ++i)
-                    if (!((c0.mask >> J.env[i]) & 1ull)) J.env[e++] = J.env[i];
+                std::int8_t t[32];
+                for (int i = 0; i < a; ++i) t[i] = J.kept[i];
+                for (int i = 0; i < e; ++i) J.kept[i] = J.env[i];
+                for (int i = 0; i < a; ++i) J.env[i] = t[i];
+                const int x = a;
+                a = e;
+                e = x;
+            }
+            if (drop != 0ull || swap)
+            {
                 J.k = a;
                 J.rows_fastest = (a > 0 && J.kept[0] == 0) ? 1 : 0;
                 s_nenv = e;
-                s_fixed = c0.value & c0.mask;
+                s_fixed = c0.value & drop;
                 s_reduced = 1;
+                if (drop != 0ull) s_check = 0;
             }
         }
         if (dims_out != nullptr && blockIdx.x == 0 && blockIdx.y == 0) dims_out[job] = 1 << J.k;
@@ -249,7 +295,7 @@ __global__ void __launch_bounds__(kGramThreads)
     }
     Collapse cl{0, 0, 1.0, 0};
     if (has_col) cl = col[J.traj * col_stride];
-    const bool check = has_col && !s_reduced;
+    const bool check = s_check != 0;
     const std::uint64_t fixed = s_fixed;
     __syncthreads();
 
@@ -259,10 +305,18 @@ __global__ void __launch_bounds__(kGramThreads)
     // columns, each run added to the FP64 totals (the reference's
     // mixed-precision sweep, cpp/include/mipt/cuda/reduce_sweep.cuh:59-96);
     // otherwise the products go straight into Acc.
+    // kComp (with kMixed): each FP32 run is a compensated dot product (its
+    // rounding errors carried in a second FP32 accumulator), accurate as if
+    // computed in twice the working precision, so runs can be 8 chunks (256
+    // columns) long: FP64-quality rho entries at the FP32 rate (ten FP32
+    // operations per product; GB300 runs FP32 about 64x faster than FP64).
     static_assert(!kMixed || (sizeof(Real) == 4 && sizeof(Acc) == 8), "mixed runs: FP32 states, FP64 totals");
+    static_assert(!kComp || kMixed, "compensated runs are FP32 runs");
     using Run = typename std::conditional<kMixed, float, Acc>::type;
+    constexpr int kRunChunks = kComp ? 8 : 2;
     Acc accr[4][4], acci[4][4];
     Run runr[4][4], runi[4][4];
+    Run cmpr[kComp ? 4 : 1][kComp ? 4 : 1], cmpi[kComp ? 4 : 1][kComp ? 4 : 1];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -270,6 +324,7 @@ __global__ void __launch_bounds__(kGramThreads)
         {
             accr[i][j] = acci[i][j] = Acc(0);
             runr[i][j] = runi[i][j] = Run(0);
+            if constexpr (kComp) cmpr[i][j] = cmpi[i][j] = Run(0);
         }
     int run_chunks = 0;
 
@@ -321,23 +376,42 @@ __global__ void __launch_bounds__(kGramThreads)
                 for (int j = 0; j < 4; ++j)
                 {
                     // a * conj(b)
-                    runr[i][j] = fma(Run(a[i].re), Run(b[j].re), runr[i][j]);
-                    runr[i][j] = fma(Run(a[i].im), Run(b[j].im), runr[i][j]);
-                    runi[i][j] = fma(Run(a[i].im), Run(b[j].re), runi[i][j]);
-                    runi[i][j] = fma(-Run(a[i].re), Run(b[j].im), runi[i][j]);
+                    if constexpr (kComp)
+                    {
+                        comp_fma(a[i].re, b[j].re, runr[i][j], cmpr[i][j]);
+                        comp_fma(a[i].im, b[j].im, runr[i][j], cmpr[i][j]);
+                        comp_fma(a[i].im, b[j].re, runi[i][j], cmpi[i][j]);
+                        comp_fma(-a[i].re, b[j].im, runi[i][j], cmpi[i][j]);
+                    }
+                    else
+                    {
+                        runr[i][j] = fma(Run(a[i].re), Run(b[j].re), runr[i][j]);
+                        runr[i][j] = fma(Run(a[i].im), Run(b[j].im), runr[i][j]);
+                        runi[i][j] = fma(Run(a[i].im), Run(b[j].re), runi[i][j]);
+                        runi[i][j] = fma(-Run(a[i].re), Run(b[j].im), runi[i][j]);
+                    }
                 }
         }
         if constexpr (kMixed)
         {
-            if (++run_chunks == 2 || e0 + TK >= eend)
+            if (++run_chunks == kRunChunks || e0 + TK >= eend)
             {
 #pragma unroll
                 for (int i = 0; i < 4; ++i)
 #pragma unroll
                     for (int j = 0; j < 4; ++j)
                     {
-                        accr[i][j] += static_cast<Acc>(runr[i][j]);
-                        acci[i][j] += static_cast<Acc>(runi[i][j]);
+                        if constexpr (kComp)
+                        {
+                            accr[i][j] += static_cast<Acc>(runr[i][j]) + static_cast<Acc>(cmpr[i][j]);
+                            acci[i][j] += static_cast<Acc>(runi[i][j]) + static_cast<Acc>(cmpi[i][j]);
+                            cmpr[i][j] = cmpi[i][j] = Run(0);
+                        }
+                        else
+                        {
+                            accr[i][j] += static_cast<Acc>(runr[i][j]);
+                            acci[i][j] += static_cast<Acc>(runi[i][j]);
+                        }
                         runr[i][j] = runi[i][j] = Run(0);
                     }
                 run_chunks = 0;
@@ -817,13 +891,29 @@ cudaError_t gram_rho(const Cx<Real> *states, int n, const GramJob *d_jobs, int n
     const std::uint64_t kchunk = (E + splits - 1) / splits;
     dim3 grid(gram_tiles(k), splits, njobs);
     const int compact = measured_compact_enabled() ? 1 : 0;
-    // Exact FP64 sums of the (exact) products: rho feeds -lambda log lambda,
-    // and FP32 runs of 64 products left about 5e-7 relative error in its
-    // entries, which moved the S_vN of near-pure reduced states by up to
-    // 2e-5 at n = 20 (the measured-site reduction keeps the FP64 work small).
-    k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits, kchunk,
-                                                       0, static_cast<double *>(scratch), nullptr, compact,
-                                                       dims_out);
+    // rho feeds -lambda log lambda: plain FP32 runs of 64 products left
+    // about 5e-7 relative error in its entries, which moved the S_vN of
+    // near-pure reduced states by up to 2e-5 at n = 20. FP32 states sum in
+    // compensated FP32 runs (FP64-quality entries at the FP32 rate), FP64
+    // states exactly in FP64.
+    // Compensated runs (rho entries to about 1e-13 of their scale) for tall
+    // Grams (environment >= 64x the kept dimension), where the Gram's work
+    // dominates; exact FP64 sums otherwise: their entries are cleaner, and the
+    // QL sweeps, which dominate square Grams, resolve fewer noise-level
+    // eigenvalues (half-chain spectra of L = 16 and 18: 1.7x faster QL).
+    bool comp = false;
+    if constexpr (sizeof(Real) == 4) comp = compensated_rho_sums() && n - k >= k + 6;
+    if (comp)
+    {
+        if constexpr (sizeof(Real) == 4)
+            k_gram<Real, double, true, true><<<grid, kGramThreads, 0, s>>>(
+                states, n, d_jobs, collapse, collapse_stride, splits, kchunk, 0, static_cast<double *>(scratch),
+                nullptr, compact, dims_out);
+    }
+    else
+        k_gram<Real, double><<<grid, kGramThreads, 0, s>>>(states, n, d_jobs, collapse, collapse_stride, splits,
+                                                           kchunk, 0, static_cast<double *>(scratch), nullptr,
+                                                           compact, dims_out);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const int d = 1 << k;
@@ -1522,6 +1612,18 @@ __global__ void k_compact_jobs(const GramJob *__restrict__ jobs, int njobs, int 
         if (!((drop >> J.kept[i]) & 1ull)) c.kpos[kq++] = J.kept[i];
     for (int i = 0; i < n - k; ++i)
         if (!((drop >> J.env[i]) & 1ull)) c.epos[eq++] = J.env[i];
+    // The smaller side (same purity from M^H M), when the kept modes left
+    // fit the operand rows' chunks of environment columns (kq <= n - k).
+    if (compact && !J.fermion && eq < kq && kq <= n - k)
+    {
+        std::int8_t t[16];
+        for (int i = 0; i < kq; ++i) t[i] = c.kpos[i];
+        for (int i = 0; i < eq; ++i) c.kpos[i] = c.epos[i];
+        for (int i = 0; i < kq; ++i) c.epos[i] = t[i];
+        const int x = kq;
+        kq = eq;
+        eq = x;
+    }
     c.kq = kq;
     c.eq = eq;
     out[j] = c;
