@@ -21,7 +21,8 @@ plain_fp64: the plain FP64 path, one trajectory per launch sequence,
 gram  : the final S_2 Gram's time and algorithmic flops. The entropies are
         taken with the last layer's collapse pending, so each trajectory's
         Gram covers only the rows and columns outside its measured sites
-        (the state is a product on them); the flops count that block.
+        (the state is a product on them), formed over the smaller side; the
+        flops count that block.
 The reference arm times the CPU FP64 oracle on the host cores.
 """
 import argparse
@@ -340,13 +341,16 @@ def run_gb300(args):
         # Final half-chain S_2: tensor-core Gram of each trajectory's block
         # without the sites its last layer measured (the state is a product
         # on them): d_A' = 2^(12 - measured sites among 0..11), d_B' likewise
-        # for 12..23, 4 d_A'^2 d_B' real flops for the Hermitian half.
+        # for 12..23. The Gram runs over the smaller side (same purity), so
+        # 4 min(d_A', d_B')^2 max(d_A', d_B') real flops for the Hermitian half.
         obs_ms = stats["observables"][0]
         half = N_QUBITS // 2
         last = np.asarray(out["measured"])[:, -1].astype(np.uint64)
         lo_meas = np.array([bin(int(m) & ((1 << half) - 1)).count("1") for m in last])
         hi_meas = np.array([bin(int(m) >> half).count("1") for m in last])
-        gram_flops = float(np.sum(4.0 * 2.0 ** (2 * (half - lo_meas)) * 2.0 ** (half - hi_meas)))
+        small = np.minimum(half - lo_meas, half - hi_meas)
+        large = np.maximum(half - lo_meas, half - hi_meas)
+        gram_flops = float(np.sum(4.0 * 2.0 ** (2 * small) * 2.0 ** large))
         full_flops = B * 4.0 * float(1 << half) ** 3
         gram = {"kernel": "k_tf32_rows + k_gram_tc_pre (tcgen05 3xTF32, TMA-fed)", "ms_per_step": obs_ms,
                 "alg_tflops": gram_flops / (obs_ms / 1000.0) / 1e12 if obs_ms > 0 else None,
